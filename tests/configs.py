@@ -1,0 +1,52 @@
+"""Workload definitions shared by the tests (frames and channels of the named workloads)."""
+
+import numpy as np
+
+from oracle import fading as ofad
+from oracle.frame import DATA, REFERENCE, FrameSpec, Resource, Section
+
+
+def siso_frame(order: int = 16) -> FrameSpec:
+    """SISO 256-point frame: 200 used subcarriers, CP 18, 14 words, comb pilots on
+    every 4th subcarrier of words 0 and 7."""
+
+    N, U, CP = 256, 200, 18
+    res = [Resource(1, CP / N, [(DATA, U)]), Resource(U // 4, CP / N, [(REFERENCE, 1), (DATA, 3)])]
+    return FrameSpec(N, res, [Section(1, [1, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0])], order, True)
+
+
+def mimo_frame(order: int = 64) -> FrameSpec:
+    """1024-point frame: 600 used data subcarriers, CP 72, 14 words."""
+
+    N, U, CP = 1024, 600, 72
+    return FrameSpec(N, [Resource(1, CP / N, [(DATA, U)])], [Section(14, [0])], order, True)
+
+
+# name: (delays [samples], power, rice, S, doppler, los_doppler, gain, Nrx, Ntx, T, fs)
+FADING_CASES = {
+    "c1": (np.arange(6), 10 ** (-0.3 * np.arange(6)), np.zeros(6), 20, 100.0, None, 1.0, 1, 1, 3836, 15.36e6),
+    "c2": (np.rint(np.arange(23) * 50e-9 * 30.72e6), 10 ** (-0.04 * np.arange(23)), np.zeros(23), 20, 500.0,
+           None, 1.0, 4, 4, 3000, 30.72e6),
+    "fast": (np.array([0, 3, 7, 19]), np.array([1.0, 0.5, 0.3, 0.1]), np.array([0.0, 1.0, 0.0, 2.0]), 5,
+             50 * 1e6, 20 * 1e6, 0.987, 2, 3, 700, 1e6),
+    "los": (np.array([0, 2]), np.array([1.0, 0.2]), np.array([np.inf, 3.0]), 7, 1e5, 3e4, 1.0, 1, 2, 500, 1e6),
+}
+
+
+def fading_case(name):
+    d, p, k, S, fd, flos, g, nrx, ntx, T, fs = FADING_CASES[name]
+    cfg = ofad.FadingConfig(np.asarray(d, float) / fs, p, k, S, fd, flos, g)
+    return cfg, nrx, ntx, T, fs
+
+
+def siso_channel(fs: float = 15.36e6) -> ofad.FadingConfig:
+    """6 taps at 0..5 samples, 3 dB/tap decay, 20 sinusoids, 100 Hz Doppler (Rayleigh)."""
+
+    return ofad.FadingConfig(np.arange(6) / fs, 10 ** (-0.3 * np.arange(6)), np.zeros(6), 20, 100.0)
+
+
+def mimo_channel(fs: float = 30.72e6) -> ofad.FadingConfig:
+    """23 taps at k*50 ns with -0.4k dB power, 20 sinusoids, 500 Hz Doppler (Rayleigh)."""
+
+    k = np.arange(23)
+    return ofad.FadingConfig(k * 50e-9, 10 ** (-0.04 * k), np.zeros(23), 20, 500.0)

@@ -1,0 +1,393 @@
+"""Generate the golden fixtures of the HermesPy reference (run where its source is available).
+
+Usage:  python tests/golden/make_golden.py [path-to-hermespy-checkout]
+
+Every fixture is an output of the reference's own code, fed inputs that the
+oracle can reproduce (seeded numpy draws or the engine's Philox streams):
+
+qam.npz      ``PskQamMapping.get_symbols`` / ``get_mapping`` / ``detect_bits`` for
+             BPSK, QPSK, 16-, 64-, 256-QAM, including decision-boundary ties.
+ofdm.npz     ``OFDMWaveform.place`` + ``modulate`` and ``demodulate`` for the SISO
+             256/200 comb-pilot frame and the 1024/600 data-only frame.
+fading.npz   ``MultipathFadingSample.propagate`` and ``.state`` for samples built
+             from explicit angles/phases (low Doppler, high Doppler, 2x3 MIMO, LOS).
+ls.npz       ``OrthogonalLeastSquaresChannelEstimation.estimate_channel`` on the
+             comb-pilot frame.
+ideal.npz    ``OFDMIdealChannelEstimation.estimate_channel`` for a 2x2 sample.
+zf.npz       ``ZeroForcingChannelEqualization.equalize_channel``, SISO and 4x4.
+ber.npz      ``BitErrorEvaluator.evaluate`` including unequal-length padding.
+drops.npz    Whole ``SimulationScenario.drop()`` runs (SISO LS+ZF at three Eb/N0,
+             2x2 ideal CSI + ZF) with bits, fading draws and noise injected from
+             the engine's Philox streams.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+from types import SimpleNamespace
+from unittest.mock import patch
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(HERE))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import refimport  # noqa: E402
+
+REF = sys.argv[1] if len(sys.argv) > 1 else refimport.DEFAULT_REFERENCE
+refimport.import_reference(REF)
+
+from scipy.stats import norm  # noqa: E402
+
+from hermespy.channel import MultipathFadingChannel  # noqa: E402
+from hermespy.channel.channel import LinkState  # noqa: E402
+from hermespy.channel.consistent import StaticConsistentRealization  # noqa: E402
+from hermespy.channel.fading.fading import MultipathFadingSample  # noqa: E402
+from hermespy.core import Signal  # noqa: E402
+from hermespy.modem import (  # noqa: E402
+    BitErrorEvaluator,
+    ElementType,
+    GridElement,
+    GridResource,
+    OFDMWaveform,
+    OrthogonalLeastSquaresChannelEstimation,
+    OrthogonalZeroForcingChannelEqualization,
+    PskQamMapping,
+    SimplexLink,
+    StatedSymbols,
+    Symbols,
+    SymbolSection,
+)
+from hermespy.modem.bits_source import BitsSource  # noqa: E402
+from hermespy.modem.waveform import ZeroForcingChannelEqualization  # noqa: E402
+from hermespy.simulation import AWGN, OFDMIdealChannelEstimation, SimulationScenario  # noqa: E402
+from hermespy.simulation.modem.noise import EBN0  # noqa: E402
+from hermespy.simulation.rf.noise.model import AWGNRealization  # noqa: E402
+from hermespy.simulation import SimulatedUniformArray, SimulatedIdealAntenna  # noqa: E402
+
+from oracle import fading as ofad  # noqa: E402
+from oracle import streams  # noqa: E402
+
+OUT = HERE
+
+
+def save(name: str, **arrays) -> None:
+    path = os.path.join(OUT, name)
+    np.savez_compressed(path, **arrays)
+    print(f"wrote {path} ({os.path.getsize(path) // 1024} KiB)")
+
+
+# ----------------------------------------------------------------------------- frames
+def c1_waveform(order: int = 16) -> OFDMWaveform:
+    """SISO 256-point frame: 200 used subcarriers, CP 18, 14 words, comb pilots
+    on every 4th subcarrier of words 0 and 7."""
+
+    N, U, CP = 256, 200, 18
+    res = [
+        GridResource(1, prefix_ratio=CP / N, elements=[GridElement(ElementType.DATA, U)]),
+        GridResource(U // 4, prefix_ratio=CP / N,
+                     elements=[GridElement(ElementType.REFERENCE, 1), GridElement(ElementType.DATA, 3)]),
+    ]
+    struct = [SymbolSection(1, [1, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0])]
+    return OFDMWaveform(grid_resources=res, grid_structure=struct, num_subcarriers=N, modulation_order=order)
+
+
+def c2_waveform(order: int = 64) -> OFDMWaveform:
+    """1024-point frame: 600 used data subcarriers, CP 72, 14 words."""
+
+    N, U, CP = 1024, 600, 72
+    res = [GridResource(1, prefix_ratio=CP / N, elements=[GridElement(ElementType.DATA, U)])]
+    struct = [SymbolSection(14, [0])]
+    return OFDMWaveform(grid_resources=res, grid_structure=struct, num_subcarriers=N, modulation_order=order)
+
+
+# ----------------------------------------------------------------------------- QAM
+def make_qam() -> None:
+    rng = np.random.default_rng(7)
+    out = {}
+    for M in (2, 4, 16, 64, 256):
+        m = PskQamMapping(M)
+        k = int(np.log2(M))
+        idx = np.arange(M)
+        bits = ((idx[:, None] >> (k - 1 - np.arange(k))[None, :]) & 1).astype(np.uint8).reshape(-1)
+        out[f"bits_{M}"] = bits
+        out[f"symbols_{M}"] = m.get_symbols(bits)
+        out[f"mapping_{M}"] = m.get_mapping()
+        pam_scale = {2: 1.0, 4: 1.0, 16: np.sqrt(5), 64: np.sqrt(21), 256: np.sqrt(85)}[M]
+        ties = np.arange(-18, 19) / np.sqrt(2) / pam_scale
+        pts = np.concatenate([
+            (rng.standard_normal(1000) + 1j * rng.standard_normal(1000)) * 0.9,
+            ties + 1j * ties[::-1],
+            np.nextafter(ties, np.inf) + 1j * np.nextafter(ties, -np.inf),
+            np.array([0.0, np.nan, np.inf, -np.inf, 1e-300]) + 0j,
+        ])
+        with np.errstate(invalid="ignore"):
+            out[f"detect_in_{M}"] = pts
+            out[f"detect_out_{M}"] = m.detect_bits(pts).astype(np.uint8)
+    save("qam.npz", **out)
+
+
+# ----------------------------------------------------------------------------- OFDM
+def ofdm_rx_distortion(x: np.ndarray) -> np.ndarray:
+    """Deterministic stand-in for a channel so that the fixture needs no received samples."""
+
+    return np.roll(x, 3) + 0.5 * x
+
+
+def make_ofdm() -> None:
+    rng = np.random.default_rng(11)
+    out = {}
+    for name, wf in (("c1", c1_waveform()), ("c2", c2_waveform())):
+        data = ((rng.standard_normal(wf.num_data_symbols) + 1j * rng.standard_normal(wf.num_data_symbols))
+                / np.sqrt(2)).astype(np.complex64).astype(np.complex128)
+        placed = wf.place(Symbols(data[None, :, None]))
+        x = wf.modulate(placed, 1.0, 1)
+        rx = ofdm_rx_distortion(x)
+        grid = wf.demodulate(rx, 1.0, 1).raw[0]
+        # The 1024-point frame repeats one resource per word, so its first words pin it;
+        # keep the fixture small by storing those only.
+        keep_words = 14 if name == "c1" else 3
+        keep_samples = keep_words * wf.samples_per_frame(1.0, 1) // wf.words_per_frame
+        out[f"{name}_data"] = data
+        out[f"{name}_placed"] = placed.raw[0][:keep_words]
+        out[f"{name}_x"] = x[:keep_samples]
+        out[f"{name}_grid"] = grid[:keep_words]
+        out[f"{name}_mask"] = wf.resource_mask
+        out[f"{name}_samples_per_frame"] = wf.samples_per_frame(1.0, 1)
+        # DC suppression off
+        wf.dc_suppression = False
+        out[f"{name}_x_nodc"] = wf.modulate(placed, 1.0, 1)[:keep_samples]
+        out[f"{name}_grid_nodc"] = wf.demodulate(rx, 1.0, 1).raw[0][:keep_words]
+    save("ofdm.npz", **out)
+
+
+# ----------------------------------------------------------------------------- fading
+def _state(num_tx: int, num_rx: int, fs: float):
+    sc = SimulationScenario(seed=1)
+    tx = sc.new_device(carrier_frequency=0.0, bandwidth=fs, oversampling_factor=1,
+                       antennas=SimulatedUniformArray(SimulatedIdealAntenna, 0.01, [num_tx, 1, 1]))
+    rx = sc.new_device(carrier_frequency=0.0, bandwidth=fs, oversampling_factor=1,
+                       antennas=SimulatedUniformArray(SimulatedIdealAntenna, 0.01, [num_rx, 1, 1]))
+    return LinkState(tx.state(0.0), rx.state(0.0), 0.0, fs, 0.0)
+
+
+def ref_sample(cfg: ofad.FadingConfig, smp: ofad.FadingSample, fs: float) -> MultipathFadingSample:
+    los_g, nlos_g = cfg.gains()
+    num_rx, num_tx = smp.spatial.shape
+    return MultipathFadingSample(
+        cfg.power_profile, cfg.delays, smp.los_angles, smp.nlos_angles, smp.los_phases, smp.nlos_phases,
+        los_g, nlos_g, cfg.los_doppler, cfg.doppler_frequency, smp.spatial, cfg.gain,
+        _state(num_tx, num_rx, fs))
+
+
+from configs import FADING_CASES  # noqa: E402  (shared with the tests)
+
+
+def make_fading() -> None:
+    out = {}
+    rng = np.random.default_rng(5)
+    for name, (d, p, k, S, fd, flos, g, nrx, ntx, T, fs) in FADING_CASES.items():
+        cfg = ofad.FadingConfig(np.asarray(d, float) / fs, p, k, S, fd, flos, g)
+        smp = ofad.realize(cfg, seed=1234, drop=3, num_rx=nrx, num_tx=ntx)
+        ref = ref_sample(cfg, smp, fs)
+        x = ((rng.standard_normal((ntx, T)) + 1j * rng.standard_normal((ntx, T))) / np.sqrt(2)
+             ).astype(np.complex64).astype(np.complex128)
+        sig = Signal.Create(x, fs, 0.0)
+        y = np.array(ref.propagate(sig).view(np.ndarray))
+        out[f"{name}_x"] = x
+        out[f"{name}_y"] = y
+        Ts = min(T, 96)
+        out[f"{name}_state"] = ref.state(Ts, Ts).dense_state()[:2, :2]
+    save("fading.npz", **out)
+
+
+# ----------------------------------------------------------------------------- LS
+def make_ls() -> None:
+    wf = c1_waveform()
+    wf.channel_estimation = OrthogonalLeastSquaresChannelEstimation()
+    rng = np.random.default_rng(13)
+    grid = rng.standard_normal((14, 256)) + 1j * rng.standard_normal((14, 256))
+    est = wf.channel_estimation.estimate_channel(Symbols(grid[None]), 1.0, 1)
+    save("ls.npz", grid=grid, estimate=np.asarray(est.dense_states())[0, 0])
+
+
+# ----------------------------------------------------------------------------- ideal CSI
+def make_ideal() -> None:
+    fs = 30.72e6
+    d, p, k, S, fd, flos, g, nrx, ntx, T, _ = FADING_CASES["c2"]
+    cfg = ofad.FadingConfig(np.asarray(d, float) / fs, p, k, S, fd, flos, g)
+    smp = ofad.realize(cfg, seed=99, drop=7, num_rx=2, num_tx=2)
+    ref = ref_sample(cfg, smp, fs)
+    wf = c2_waveform()
+    est = OFDMIdealChannelEstimation.__new__(OFDMIdealChannelEstimation)
+    est.reference_position = None
+    est._IdealChannelEstimation__cached_sample = ref
+    with patch.object(type(est), "waveform", new=wf):
+        syms = Symbols(np.zeros((2, 14, 1024), complex))
+        out = est.estimate_channel(syms, fs, 1)
+    # words 0, 5, 10 of the (2, 2, 14, 1024) state keep the fixture small
+    save("ideal.npz", csi=np.asarray(out.dense_states())[:, :, ::5, :])
+
+
+# ----------------------------------------------------------------------------- ZF
+def make_zf() -> None:
+    rng = np.random.default_rng(17)
+    eq = ZeroForcingChannelEqualization()
+    out = {}
+    for nrx, ntx, name in ((1, 1, "siso"), (4, 4, "mimo")):
+        y = rng.standard_normal((nrx, 50, 1)) + 1j * rng.standard_normal((nrx, 50, 1))
+        h = rng.standard_normal((nrx, ntx, 50, 1)) + 1j * rng.standard_normal((nrx, ntx, 50, 1))
+        res = eq.equalize_channel(StatedSymbols(y, h))
+        out[f"{name}_y"], out[f"{name}_h"], out[f"{name}_x"] = y[..., 0], h[..., 0], res.raw[..., 0]
+    save("zf.npz", **out)
+
+
+# ----------------------------------------------------------------------------- BER
+def make_ber() -> None:
+    rng = np.random.default_rng(19)
+    ev = BitErrorEvaluator.__new__(BitErrorEvaluator)
+    out = {}
+    for i, (nt, nr) in enumerate(((500, 500), (480, 500), (500, 470))):
+        a = rng.integers(0, 2, nt).astype(np.uint8)
+        b = rng.integers(0, 2, nr).astype(np.uint8)
+        b[: min(nt, nr) // 2] = a[: min(nt, nr) // 2]
+        with patch.object(BitErrorEvaluator, "_fetch_dsp_results",
+                          return_value=(SimpleNamespace(bits=a), SimpleNamespace(bits=b))):
+            e = ev.evaluate()
+        out[f"tx_{i}"], out[f"rx_{i}"] = a, b
+        out[f"errors_{i}"] = np.asarray(e.evaluation)
+        out[f"ber_{i}"] = e.artifact().to_scalar()
+    save("ber.npz", **out)
+
+
+# ----------------------------------------------------------------------------- full drops
+class InjectedBits(BitsSource):
+    """Bits source returning the engine's Philox bits for the current drop."""
+
+    def __init__(self, seed, num_streams):
+        BitsSource.__init__(self)
+        self.seed, self.num_streams, self.drop = seed, num_streams, 0
+
+    def generate_bits(self, num_bits):
+        per = num_bits // self.num_streams
+        return np.concatenate([streams.data_bits(self.seed, self.drop, s, per) for s in range(self.num_streams)])
+
+    def serialize(self, process):
+        pass
+
+
+class InjectedNoise(AWGN):
+    """Noise model adding the engine's Philox AWGN for the current drop."""
+
+    def __init__(self, seed):
+        AWGN.__init__(self)
+        self.inj_seed, self.drop = seed, 0
+
+    def realize(self, power):
+        model = self
+
+        class _R(AWGNRealization):
+            def add_to(self, signal):
+                if self.power == 0.0:
+                    return signal
+                noisy = signal.copy()
+                arr = noisy.view(np.ndarray)
+                n = streams.awgn(model.inj_seed, model.drop, arr.shape[0], arr.shape[1], self.power)
+                for block in noisy.blocks:
+                    block += n
+                noisy.noise_power = self.power
+                return noisy
+
+        return _R(power, 0)
+
+
+def _drop_scenario(wf, cfg: ofad.FadingConfig, fs, num_tx, num_rx, seed, ideal):
+    sc = SimulationScenario(seed=3)
+    tx = sc.new_device(carrier_frequency=0.0, bandwidth=fs, oversampling_factor=1,
+                       antennas=SimulatedUniformArray(SimulatedIdealAntenna, 0.01, [num_tx, 1, 1]))
+    rx = sc.new_device(carrier_frequency=0.0, bandwidth=fs, oversampling_factor=1,
+                       antennas=SimulatedUniformArray(SimulatedIdealAntenna, 0.01, [num_rx, 1, 1]))
+    link = SimplexLink()
+    tx.transmitters.add(link)
+    rx.receivers.add(link)
+    ch = MultipathFadingChannel(cfg.delays, cfg.power_profile, cfg.rice_factors,
+                                num_sinusoids=cfg.num_sinusoids, doppler_frequency=cfg.doppler_frequency)
+    sc.set_channel(tx, rx, ch)
+    if ideal:
+        wf.channel_estimation = OFDMIdealChannelEstimation(ch, tx, rx)
+    else:
+        wf.channel_estimation = OrthogonalLeastSquaresChannelEstimation()
+    wf.channel_equalization = OrthogonalZeroForcingChannelEqualization()
+    link.waveform = wf
+    bits = InjectedBits(seed, num_tx)
+    link.bits_source = bits
+    noise = InjectedNoise(seed)
+    rx.noise_model = noise
+    tx.noise_model = InjectedNoise(seed + 1)
+    ber = BitErrorEvaluator(link, link)
+    return sc, ch, link, rx, bits, noise, ber
+
+
+def _inject_fading(ch, cfg, seed, drop, num_rx, num_tx):
+    """Route the engine's fading uniforms through the reference's own variables."""
+
+    L, S = cfg.num_taps, cfg.num_sinusoids
+    u = streams.fading_uniforms(seed, drop, cfg.num_draws(num_rx, num_tx))
+    ref_u = np.full(100 + 2 * L * (1 + S), 0.5)
+    # SimulationScenario.propagate (simulation/scenario.py:575-609) samples the link
+    # (device 1 -> device 0) and serves device 0 -> device 1 with its reciprocal, whose
+    # spatial response is the transpose: entry [rx, tx] comes from variable entry [tx, rx].
+    sp = np.full((10, 10), 0.5)
+    sp[:num_tx, :num_rx] = u[: num_rx * num_tx].reshape(num_rx, num_tx).T
+    ref_u[:100] = sp.reshape(-1)
+    ref_u[100:] = u[num_rx * num_tx:]
+    scalars = norm.ppf(ref_u)
+    gen = ch._MultipathFadingChannel__rng
+    gen.realize = lambda distance, *a, **k: StaticConsistentRealization(scalars)
+
+
+def make_drops() -> None:
+    out = {}
+    seed = 20240611
+    fs = 15.36e6
+    cfg = ofad.FadingConfig(np.arange(6) / fs, 10 ** (-0.3 * np.arange(6)), np.zeros(6), 20, 100.0)
+    for i, (drop, ebn0_db) in enumerate(((0, 0.0), (1, 10.0), (2, 20.0))):
+        wf = c1_waveform()
+        sc, ch, link, rx, bits, noise, ber = _drop_scenario(wf, cfg, fs, 1, 1, seed, ideal=False)
+        rx.noise_level = EBN0(link, 10 ** (ebn0_db / 10))
+        bits.drop = noise.drop = drop
+        _inject_fading(ch, cfg, seed, drop, 1, 1)
+        dr = sc.drop()
+        e = ber.evaluate()
+        out[f"c1_{i}_drop"], out[f"c1_{i}_ebn0_db"] = drop, ebn0_db
+        out[f"c1_{i}_errors"] = int(np.sum(e.evaluation))
+        out[f"c1_{i}_rx_bits"] = np.packbits(dr.device_receptions[1].operator_receptions[0].bits)
+    # 2x2 ideal CSI + ZF on the 1024/600 frame with 23 taps
+    fs2 = 30.72e6
+    d, p, k, S, fd, flos, g, _, _, _, _ = FADING_CASES["c2"]
+    cfg2 = ofad.FadingConfig(np.asarray(d, float) / fs2, p, k, S, fd, flos, g)
+    wf = c2_waveform(16)
+    sc, ch, link, rx, bits, noise, ber = _drop_scenario(wf, cfg2, fs2, 2, 2, seed, ideal=True)
+    rx.noise_level = EBN0(link, 10 ** (15 / 10))
+    bits.drop = noise.drop = 5
+    _inject_fading(ch, cfg2, seed, 5, 2, 2)
+    dr = sc.drop()
+    e = ber.evaluate()
+    out["c2_errors"] = int(np.sum(e.evaluation))
+    out["c2_rx_bits"] = np.packbits(dr.device_receptions[1].operator_receptions[0].bits)
+    out["seed"] = seed
+    save("drops.npz", **out)
+
+
+if __name__ == "__main__":
+    make_qam()
+    make_ofdm()
+    make_fading()
+    make_ls()
+    make_ideal()
+    make_zf()
+    make_ber()
+    make_drops()
