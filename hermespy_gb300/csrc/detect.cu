@@ -1,0 +1,504 @@
+// Channel estimation (LS), per-element equalization (ZF / LMMSE) and the fused
+// receivers that end in bit-error counts.
+#include "fading_dev.cuh"
+
+struct hpx_ls {
+  const hpx_frame* frame;
+  int C;          // columns of the estimate
+  int nnz;
+  int32_t* d_indptr = nullptr;   // [W*C + 1]
+  int32_t* d_indices = nullptr;  // [nnz] reference index
+  float* d_weights = nullptr;    // [nnz]
+  int32_t* d_ref_word = nullptr;    // [num_refs]
+  int32_t* d_ref_column = nullptr;  // [num_refs]
+};
+
+namespace {
+
+// --------------------------------------------------------------- solvers
+
+// Cholesky solve of the Hermitian positive definite A x = b (lower triangle of A
+// used and overwritten). Returns false if a pivot is not positive.
+template <int n>
+__device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], float2 (&x)[n]) {
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < n; ++j) {
+    float d = A[j][j].x;
+#pragma unroll
+    for (int k = 0; k < j; ++k) d -= A[j][k].x * A[j][k].x + A[j][k].y * A[j][k].y;
+    ok = ok && (d > 0.0f);
+    const float ljj = sqrtf(d);
+    const float inv = 1.0f / ljj;
+    A[j][j] = make_float2(ljj, 0.f);
+#pragma unroll
+    for (int i = j + 1; i < n; ++i) {
+      float2 s = A[i][j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) {
+        // s -= A[i][k] * conj(A[j][k])
+        s.x -= A[i][k].x * A[j][k].x + A[i][k].y * A[j][k].y;
+        s.y -= A[i][k].y * A[j][k].x - A[i][k].x * A[j][k].y;
+      }
+      A[i][j] = cscale(s, inv);
+    }
+  }
+  float2 z[n];
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+    float2 s = b[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) s = csub(s, cmul(A[i][k], z[k]));
+    z[i] = cscale(s, 1.0f / A[i][i].x);
+  }
+#pragma unroll
+  for (int i = n - 1; i >= 0; --i) {
+    float2 s = z[i];
+#pragma unroll
+    for (int k = i + 1; k < n; ++k) s = csub(s, cmulc(A[k][i], x[k]));
+    x[i] = cscale(s, 1.0f / A[i][i].x);
+  }
+  return ok;
+}
+
+// Equalize one resource element. Returns the number of output streams
+// (1 for ZF with a single receive antenna, which divides by sum_tx h like the
+// reference, NTX otherwise).
+template <int NRX, int NTX>
+__device__ __forceinline__ void equalize_one(int mode, const float2 (&H)[NRX][NTX], const float2 (&y)[NRX], float s2,
+                                             float2 (&x)[NTX]) {
+  if (mode == HPX_EQ_ZF && NRX == 1) {
+    float2 hs = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int t = 0; t < NTX; ++t) hs = cadd(hs, H[0][t]);
+    // complex division y / hs (numpy semantics: inf/nan for hs == 0)
+    const float den = hs.x * hs.x + hs.y * hs.y;
+    x[0] = make_float2((y[0].x * hs.x + y[0].y * hs.y) / den, (y[0].y * hs.x - y[0].x * hs.y) / den);
+#pragma unroll
+    for (int t = 1; t < NTX; ++t) x[t] = make_float2(0.f, 0.f);
+    return;
+  }
+  const float reg = mode == HPX_EQ_LMMSE ? s2 : 0.0f;
+  if (mode == HPX_EQ_ZF && NRX < NTX) {
+    // minimum-norm pseudo-inverse: x = H^H (H H^H)^-1 y
+    float2 A[NRX][NRX], yy[NRX], w[NRX];
+#pragma unroll
+    for (int i = 0; i < NRX; ++i) {
+      yy[i] = y[i];
+#pragma unroll
+      for (int j = 0; j <= i; ++j) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < NTX; ++t) cfma(acc, H[i][t], cconj(H[j][t]));
+        A[i][j] = acc;
+      }
+    }
+    if (!chol_solve<NRX>(A, yy, w)) {
+#pragma unroll
+      for (int t = 0; t < NTX; ++t) x[t] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+      return;
+    }
+#pragma unroll
+    for (int t = 0; t < NTX; ++t) {
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int i = 0; i < NRX; ++i) cfmac(acc, H[i][t], w[i]);
+      x[t] = acc;
+    }
+    return;
+  }
+  float2 A[NTX][NTX], b[NTX];
+#pragma unroll
+  for (int i = 0; i < NTX; ++i) {
+    float2 mf = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < NRX; ++r) cfmac(mf, H[r][i], y[r]);
+    b[i] = mf;
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int r = 0; r < NRX; ++r) cfmac(acc, H[r][i], H[r][j]);  // (H^H H)[i][j] = sum_r conj(H[r][i]) H[r][j]
+      A[i][j] = acc;
+    }
+    A[i][i].x += reg;
+    A[i][i].y = 0.0f;
+  }
+  if (!chol_solve<NTX>(A, b, x)) {
+#pragma unroll
+    for (int t = 0; t < NTX; ++t) x[t] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+  }
+}
+
+template <int NRX, int NTX>
+__global__ void k_equalize(int mode, int64_t K, const float2* __restrict__ Hg, const float2* __restrict__ Yg,
+                           const float* __restrict__ nv, float2* __restrict__ Xg, int out_streams) {
+  const int b = blockIdx.y;
+  const float s2 = nv ? nv[b] : 0.0f;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K; k += (int64_t)gridDim.x * blockDim.x) {
+    float2 H[NRX][NTX], y[NRX], x[NTX];
+#pragma unroll
+    for (int r = 0; r < NRX; ++r) {
+      y[r] = Yg[((int64_t)b * NRX + r) * K + k];
+#pragma unroll
+      for (int t = 0; t < NTX; ++t) H[r][t] = Hg[(((int64_t)b * NRX + r) * NTX + t) * K + k];
+    }
+    equalize_one<NRX, NTX>(mode, H, y, s2, x);
+    for (int t = 0; t < out_streams; ++t) Xg[((int64_t)b * out_streams + t) * K + k] = x[t];
+  }
+}
+
+// Stage the packed Philox bits of data elements [k0, k0 + nd) of `nstreams`
+// streams in shared memory; returns the word offset to index with absolute
+// stream bit positions (words(s)[pos >> 5]).
+__device__ __forceinline__ void stage_bits(uint32_t* bitsm, int BW, int nstreams, uint64_t seed, int64_t drop, int64_t k0,
+                                           int nd, int m) {
+  if (nd <= 0) return;
+  const int64_t blk0 = ((k0 * m) >> 5) >> 2, blk1 = (((k0 + nd) * m - 1) >> 5) >> 2;
+  const int nblk = (int)(blk1 - blk0 + 1);
+  for (int q = threadIdx.x; q < nblk * nstreams; q += blockDim.x) {
+    const int s = q / nblk;
+    const int64_t blk = blk0 + (q - s * nblk);
+    const uint4 r = hpx_random_block(seed, drop, (uint32_t)s, HPX_DOMAIN_BITS, (uint32_t)blk);
+    uint32_t* dst = bitsm + s * BW + (blk - blk0) * 4;
+    dst[0] = r.x;
+    dst[1] = r.y;
+    dst[2] = r.z;
+    dst[3] = r.w;
+  }
+}
+
+__device__ __forceinline__ void block_count(unsigned int local, uint32_t* out) {
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+  __shared__ unsigned int warp_sums[32];
+  if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    unsigned int v = threadIdx.x < (blockDim.x >> 5) ? warp_sums[threadIdx.x] : 0u;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0 && v) atomicAdd(out, v);
+  }
+}
+
+constexpr int DTHREADS = 256;
+
+// Fused ideal-CSI receiver, one block per (word, drop).
+template <int NRX, int NTX>
+__global__ void __launch_bounds__(DTHREADS) k_detect_ideal(FadingConst fc, FadingView v, int N, int W, int C, int m,
+                                                           const int32_t* __restrict__ window_start,
+                                                           const int32_t* __restrict__ data_offset,
+                                                           const int32_t* __restrict__ num_data_word,
+                                                           const int32_t* __restrict__ data_column,
+                                                           const int32_t* __restrict__ bins,
+                                                           const float2* __restrict__ tw, QamDemapTable qt, int mode,
+                                                           const float2* __restrict__ grid, int gcols,
+                                                           const float* __restrict__ nv, uint64_t seed, int64_t drop0,
+                                                           uint32_t* __restrict__ errors) {
+  extern __shared__ float4 smem4[];
+  const int w = blockIdx.x, b = blockIdx.y;
+  const int BW = ((C * m) >> 5) + 8;
+  float2* hb = reinterpret_cast<float2*>(smem4);
+  float2* scratch = hb + fc.L;
+  float2* Sm = scratch + fc.L * fc.S1;
+  int* ds = reinterpret_cast<int*>(Sm + NRX * NTX);
+  uint32_t* bitsm = reinterpret_cast<uint32_t*>(ds + fc.L + 4);
+  const int64_t k0 = data_offset[w];
+  const int nd = num_data_word[w];
+  for (int l = threadIdx.x; l < fc.L; l += blockDim.x) ds[l] = fc.delay[l];
+  for (int i = threadIdx.x; i < NRX * NTX; i += blockDim.x) Sm[i] = v.spatial(b)[i];
+  stage_bits(bitsm, BW, NTX, seed, drop0 + b, k0, nd, m);
+  tap_averages(fc, v.W(b), v.P0(b), window_start[w], N, hb, scratch);  // contains __syncthreads
+  const int64_t wofs = (((k0 * m) >> 5) >> 2) * 4;
+  const float s2 = nv ? nv[b] : 0.0f;
+  const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
+  unsigned int local = 0;
+  for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+    const int64_t k = k0 + j;
+    const int c = data_column[k];
+    const float2 g = tap_response(fc, hb, ds, tw, bins[c], N);
+    float2 H[NRX][NTX], y[NRX], x[NTX];
+#pragma unroll
+    for (int r = 0; r < NRX; ++r) {
+      y[r] = grid[(((int64_t)b * NRX + r) * W + w) * gcols + c];
+#pragma unroll
+      for (int t = 0; t < NTX; ++t) H[r][t] = cmul(Sm[r * NTX + t], g);
+    }
+    equalize_one<NRX, NTX>(mode, H, y, s2, x);
+    for (int t = 0; t < NTX; ++t) {
+      // streams the equalizer does not return are received as zero bits
+      // (BitErrorEvaluator zero-pads the shorter sequence)
+      const uint32_t rx_v = t < out_streams ? qam_decide(qt, x[t]) : 0u;
+      const uint32_t tx_v = extract_bits_msb(bitsm + t * BW - wofs, k * m, m);
+      local += __popc(rx_v ^ tx_v);
+    }
+  }
+  block_count(local, errors + b);
+}
+
+// Fused SISO LS receiver, one block per (word, drop).
+__global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, const int32_t* __restrict__ data_offset,
+                                                        const int32_t* __restrict__ num_data_word,
+                                                        const int32_t* __restrict__ data_column,
+                                                        const int32_t* __restrict__ indptr,
+                                                        const int32_t* __restrict__ indices,
+                                                        const float* __restrict__ weights,
+                                                        const int32_t* __restrict__ ref_word,
+                                                        const int32_t* __restrict__ ref_column,
+                                                        const float2* __restrict__ pilots, QamDemapTable qt, int mode,
+                                                        const float2* __restrict__ grid, int gcols,
+                                                        const float* __restrict__ nv, uint64_t seed, int64_t drop0,
+                                                        uint32_t* __restrict__ errors) {
+  extern __shared__ float4 smem4[];
+  uint32_t* bitsm = reinterpret_cast<uint32_t*>(smem4);
+  const int w = blockIdx.x, b = blockIdx.y;
+  const int BW = ((C * m) >> 5) + 8;
+  const int64_t k0 = data_offset[w];
+  const int nd = num_data_word[w];
+  stage_bits(bitsm, BW, 1, seed, drop0 + b, k0, nd, m);
+  __syncthreads();
+  const int64_t wofs = (((k0 * m) >> 5) >> 2) * 4;
+  const float s2 = nv ? nv[b] : 0.0f;
+  const float2* gb = grid + (int64_t)b * W * gcols;
+  unsigned int local = 0;
+  for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+    const int64_t k = k0 + j;
+    const int c = data_column[k];
+    const int row = w * C + c;
+    float2 h = make_float2(0.f, 0.f);
+    for (int e = indptr[row]; e < indptr[row + 1]; ++e) {
+      const int p = indices[e];
+      const float2 yp = gb[ref_word[p] * gcols + ref_column[p]];
+      const float2 xp = pilots[p];
+      const float den = xp.x * xp.x + xp.y * xp.y;
+      const float2 ls = make_float2((yp.x * xp.x + yp.y * xp.y) / den, (yp.y * xp.x - yp.x * xp.y) / den);
+      h = cadd(h, cscale(ls, weights[e]));
+    }
+    float2 H[1][1] = {{h}}, y[1] = {gb[w * gcols + c]}, x[1];
+    equalize_one<1, 1>(mode, H, y, s2, x);
+    const uint32_t rx_v = qam_decide(qt, x[0]);
+    const uint32_t tx_v = extract_bits_msb(bitsm - wofs, k * m, m);
+    local += __popc(rx_v ^ tx_v);
+  }
+  block_count(local, errors + b);
+}
+
+__global__ void k_ls_estimate(int W, int C, const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                              const float* __restrict__ weights, const int32_t* __restrict__ ref_word,
+                              const int32_t* __restrict__ ref_column, const float2* __restrict__ pilots,
+                              const float2* __restrict__ grid, int gcols, float2* __restrict__ est) {
+  const int b = blockIdx.y;
+  const float2* gb = grid + (int64_t)b * W * gcols;
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < W * C; row += gridDim.x * blockDim.x) {
+    float2 h = make_float2(0.f, 0.f);
+    for (int e = indptr[row]; e < indptr[row + 1]; ++e) {
+      const int p = indices[e];
+      const float2 yp = gb[ref_word[p] * gcols + ref_column[p]];
+      const float2 xp = pilots[p];
+      const float den = xp.x * xp.x + xp.y * xp.y;
+      const float2 ls = make_float2((yp.x * xp.x + yp.y * xp.y) / den, (yp.y * xp.x - yp.x * xp.y) / den);
+      h = cadd(h, cscale(ls, weights[e]));
+    }
+    est[(int64_t)b * W * C + row] = h;
+  }
+}
+
+template <int NRX>
+hpx_status eq_dispatch_tx(int mode, int ntx, int64_t K, int B, const float2* H, const float2* Y, const float* nv,
+                          float2* X, cudaStream_t s) {
+  const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : ntx;
+  int gx = (int)((K + 255) / 256);
+  if (gx > 1024) gx = 1024;
+  dim3 grid(gx, B);
+  switch (ntx) {
+    case 1: k_equalize<NRX, 1><<<grid, 256, 0, s>>>(mode, K, H, Y, nv, X, out_streams); break;
+    case 2: k_equalize<NRX, 2><<<grid, 256, 0, s>>>(mode, K, H, Y, nv, X, out_streams); break;
+    case 4: k_equalize<NRX, 4><<<grid, 256, 0, s>>>(mode, K, H, Y, nv, X, out_streams); break;
+    case 8: k_equalize<NRX, 8><<<grid, 128, 0, s>>>(mode, K, H, Y, nv, X, out_streams); break;
+    default: return hpx_fail(HPX_ERR_UNSUPPORTED, "equalize: %d transmit streams not supported (1, 2, 4, 8)", ntx);
+  }
+  HPX_LAUNCHED("equalize");
+  return HPX_OK;
+}
+
+template <int NRX, int NTX>
+hpx_status launch_detect_ideal(const hpx_fading* f, const void* state, const hpx_frame* fr, int mode,
+                               const hpx_cf32* grid, int gcols, const float* nv, uint64_t seed, int64_t drop0, int B,
+                               uint32_t* errors, cudaStream_t s) {
+  QamDemapTable qt;
+  HPX_TRY(qam_demap_table(fr->info.modulation_order, &qt));
+  const FadingConst fc = fading_const(f);
+  const int C = fr->info.num_columns, m = fr->info.bits_per_symbol;
+  const int BW = ((C * m) >> 5) + 8;
+  const size_t smem = (size_t)fc.L * sizeof(float2) * (1 + fc.S1) + NRX * NTX * sizeof(float2) +
+                      (fc.L + 4) * sizeof(int) + (size_t)NTX * BW * 4 + 16;
+  auto kern = k_detect_ideal<NRX, NTX>;
+  if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid_dim(fr->info.num_words, B);
+  kern<<<grid_dim, DTHREADS, smem, s>>>(fc, fading_view(f, state), fr->info.num_subcarriers, fr->info.num_words, C, m,
+                                        fr->d_window_start, fr->d_data_offset, fr->d_num_data_word, fr->d_data_column,
+                                        fr->d_bins, fr->d_twiddle, qt, mode, reinterpret_cast<const float2*>(grid),
+                                        gcols, nv, seed, drop0, errors);
+  HPX_LAUNCHED("detect_ideal");
+  return HPX_OK;
+}
+
+template <int NRX>
+hpx_status detect_ideal_tx(int ntx, const hpx_fading* f, const void* state, const hpx_frame* fr, int mode,
+                           const hpx_cf32* grid, int gcols, const float* nv, uint64_t seed, int64_t drop0, int B,
+                           uint32_t* errors, cudaStream_t s) {
+  switch (ntx) {
+    case 1: return launch_detect_ideal<NRX, 1>(f, state, fr, mode, grid, gcols, nv, seed, drop0, B, errors, s);
+    case 2: return launch_detect_ideal<NRX, 2>(f, state, fr, mode, grid, gcols, nv, seed, drop0, B, errors, s);
+    case 4: return launch_detect_ideal<NRX, 4>(f, state, fr, mode, grid, gcols, nv, seed, drop0, B, errors, s);
+    case 8: return launch_detect_ideal<NRX, 8>(f, state, fr, mode, grid, gcols, nv, seed, drop0, B, errors, s);
+    default: return hpx_fail(HPX_ERR_UNSUPPORTED, "detect: %d transmit antennas not supported (1, 2, 4, 8)", ntx);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+hpx_status hpx_ls_create(const hpx_frame* frame, int32_t C, const int32_t* indptr, const int32_t* indices,
+                         const float* weights, hpx_ls** out) {
+  if (!frame || !out || !indptr) return hpx_fail(HPX_ERR_ARG, "ls: null argument");
+  *out = nullptr;
+  const int W = frame->info.num_words;
+  if (C < frame->info.num_columns || C > frame->info.num_subcarriers)
+    return hpx_fail(HPX_ERR_ARG, "ls: columns must cover the frame's resource columns");
+  if (frame->info.num_refs < 1) return hpx_fail(HPX_ERR_ARG, "ls: frame has no reference elements");
+  const int rows = W * C;
+  const int nnz = indptr[rows];
+  if (indptr[0] != 0 || nnz < 0) return hpx_fail(HPX_ERR_ARG, "ls: malformed table");
+  for (int r = 0; r < rows; ++r)
+    if (indptr[r + 1] < indptr[r]) return hpx_fail(HPX_ERR_ARG, "ls: malformed table");
+  for (int e = 0; e < nnz; ++e)
+    if (indices[e] < 0 || indices[e] >= frame->info.num_refs) return hpx_fail(HPX_ERR_ARG, "ls: index out of range");
+  std::vector<int32_t> rw, rc;
+  const int FC = frame->info.num_columns;
+  for (int w = 0; w < W; ++w)
+    for (int c = 0; c < FC; ++c)
+      if (frame->h_kind[(size_t)w * FC + c] == HPX_RE_REFERENCE) {
+        rw.push_back(w);
+        rc.push_back(c);
+      }
+  hpx_ls* ls = new hpx_ls();
+  ls->frame = frame;
+  ls->C = C;
+  ls->nnz = nnz;
+  auto up = [](void** dst, const void* src, size_t bytes) -> cudaError_t {
+    if (bytes == 0) {
+      *dst = nullptr;
+      return cudaSuccess;
+    }
+    cudaError_t e = cudaMalloc(dst, bytes);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+  };
+  cudaError_t e;
+  if ((e = up((void**)&ls->d_indptr, indptr, (rows + 1) * sizeof(int32_t))) != cudaSuccess ||
+      (e = up((void**)&ls->d_indices, indices, nnz * sizeof(int32_t))) != cudaSuccess ||
+      (e = up((void**)&ls->d_weights, weights, nnz * sizeof(float))) != cudaSuccess ||
+      (e = up((void**)&ls->d_ref_word, rw.data(), rw.size() * sizeof(int32_t))) != cudaSuccess ||
+      (e = up((void**)&ls->d_ref_column, rc.data(), rc.size() * sizeof(int32_t))) != cudaSuccess) {
+    hpx_ls_destroy(ls);
+    return hpx_cuda_status(e, "ls tables");
+  }
+  *out = ls;
+  return HPX_OK;
+}
+
+hpx_status hpx_ls_destroy(hpx_ls* ls) {
+  if (!ls) return HPX_OK;
+  void* p[] = {ls->d_indptr, ls->d_indices, ls->d_weights, ls->d_ref_word, ls->d_ref_column};
+  for (void* q : p)
+    if (q) cudaFree(q);
+  delete ls;
+  return HPX_OK;
+}
+
+hpx_status hpx_ls_estimate(const hpx_ls* ls, const hpx_cf32* grid, int32_t gcols, int32_t B, hpx_cf32* est,
+                           void* stream) {
+  if (!ls || !grid || !est) return hpx_fail(HPX_ERR_ARG, "ls_estimate: null argument");
+  if (B < 0) return hpx_fail(HPX_ERR_ARG, "ls_estimate: negative batch");
+  if (gcols < ls->frame->info.num_columns) return hpx_fail(HPX_ERR_SHAPE, "ls_estimate: grid too narrow");
+  if (B == 0) return HPX_OK;
+  if (B > 65535) return hpx_fail(HPX_ERR_ARG, "ls_estimate: batch too large");
+  const int W = ls->frame->info.num_words;
+  dim3 grid_dim((W * ls->C + 255) / 256, B);
+  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, ls->C, ls->d_indptr, ls->d_indices, ls->d_weights,
+                                                         ls->d_ref_word, ls->d_ref_column, ls->frame->d_pilots,
+                                                         reinterpret_cast<const float2*>(grid), gcols,
+                                                         reinterpret_cast<float2*>(est));
+  HPX_LAUNCHED("ls_estimate");
+  return HPX_OK;
+}
+
+hpx_status hpx_equalize(int32_t mode, int32_t nrx, int32_t ntx, int64_t K, int32_t B, const hpx_cf32* H,
+                        const hpx_cf32* Y, const float* nv, hpx_cf32* X, void* stream) {
+  if (mode != HPX_EQ_ZF && mode != HPX_EQ_LMMSE) return hpx_fail(HPX_ERR_ARG, "equalize: unknown mode %d", mode);
+  if (K < 0 || B < 0) return hpx_fail(HPX_ERR_ARG, "equalize: negative size");
+  if (K == 0 || B == 0) return HPX_OK;
+  if (!H || !Y || !X) return hpx_fail(HPX_ERR_ARG, "equalize: null buffer");
+  if (mode == HPX_EQ_LMMSE && !nv) return hpx_fail(HPX_ERR_ARG, "equalize: LMMSE needs noise variances");
+  if (B > 65535) return hpx_fail(HPX_ERR_ARG, "equalize: batch too large");
+  const float2* h = reinterpret_cast<const float2*>(H);
+  const float2* y = reinterpret_cast<const float2*>(Y);
+  float2* x = reinterpret_cast<float2*>(X);
+  cudaStream_t s = as_stream(stream);
+  switch (nrx) {
+    case 1: return eq_dispatch_tx<1>(mode, ntx, K, B, h, y, nv, x, s);
+    case 2: return eq_dispatch_tx<2>(mode, ntx, K, B, h, y, nv, x, s);
+    case 4: return eq_dispatch_tx<4>(mode, ntx, K, B, h, y, nv, x, s);
+    case 8: return eq_dispatch_tx<8>(mode, ntx, K, B, h, y, nv, x, s);
+    default: return hpx_fail(HPX_ERR_UNSUPPORTED, "equalize: %d receive streams not supported (1, 2, 4, 8)", nrx);
+  }
+}
+
+hpx_status hpx_detect_ideal(const hpx_fading* f, const void* state, const hpx_frame* fr, int32_t mode,
+                            const hpx_cf32* grid, int32_t gcols, const float* nv, uint64_t seed, int64_t drop0,
+                            int32_t B, uint32_t* errors, void* stream) {
+  if (!f || !state || !fr || !grid || !errors) return hpx_fail(HPX_ERR_ARG, "detect_ideal: null argument");
+  if (mode != HPX_EQ_ZF && mode != HPX_EQ_LMMSE) return hpx_fail(HPX_ERR_ARG, "detect_ideal: unknown mode");
+  if (mode == HPX_EQ_LMMSE && !nv) return hpx_fail(HPX_ERR_ARG, "detect_ideal: LMMSE needs noise variances");
+  if (B < 0 || drop0 < 0) return hpx_fail(HPX_ERR_ARG, "detect_ideal: bad drop range");
+  if (gcols < fr->info.num_columns) return hpx_fail(HPX_ERR_SHAPE, "detect_ideal: grid too narrow");
+  if (B == 0) return HPX_OK;
+  if (B > 65535) return hpx_fail(HPX_ERR_ARG, "detect_ideal: batch above 65535 drops per call");
+  cudaStream_t s = as_stream(stream);
+  HPX_CUDA(cudaMemsetAsync(errors, 0, sizeof(uint32_t) * B, s));
+  switch (f->nrx) {
+    case 1: return detect_ideal_tx<1>(f->ntx, f, state, fr, mode, grid, gcols, nv, seed, drop0, B, errors, s);
+    case 2: return detect_ideal_tx<2>(f->ntx, f, state, fr, mode, grid, gcols, nv, seed, drop0, B, errors, s);
+    case 4: return detect_ideal_tx<4>(f->ntx, f, state, fr, mode, grid, gcols, nv, seed, drop0, B, errors, s);
+    case 8: return detect_ideal_tx<8>(f->ntx, f, state, fr, mode, grid, gcols, nv, seed, drop0, B, errors, s);
+    default: return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_ideal: %d receive antennas not supported", f->nrx);
+  }
+}
+
+hpx_status hpx_detect_ls(const hpx_ls* ls, int32_t mode, const hpx_cf32* grid, int32_t gcols, const float* nv,
+                         uint64_t seed, int64_t drop0, int32_t B, uint32_t* errors, void* stream) {
+  if (!ls || !grid || !errors) return hpx_fail(HPX_ERR_ARG, "detect_ls: null argument");
+  if (mode != HPX_EQ_ZF && mode != HPX_EQ_LMMSE) return hpx_fail(HPX_ERR_ARG, "detect_ls: unknown mode");
+  if (mode == HPX_EQ_LMMSE && !nv) return hpx_fail(HPX_ERR_ARG, "detect_ls: LMMSE needs noise variances");
+  if (B < 0 || drop0 < 0) return hpx_fail(HPX_ERR_ARG, "detect_ls: bad drop range");
+  const hpx_frame* fr = ls->frame;
+  if (gcols < fr->info.num_columns) return hpx_fail(HPX_ERR_SHAPE, "detect_ls: grid too narrow");
+  if (B == 0) return HPX_OK;
+  if (B > 65535) return hpx_fail(HPX_ERR_ARG, "detect_ls: batch above 65535 drops per call");
+  QamDemapTable qt;
+  HPX_TRY(qam_demap_table(fr->info.modulation_order, &qt));
+  cudaStream_t s = as_stream(stream);
+  HPX_CUDA(cudaMemsetAsync(errors, 0, sizeof(uint32_t) * B, s));
+  const int C = ls->C, m = fr->info.bits_per_symbol;
+  const size_t smem = (size_t)(((fr->info.num_columns * m) >> 5) + 8) * 4 + 16;
+  dim3 grid_dim(fr->info.num_words, B);
+  k_detect_ls<<<grid_dim, DTHREADS, smem, s>>>(fr->info.num_words, C, m, fr->d_data_offset, fr->d_num_data_word,
+                                               fr->d_data_column, ls->d_indptr, ls->d_indices, ls->d_weights,
+                                               ls->d_ref_word, ls->d_ref_column, fr->d_pilots, qt, mode,
+                                               reinterpret_cast<const float2*>(grid), gcols, nv, seed, drop0, errors);
+  HPX_LAUNCHED("detect_ls");
+  return HPX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,164 @@
+// Frame layout tables and the library's error state.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "hpx_internal.cuh"
+
+// ------------------------------------------------------------------ errors
+
+static thread_local std::string g_last_error;
+
+hpx_status hpx_fail(hpx_status code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+hpx_status hpx_cuda_status(cudaError_t err, const char* what) {
+  return hpx_fail(HPX_ERR_CUDA, "CUDA error %d (%s) in %s", (int)err, cudaGetErrorString(err), what);
+}
+
+template <typename T>
+static hpx_status upload(T** dst, const std::vector<T>& src) {
+  if (src.empty()) {
+    *dst = nullptr;
+    return HPX_OK;
+  }
+  HPX_CUDA(cudaMalloc(reinterpret_cast<void**>(dst), src.size() * sizeof(T)));
+  HPX_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return HPX_OK;
+}
+
+static void release(hpx_frame* f) {
+  if (!f) return;
+  void* ptrs[] = {f->d_prefix, f->d_zero_prefix, f->d_word_start, f->d_window_start, f->d_data_offset,
+                  f->d_num_data_word, f->d_kind, f->d_index, f->d_bins, f->d_data_column, f->d_data_word,
+                  f->d_twiddle, f->d_pilots};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete f;
+}
+
+extern "C" {
+
+int hpx_version(void) { return 10000; }
+
+const char* hpx_last_error(void) { return g_last_error.c_str(); }
+
+hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out) {
+  if (!desc || !out) return hpx_fail(HPX_ERR_ARG, "frame: null argument");
+  *out = nullptr;
+  const int N = desc->num_subcarriers;
+  if (N < 64 || N > 4096 || (N & (N - 1)))
+    return hpx_fail(HPX_ERR_UNSUPPORTED, "frame: number of subcarriers must be a power of two in [64, 4096] (got %d)", N);
+  const int W = desc->num_words, C = desc->num_columns;
+  if (W < 1) return hpx_fail(HPX_ERR_ARG, "frame: at least one word required");
+  if (C < 1 || C > N) return hpx_fail(HPX_ERR_ARG, "frame: num_columns must be in [1, N]");
+  int m;
+  HPX_TRY(qam_bits_per_symbol(desc->modulation_order, &m));
+  if (!desc->prefix || !desc->kind) return hpx_fail(HPX_ERR_ARG, "frame: null table");
+
+  hpx_frame* f = new hpx_frame();
+  f->dc_suppression = desc->dc_suppression ? 1 : 0;
+  f->h_prefix.assign(desc->prefix, desc->prefix + W);
+  f->h_zero_prefix.assign(W, 0);
+  if (desc->zero_prefix) f->h_zero_prefix.assign(desc->zero_prefix, desc->zero_prefix + W);
+  f->h_kind.assign(desc->kind, desc->kind + (size_t)W * C);
+  f->h_index.assign((size_t)W * C, -1);
+  f->h_word_start.resize(W);
+  f->h_window_start.resize(W);
+  f->h_data_offset.resize(W);
+  f->h_ref_offset.resize(W);
+  std::vector<int32_t> num_data_word(W, 0), data_column, data_word;
+  int64_t start = 0;
+  int nd = 0, nr = 0;
+  for (int w = 0; w < W; ++w) {
+    const int p = f->h_prefix[w];
+    if (p < 0 || p > N) {
+      release(f);
+      return hpx_fail(HPX_ERR_ARG, "frame: prefix length of word %d out of range", w);
+    }
+    f->h_word_start[w] = (int32_t)start;
+    f->h_window_start[w] = (int32_t)(start + p);
+    f->h_data_offset[w] = nd;
+    f->h_ref_offset[w] = nr;
+    for (int c = 0; c < C; ++c) {
+      const int8_t k = f->h_kind[(size_t)w * C + c];
+      if (k == HPX_RE_DATA) {
+        f->h_index[(size_t)w * C + c] = nd++;
+        data_column.push_back(c);
+        data_word.push_back(w);
+        num_data_word[w]++;
+      } else if (k == HPX_RE_REFERENCE) {
+        f->h_index[(size_t)w * C + c] = nr++;
+      } else if (k != HPX_RE_NULL) {
+        release(f);
+        return hpx_fail(HPX_ERR_ARG, "frame: unknown element type %d", (int)k);
+      }
+    }
+    start += p + N;
+  }
+  if (start > (1ll << 30)) {
+    release(f);
+    return hpx_fail(HPX_ERR_ARG, "frame: too many samples");
+  }
+  f->info.num_subcarriers = N;
+  f->info.num_words = W;
+  f->info.num_columns = C;
+  f->info.modulation_order = desc->modulation_order;
+  f->info.bits_per_symbol = m;
+  f->info.num_data = nd;
+  f->info.num_refs = nr;
+  f->info.samples_per_frame = (int32_t)start;
+
+  // grid column -> FFT bin (ofdm.py:116-128 and 146-151)
+  f->h_bins.resize(N);
+  for (int c = 0; c < N; ++c) {
+    int b;
+    if (f->dc_suppression) b = c < N / 2 ? c + N / 2 : (c < N - 1 ? c + 1 - N / 2 : 0);
+    else b = (c + N / 2) % N;
+    f->h_bins[c] = b;
+  }
+  std::vector<float2> tw(N);
+  for (int t = 0; t < N; ++t) {
+    const double a = -2.0 * M_PI * (double)t / (double)N;
+    tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  std::vector<float2> pilots(nr);
+  for (int k = 0; k < nr; ++k) pilots[k] = qam_symbol(desc->modulation_order, (uint32_t)(k % desc->modulation_order));
+
+  hpx_status s = HPX_OK;
+  if ((s = upload(&f->d_prefix, f->h_prefix)) != HPX_OK ||
+      (s = upload(&f->d_zero_prefix, f->h_zero_prefix)) != HPX_OK ||
+      (s = upload(&f->d_word_start, f->h_word_start)) != HPX_OK ||
+      (s = upload(&f->d_window_start, f->h_window_start)) != HPX_OK ||
+      (s = upload(&f->d_data_offset, f->h_data_offset)) != HPX_OK ||
+      (s = upload(&f->d_num_data_word, num_data_word)) != HPX_OK ||
+      (s = upload(&f->d_kind, f->h_kind)) != HPX_OK || (s = upload(&f->d_index, f->h_index)) != HPX_OK ||
+      (s = upload(&f->d_bins, f->h_bins)) != HPX_OK || (s = upload(&f->d_data_column, data_column)) != HPX_OK ||
+      (s = upload(&f->d_data_word, data_word)) != HPX_OK || (s = upload(&f->d_twiddle, tw)) != HPX_OK ||
+      (s = upload(&f->d_pilots, pilots)) != HPX_OK) {
+    release(f);
+    return s;
+  }
+  *out = f;
+  return HPX_OK;
+}
+
+hpx_status hpx_frame_destroy(hpx_frame* frame) {
+  release(frame);
+  return HPX_OK;
+}
+
+hpx_status hpx_frame_get_info(const hpx_frame* frame, hpx_frame_info* info) {
+  if (!frame || !info) return hpx_fail(HPX_ERR_ARG, "frame_info: null argument");
+  *info = frame->info;
+  return HPX_OK;
+}
+
+}  // extern "C"

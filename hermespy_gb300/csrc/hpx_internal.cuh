@@ -1,0 +1,281 @@
+// Internal definitions shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <vector>
+
+#include "../../include/hpx.h"
+
+// ------------------------------------------------------------------ errors
+
+hpx_status hpx_fail(hpx_status code, const char* fmt, ...);
+hpx_status hpx_cuda_status(cudaError_t err, const char* what);
+
+#define HPX_TRY(expr)                      \
+  do {                                     \
+    hpx_status _s = (expr);                \
+    if (_s != HPX_OK) return _s;           \
+  } while (0)
+
+#define HPX_CUDA(expr)                                         \
+  do {                                                         \
+    cudaError_t _e = (expr);                                   \
+    if (_e != cudaSuccess) return hpx_cuda_status(_e, #expr);  \
+  } while (0)
+
+// Check the launch of the kernel enqueued just before.
+#define HPX_LAUNCHED(name) HPX_CUDA(cudaPeekAtLastError())
+
+static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// -------------------------------------------------------------- complex math
+
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // conj(a) * b
+  return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+// acc += a * b
+__device__ __forceinline__ void cfma(float2& acc, float2 a, float2 b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(-a.y, b.y, acc.x);
+  acc.y = fmaf(a.x, b.y, acc.y);
+  acc.y = fmaf(a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+__device__ __forceinline__ void cfmac(float2& acc, float2 a, float2 b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(a.y, b.y, acc.x);
+  acc.y = fmaf(a.x, b.y, acc.y);
+  acc.y = fmaf(-a.y, b.x, acc.y);
+}
+
+// ------------------------------------------------------------- Philox4x32-10
+// Salmon et al., "Parallel random numbers: as easy as 1, 2, 3" (SC'11).
+
+__host__ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+#ifdef __CUDA_ARCH__
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x);
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z);
+#else
+    const uint32_t hi0 = (uint32_t)(((uint64_t)0xD2511F53u * c.x) >> 32);
+    const uint32_t hi1 = (uint32_t)(((uint64_t)0xCD9E8D57u * c.z) >> 32);
+#endif
+    const uint32_t lo0 = 0xD2511F53u * c.x;
+    const uint32_t lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += 0x9E3779B9u;
+    k.y += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// Random-stream layout: c0 = block, c1 = stream id, c2 = drop (low 32 bits),
+// c3 = domain | drop bits 32..55 << 8; key = 64-bit campaign seed.
+enum { HPX_DOMAIN_BITS = 1, HPX_DOMAIN_FADING = 2, HPX_DOMAIN_NOISE = 3 };
+
+__host__ __device__ __forceinline__ uint4 hpx_random_block(uint64_t seed, int64_t drop, uint32_t stream_id,
+                                                           uint32_t domain, uint32_t block) {
+  const uint64_t d = (uint64_t)drop;
+  uint4 c = make_uint4(block, stream_id, (uint32_t)(d & 0xFFFFFFFFu),
+                       (domain & 0xFFu) | ((uint32_t)((d >> 32) & 0xFFFFFFu) << 8));
+  return philox4x32_10(c, make_uint2((uint32_t)(seed & 0xFFFFFFFFu), (uint32_t)(seed >> 32)));
+}
+
+__host__ __device__ __forceinline__ uint32_t uint4_get(const uint4& v, int i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+// Uniform on (0, 1) from one 32-bit word: (w + 0.5) * 2^-32.
+__host__ __device__ __forceinline__ double u01_f64(uint32_t w) { return ((double)w + 0.5) * 2.3283064365386963e-10; }
+__device__ __forceinline__ float u01_f32(uint32_t w) { return ((float)(w >> 8) + 0.5f) * 5.9604644775390625e-08f; }
+
+// Box-Muller pair of unit normals from two words.
+__device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b) {
+  const float u1 = u01_f32(a);
+  const float u2 = u01_f32(b);
+  const float r = sqrtf(-2.0f * logf(u1));
+  float s, c;
+  sincospif(2.0f * u2, &s, &c);
+  return make_float2(r * c, r * s);
+}
+
+// ------------------------------------------------------ fixed-point phases
+// A phase in turns is held as a 64-bit two's-complement fraction of a turn, so
+// that phase(t) = P0 + W * t wraps exactly modulo one turn for any sample index.
+
+__host__ __device__ __forceinline__ int64_t turns_to_fixed(double turns) {
+  const double frac = turns - floor(turns);  // [0, 1)
+  // 2^64 * frac, computed as two 32-bit halves to stay exact in double
+  const double hi = floor(frac * 4294967296.0);
+  const double lo = floor((frac * 4294967296.0 - hi) * 4294967296.0);
+  return (int64_t)(((uint64_t)hi << 32) | (uint64_t)lo);
+}
+
+// Angle in radians in [-pi, pi) of a fixed-point phase.
+__device__ __forceinline__ float fixed_to_angle(uint64_t p) {
+  return (float)(int32_t)(uint32_t)(p >> 32) * 1.4629180792671596e-09f;  // 2*pi / 2^32
+}
+
+// ------------------------------------------------------------- frame tables
+
+struct hpx_frame {
+  hpx_frame_info info;
+  int dc_suppression;
+  // host copies
+  std::vector<int32_t> h_prefix, h_zero_prefix, h_word_start, h_window_start;
+  std::vector<int32_t> h_data_offset, h_ref_offset;  // first data / ref index of each word
+  std::vector<int8_t> h_kind;                        // [W * C]
+  std::vector<int32_t> h_index;                      // [W * C] data or ref index within the frame
+  std::vector<int32_t> h_bins;                       // [N] FFT bin of grid column c
+  // device copies
+  int32_t* d_prefix = nullptr;
+  int32_t* d_zero_prefix = nullptr;
+  int32_t* d_word_start = nullptr;
+  int32_t* d_window_start = nullptr;
+  int32_t* d_data_offset = nullptr;
+  int32_t* d_num_data_word = nullptr;  // data elements per word
+  int8_t* d_kind = nullptr;
+  int32_t* d_index = nullptr;
+  int32_t* d_bins = nullptr;
+  int32_t* d_data_column = nullptr;    // [num_data] column of data element k (word via search)
+  int32_t* d_data_word = nullptr;      // [num_data] word of data element k
+  float2* d_twiddle = nullptr;         // [N] exp(-2 pi i t / N)
+  float2* d_pilots = nullptr;          // [num_refs]
+};
+
+// ------------------------------------------------------------ fading state
+
+struct hpx_fading {
+  int L, S, S1;  // taps, sinusoids, sinusoids + LOS component
+  int nrx, ntx;
+  double fs, doppler, los_doppler, gain;
+  int max_delay;  // D
+  std::vector<int32_t> h_delay;
+  std::vector<float> h_amp_nlos, h_amp_los;  // sqrt(gain g_l) * gain_{nlos,los}
+  std::vector<double> h_rx_corr, h_tx_corr;  // complex interleaved, empty if none
+  // device copies
+  int32_t* d_delay = nullptr;
+  float* d_amp = nullptr;       // [L][2] (nlos, los)
+  double* d_rx_corr = nullptr;  // [nrx*nrx*2] or null
+  double* d_tx_corr = nullptr;
+  // per-drop state layout (bytes)
+  size_t off_w, off_p0, off_spatial, stride;
+};
+
+// Per-drop realization state, read by the kernels.
+struct FadingView {
+  const unsigned char* base;
+  size_t stride, off_w, off_p0, off_spatial;
+  int L, S1, nrx, ntx;
+  __device__ __forceinline__ const int64_t* W(int b) const {
+    return reinterpret_cast<const int64_t*>(base + b * stride + off_w);
+  }
+  __device__ __forceinline__ const int64_t* P0(int b) const {
+    return reinterpret_cast<const int64_t*>(base + b * stride + off_p0);
+  }
+  __device__ __forceinline__ const float2* spatial(int b) const {
+    return reinterpret_cast<const float2*>(base + b * stride + off_spatial);
+  }
+};
+
+static inline FadingView fading_view(const hpx_fading* f, const void* state) {
+  FadingView v;
+  v.base = static_cast<const unsigned char*>(state);
+  v.stride = f->stride;
+  v.off_w = f->off_w;
+  v.off_p0 = f->off_p0;
+  v.off_spatial = f->off_spatial;
+  v.L = f->L;
+  v.S1 = f->S1;
+  v.nrx = f->nrx;
+  v.ntx = f->ntx;
+  return v;
+}
+
+// QAM tables (mapping.cu)
+hpx_status qam_bits_per_symbol(int32_t order, int* bits);
+struct QamDemapTable {
+  int order, bits, pam_bits;  // pam_bits: bits per real dimension
+  float lo[4][8], hi[4][8];   // per PAM bit: up to 8 open intervals (lo, hi) in float32 x
+  int count[4];
+};
+hpx_status qam_demap_table(int32_t order, QamDemapTable* table);
+
+// PAM level (3GPP Gray) of `nb` bits MSB-first packed in `v` (bit nb-1 is the first bit).
+__host__ __device__ __forceinline__ float pam_level(int nb, uint32_t v) {
+  // Unnormalized amplitudes of generate_pam_symbol_3gpp (psk_qam_mapping.py:261-298)
+  float b0 = (float)((v >> (nb - 1)) & 1u);
+  if (nb == 1) return 1.0f - 2.0f * b0;
+  float b1 = (float)((v >> (nb - 2)) & 1u);
+  if (nb == 2) return (1.0f - 2.0f * b0) * (1.0f + 2.0f * b1);
+  float b2 = (float)((v >> (nb - 3)) & 1u);
+  if (nb == 3) return (2.0f * b0 - 1.0f) * ((1.0f - 2.0f * b1) * (1.0f + 2.0f * b2) - 4.0f);
+  float b3 = (float)((v >> (nb - 4)) & 1u);
+  return ((((1.0f - 2.0f * b2) * (1.0f + 2.0f * b3) - 4.0f) * (-1.0f + 2.0f * b1)) - 8.0f) * (-1.0f + 2.0f * b0);
+}
+
+// Symbol of an M-ary constellation from its MSB-first bit value (0..M-1).
+__host__ __device__ __forceinline__ float2 qam_symbol(int order, uint32_t v) {
+  switch (order) {
+    case 2: return make_float2(pam_level(1, v), 0.0f);
+    case 4: {
+      const float s = 0.70710678118654752f;
+      return make_float2(pam_level(1, v >> 1) * s, pam_level(1, v & 1u) * s);
+    }
+    default: {
+      // bits b0 b1 b2 ... : real gets b0 b2 b4.., imag gets b1 b3 b5..
+      const int m = order == 16 ? 4 : (order == 64 ? 6 : 8);
+      const int h = m / 2;
+      uint32_t re = 0, im = 0;
+      for (int i = 0; i < h; ++i) {
+        re = (re << 1) | ((v >> (m - 1 - 2 * i)) & 1u);
+        im = (im << 1) | ((v >> (m - 2 - 2 * i)) & 1u);
+      }
+      const float s = order == 16 ? 0.31622776601683794f : (order == 64 ? 0.15430334996209191f : 0.07669649888473704f);
+      return make_float2(pam_level(h, re) * s, pam_level(h, im) * s);
+    }
+  }
+}
+
+// Hard decisions of one symbol with a demap table; returns MSB-first bit value.
+// BPSK and QPSK LLRs are plain linear functions of the amplitude (no masked
+// pieces), so -inf decides 1 there, while the masked piecewise LLRs of the larger
+// constellations turn any infinity into NaN and decide 0 (open intervals).
+__device__ __forceinline__ uint32_t qam_decide(const QamDemapTable& t, float2 y) {
+  if (t.order == 2) return (y.x < 0.0f) ? 1u : 0u;
+  if (t.order == 4) return ((y.x < 0.0f) ? 2u : 0u) | ((y.y < 0.0f) ? 1u : 0u);
+  uint32_t v = 0;
+  const int h = t.pam_bits;
+  for (int i = 0; i < h; ++i) {
+    uint32_t br = 0, bi = 0;
+    for (int k = 0; k < t.count[i]; ++k) {
+      br |= (y.x > t.lo[i][k] && y.x < t.hi[i][k]) ? 1u : 0u;
+      bi |= (y.y > t.lo[i][k] && y.y < t.hi[i][k]) ? 1u : 0u;
+    }
+    v = (v << 2) | (br << 1) | bi;
+  }
+  return v;
+}
+
+// Extract `nb` (<= 8) bits MSB-first starting at stream bit position `pos` from
+// packed little-endian-in-word bit storage (bit b = bit b%32 of word b/32).
+__device__ __forceinline__ uint32_t extract_bits_msb(const uint32_t* words, int64_t pos, int nb) {
+  uint32_t v = 0;
+  for (int i = 0; i < nb; ++i) {
+    const int64_t b = pos + i;
+    v = (v << 1) | ((words[b >> 5] >> (b & 31)) & 1u);
+  }
+  return v;
+}

@@ -1,0 +1,295 @@
+/*
+ * hpx.h -- C ABI of the GB300 Monte Carlo link engine for HermesPy's OFDM
+ * fading-link drop loop.
+ *
+ * Conventions
+ *   - Complex samples are interleaved float32 pairs (hpx_cf32), i.e. the memory
+ *     layout of numpy/torch complex64.
+ *   - Every data pointer passed to a compute entry point is a DEVICE pointer on
+ *     the current CUDA device; descriptors (hpx_frame_desc, hpx_fading_desc) hold
+ *     HOST pointers and are copied at create time.
+ *   - Batched buffers are dense, batch index outermost, shapes given in brackets.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream). Compute entry
+ *     points only enqueue work; they never synchronize and never allocate.
+ *     Handles (*_create) allocate their device tables once.
+ *   - Every entry point returns an hpx_status; hpx_last_error() gives the
+ *     message of the last failure on the calling thread. The Python layer maps
+ *     HPX_ERR_ARG/HPX_ERR_SHAPE to ValueError, HPX_ERR_UNSUPPORTED to
+ *     NotImplementedError and the rest to RuntimeError, as the reference does.
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the HermesPy source tree).
+ */
+#ifndef HPX_H_
+#define HPX_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct { float re, im; } hpx_cf32;
+
+typedef enum {
+  HPX_OK = 0,
+  HPX_ERR_ARG = 1,         /* invalid argument          -> ValueError          */
+  HPX_ERR_SHAPE = 2,       /* shape / size mismatch     -> ValueError          */
+  HPX_ERR_UNSUPPORTED = 3, /* configuration not covered -> NotImplementedError */
+  HPX_ERR_CUDA = 4,        /* CUDA runtime failure      -> RuntimeError        */
+  HPX_ERR_NUMERIC = 5,     /* numerical failure         -> RuntimeError        */
+  HPX_ERR_TIMEOUT = 6      /* bounded device wait ran out -> RuntimeError      */
+} hpx_status;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int hpx_version(void);
+/* Message of the last failed call on this thread ("" if none). */
+const char* hpx_last_error(void);
+
+/* ------------------------------------------------------------------ frames */
+
+/* Element types of the resource grid, as ElementType
+ * (modem/waveforms/orthogonal/waveform.py:39-49). */
+enum { HPX_RE_REFERENCE = 0, HPX_RE_DATA = 1, HPX_RE_NULL = 2 };
+
+typedef struct {
+  int32_t num_subcarriers;   /* N, power of two in [64, 4096] (FFT size, oversampling 1) */
+  int32_t num_words;         /* OFDM symbols per frame */
+  int32_t num_columns;       /* grid columns described by `kind` (<= N) */
+  int32_t modulation_order;  /* 2, 4, 16, 64 or 256 */
+  int32_t dc_suppression;    /* 1: roll the upper half of the grid past DC (ofdm.py:116-120) */
+  const int32_t* prefix;     /* [num_words] prefix length in samples */
+  const int32_t* zero_prefix;/* [num_words] 1 = zero padding, 0 = cyclic prefix (may be NULL) */
+  const int8_t* kind;        /* [num_words * num_columns] HPX_RE_* per resource element */
+} hpx_frame_desc;
+
+typedef struct hpx_frame hpx_frame;
+
+typedef struct {
+  int32_t num_subcarriers, num_words, num_columns, modulation_order, bits_per_symbol;
+  int32_t num_data;          /* data elements per frame and stream */
+  int32_t num_refs;          /* reference elements per frame and stream */
+  int32_t samples_per_frame; /* T */
+} hpx_frame_info;
+
+/* Build the device tables of one frame layout: the grid bookkeeping of
+ * OrthogonalWaveform (resource_mask, samples_per_frame, pilot_symbols;
+ * modem/waveforms/orthogonal/waveform.py:1140-1211, modem/waveform.py:797-820). */
+hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out);
+hpx_status hpx_frame_destroy(hpx_frame* frame);
+hpx_status hpx_frame_get_info(const hpx_frame* frame, hpx_frame_info* info);
+
+/* ------------------------------------------------------- bits and mapping */
+
+/* Data bits of `num_streams` streams of drops [drop0, drop0+num_drops), one byte
+ * (0/1) per bit: bits[num_drops][num_streams][bits_per_stream].
+ * Replaces RandomBitsSource.generate_bits (modem/bits_source.py:62-63) with the
+ * engine's Philox4x32-10 stream (domain 1). */
+hpx_status hpx_bits_generate(uint64_t seed, int64_t drop0, int32_t num_drops, int32_t num_streams,
+                             int64_t bits_per_stream, uint8_t* bits, void* stream);
+
+/* Gray PSK/QAM mapping, MSB first: bits[num_symbols * log2(order)] -> symbols.
+ * Replaces PskQamMapping.get_symbols (modem/tools/psk_qam_mapping.py:104-169). */
+hpx_status hpx_qam_map(int32_t order, const uint8_t* bits, int64_t num_symbols, hpx_cf32* symbols,
+                       void* stream);
+
+/* Hard demapping, bit-exact with PskQamMapping.detect_bits
+ * (modem/tools/psk_qam_mapping.py:171-259) evaluated in float64 on the same
+ * (float32) symbols: ties and NaN give 0. */
+hpx_status hpx_qam_demap(int32_t order, const hpx_cf32* symbols, int64_t num_symbols, uint8_t* bits,
+                         void* stream);
+
+/* Bit errors of `batch` pairs of 0/1 byte vectors a[batch][len_a], b[batch][len_b]
+ * after zero-padding the shorter one: errors[batch].
+ * Replaces BitErrorEvaluator.evaluate (modem/evaluators.py:239-258). */
+hpx_status hpx_count_errors(const uint8_t* a, int64_t len_a, const uint8_t* b, int64_t len_b,
+                            int32_t batch, uint64_t* errors, void* stream);
+
+/* -------------------------------------------------------------------- OFDM */
+
+/* Place + modulate: data[batch][num_data] -> samples[batch][T].
+ * Replaces OrthogonalWaveform.place + modulate with OFDMWaveform._forward_transformation
+ * (modem/waveforms/orthogonal/waveform.py:1221-1258, 1292-1323; ofdm.py:98-130). */
+hpx_status hpx_ofdm_modulate(const hpx_frame* frame, const hpx_cf32* data, int32_t batch,
+                             hpx_cf32* samples, void* stream);
+
+/* Modulate an already placed grid: grid[batch][num_words][grid_columns] (columns
+ * 0..grid_columns-1 of the reference's (words, N) grid) -> samples[batch][T].
+ * Replaces OrthogonalWaveform.modulate on the output of place
+ * (modem/waveforms/orthogonal/waveform.py:1292-1323; ofdm.py:98-130). */
+hpx_status hpx_ofdm_modulate_grid(const hpx_frame* frame, const hpx_cf32* grid, int32_t grid_columns, int32_t batch,
+                                  hpx_cf32* samples, void* stream);
+
+/* Fused bits -> map -> place -> modulate for the engine's Philox bits:
+ * samples[num_drops][num_streams][T]. Replaces TransmittingModemBase._transmit's
+ * bit generation, __map and __modulate (modem/modem.py:747-888). */
+hpx_status hpx_ofdm_modulate_bits(const hpx_frame* frame, uint64_t seed, int64_t drop0,
+                                  int32_t num_drops, int32_t num_streams, hpx_cf32* samples,
+                                  void* stream);
+
+/* Demodulate: samples[batch][sample_stride] (first T used) -> grid[batch][num_words][num_columns],
+ * columns 0..num_columns-1 of the reference's (words, N) grid.
+ * Replaces OrthogonalWaveform.demodulate with OFDMWaveform._backward_transformation
+ * (modem/waveforms/orthogonal/waveform.py:1325-1364; ofdm.py:133-161). */
+hpx_status hpx_ofdm_demodulate(const hpx_frame* frame, const hpx_cf32* samples, int64_t sample_stride,
+                               int32_t batch, int32_t num_columns, hpx_cf32* grid, void* stream);
+
+/* Gather the data elements: grid[batch][num_words][grid_columns] -> out[batch][num_data].
+ * Replaces OrthogonalWaveform.pick (modem/waveforms/orthogonal/waveform.py:1260-1290). */
+hpx_status hpx_ofdm_pick(const hpx_frame* frame, const hpx_cf32* grid, int32_t grid_columns,
+                         int32_t batch, hpx_cf32* out, void* stream);
+
+/* ------------------------------------------------------------------ fading */
+
+typedef struct {
+  int32_t num_taps;             /* L (delays sorted ascending by the caller) */
+  int32_t num_sinusoids;        /* S >= 0 */
+  int32_t num_rx, num_tx;       /* antennas */
+  double sampling_rate;         /* Hz */
+  double doppler_frequency;     /* NLOS Doppler, Hz */
+  double los_doppler_frequency; /* LOS Doppler, Hz */
+  double gain;                  /* linear power gain */
+  const double* delays;         /* [L] seconds */
+  const double* power_profile;  /* [L] linear */
+  const double* rice_factors;   /* [L] linear, +inf for pure LOS */
+  const double* rx_correlation; /* [num_rx*num_rx] interleaved complex, or NULL */
+  const double* tx_correlation; /* [num_tx*num_tx] interleaved complex, or NULL */
+  const double* los_gains;      /* [L] explicit LOS gains, or NULL to derive sqrt(K/(1+K)) */
+  const double* nlos_gains;     /* [L] explicit NLOS gains, or NULL to derive sqrt(1/((1+K)S)) */
+} hpx_fading_desc;
+
+typedef struct hpx_fading hpx_fading;
+
+/* Validate and precompute a MultipathFadingChannel configuration
+ * (channel/fading/fading.py:606-754): gains sqrt(K/(1+K)), sqrt(1/((1+K)S)),
+ * delays rint(tau*fs). Raises HPX_ERR_ARG for the reference's ValueErrors. */
+hpx_status hpx_fading_create(const hpx_fading_desc* desc, hpx_fading** out);
+hpx_status hpx_fading_destroy(hpx_fading* fading);
+/* Bytes of the per-drop realization state buffer for `num_drops` drops. */
+hpx_status hpx_fading_state_bytes(const hpx_fading* fading, int32_t num_drops, int64_t* bytes);
+/* D = round(max delay * fs): propagated frames have T + D samples. */
+hpx_status hpx_fading_max_delay(const hpx_fading* fading, int32_t* samples);
+
+/* Realize drops [drop0, drop0+num_drops) from the engine's Philox stream (domain 2)
+ * into `state`. Replaces MultipathFadingChannel._realize + MultipathFadingRealization._sample
+ * (channel/fading/fading.py:468-515, 893-910; channel/consistent.py:431-432, 475-485). */
+hpx_status hpx_fading_realize(const hpx_fading* fading, uint64_t seed, int64_t drop0, int32_t num_drops,
+                              void* state, void* stream);
+
+/* Load explicit sample parameters (device float64 arrays): los_angles[B][L],
+ * nlos_angles[B][L][S], los_phases[B][L], nlos_phases[B][L][S], spatial[B][Nrx][Ntx]
+ * (interleaved complex). Mirrors the MultipathFadingSample constructor
+ * (channel/fading/fading.py:153-214). */
+hpx_status hpx_fading_load(const hpx_fading* fading, int32_t num_drops, const double* los_angles,
+                           const double* nlos_angles, const double* los_phases, const double* nlos_phases,
+                           const double* spatial, void* state, void* stream);
+
+/* The float64 uniforms of drops [drop0, drop0+num_drops) in the realization's draw
+ * layout [spatial Nrx*Ntx][LOS angle L][NLOS angles L*S][LOS phase L][NLOS phases L*S]:
+ * uniforms[num_drops][num_draws]. Exposes what hpx_fading_realize consumes (the
+ * reference's ConsistentUniform samples, channel/consistent.py:475-485). */
+hpx_status hpx_fading_draws(const hpx_fading* fading, uint64_t seed, int64_t drop0, int32_t num_drops,
+                            double* uniforms, void* stream);
+
+/* Tap coefficients taps[B][L][num_samples] by direct sum of sinusoids.
+ * Replaces MultipathFadingSample.__path_impulse_generator (channel/fading/fading.py:293-343). */
+hpx_status hpx_fading_taps(const hpx_fading* fading, const void* state, int32_t num_drops,
+                           int32_t num_samples, hpx_cf32* taps, void* stream);
+
+/* Impulse-response CSI csi[B][Nrx][Ntx][num_samples][num_taps_out], num_taps_out =
+ * min(1 + D, max_num_taps). Replaces MultipathFadingSample.state (fading.py:345-369). */
+hpx_status hpx_fading_csi(const hpx_fading* fading, const void* state, int32_t num_drops,
+                          int32_t num_samples, int32_t max_num_taps, hpx_cf32* csi, void* stream);
+
+/* Propagate x[B][Ntx][num_samples] -> y[B][Nrx][num_samples + D] and, when
+ * noise_power != NULL, add complex AWGN of power noise_power[b] from the engine's
+ * Philox stream (domain 3, drop index drop0+b).
+ * Replaces MultipathFadingSample._propagate (channel/fading/fading.py:371-406) and
+ * AWGNRealization.add_to (simulation/rf/noise/model.py:143-160). */
+hpx_status hpx_fading_propagate(const hpx_fading* fading, const void* state, int32_t num_drops,
+                                const hpx_cf32* x, int32_t num_samples, hpx_cf32* y,
+                                const float* noise_power, uint64_t seed, int64_t drop0, void* stream);
+
+/* Ideal frequency-domain CSI H[B][Nrx][Ntx][num_words][num_columns] of a frame.
+ * Replaces OFDMIdealChannelEstimation.estimate_channel
+ * (simulation/modem/channel_estimation.py:215-295). */
+hpx_status hpx_fading_ideal_csi(const hpx_fading* fading, const void* state, int32_t num_drops,
+                                const hpx_frame* frame, int32_t num_columns, hpx_cf32* csi, void* stream);
+
+/* ------------------------------------------------- estimation / detection */
+
+typedef struct hpx_ls hpx_ls;
+
+/* Least-squares interpolator of a SISO frame as a CSR map from the reference
+ * elements' LS values to grid[num_words][num_columns] (host arrays, row-major rows).
+ * The map is the one OrthogonalLeastSquaresChannelEstimation.estimate_channel applies
+ * (modem/waveforms/orthogonal/channel.py:29-66). */
+hpx_status hpx_ls_create(const hpx_frame* frame, int32_t num_columns, const int32_t* indptr,
+                         const int32_t* indices, const float* weights, hpx_ls** out);
+hpx_status hpx_ls_destroy(hpx_ls* ls);
+/* grid[B][num_words][grid_columns] -> H[B][num_words][num_columns]. */
+hpx_status hpx_ls_estimate(const hpx_ls* ls, const hpx_cf32* grid, int32_t grid_columns, int32_t batch,
+                           hpx_cf32* estimate, void* stream);
+
+enum { HPX_EQ_ZF = 0, HPX_EQ_LMMSE = 1 };
+
+/* Per-element equalization: H[B][Nrx][Ntx][K], y[B][Nrx][K] -> x[B][Ntx][K].
+ * HPX_EQ_ZF replaces ZeroForcingChannelEqualization.equalize_channel
+ * (modem/waveform.py:235-250: y / sum_tx h for one receive stream, pinv(H) y otherwise);
+ * HPX_EQ_LMMSE solves (H^H H + s2 I) x = H^H y by Cholesky (no reference counterpart),
+ * s2 = noise_var[b]. */
+hpx_status hpx_equalize(int32_t mode, int32_t num_rx, int32_t num_tx, int64_t num_elements, int32_t batch,
+                        const hpx_cf32* channel, const hpx_cf32* received, const float* noise_var,
+                        hpx_cf32* equalized, void* stream);
+
+/* Fused receiver for drops with ideal CSI: grid[B][Nrx][num_words][grid_columns] ->
+ * ideal CSI (as hpx_fading_ideal_csi) -> pick -> equalize (ZF or LMMSE) -> hard demap ->
+ * compare with the regenerated Philox bits -> errors[B] (bit errors per drop).
+ * Replaces the estimate/pick/equalize/unmap chain of ReceivingModemBase._receive
+ * (modem/modem.py:1192-1267) and BitErrorEvaluator (modem/evaluators.py:239-258). */
+hpx_status hpx_detect_ideal(const hpx_fading* fading, const void* state, const hpx_frame* frame,
+                            int32_t mode, const hpx_cf32* grid, int32_t grid_columns,
+                            const float* noise_var, uint64_t seed, int64_t drop0, int32_t num_drops,
+                            uint32_t* errors, void* stream);
+
+/* Fused SISO receiver with LS estimation: grid[B][num_words][grid_columns] -> LS ->
+ * pick -> ZF (or LMMSE) -> hard demap -> errors[B]. */
+hpx_status hpx_detect_ls(const hpx_ls* ls, int32_t mode, const hpx_cf32* grid, int32_t grid_columns,
+                         const float* noise_var, uint64_t seed, int64_t drop0, int32_t num_drops,
+                         uint32_t* errors, void* stream);
+
+/* ------------------------------------------------------------------- noise */
+
+/* Add complex AWGN of power noise_power[b] to samples[batch][num_streams][num_samples]
+ * in place, from the engine's Philox stream (domain 3, drop drop0+b, stream id =
+ * stream index). Replaces AWGN.realize + AWGNRealization.add_to
+ * (simulation/rf/noise/model.py:143-178). */
+hpx_status hpx_awgn_add(hpx_cf32* samples, int32_t batch, int32_t num_streams, int64_t num_samples,
+                        const float* noise_power, uint64_t seed, int64_t drop0, void* stream);
+
+/* ------------------------------------------------------- batched drop loop */
+
+enum { HPX_EST_IDEAL = 0, HPX_EST_LS = 1 };
+
+typedef struct hpx_link hpx_link;
+
+/* Device workspace of a link for `num_drops` drops per run (bytes). */
+hpx_status hpx_link_workspace_bytes(const hpx_frame* frame, const hpx_fading* fading, int32_t num_drops,
+                                    int64_t* bytes);
+/* A simplex OFDM link over a fading channel with its workspace for up to
+ * max_drops drops per run; `ls` is required for HPX_EST_LS (SISO only). */
+hpx_status hpx_link_create(const hpx_frame* frame, const hpx_fading* fading, const hpx_ls* ls, int32_t estimator,
+                           int32_t equalizer, int32_t max_drops, hpx_link** out);
+hpx_status hpx_link_destroy(hpx_link* link);
+/* Simulate drops [drop0, drop0+num_drops): realize, transmit Philox bits, propagate
+ * with AWGN of power noise_power[b], demodulate, estimate, equalize, demap and
+ * count bit errors into errors[num_drops]. Replaces one SimulationScenario._drop
+ * (simulation/scenario.py:772-804) plus BitErrorEvaluator per drop. */
+hpx_status hpx_link_run(const hpx_link* link, uint64_t seed, int64_t drop0, int32_t num_drops,
+                        const float* noise_power, uint32_t* errors, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HPX_H_ */
