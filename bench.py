@@ -178,7 +178,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--drops", type=int, default=DROPS)
-    ap.add_argument("--cpu-rounds", type=int, default=1, help="rounds of per-core oracle drops for cpu_baseline")
+    ap.add_argument("--cpu-rounds", type=int, default=4, help="rounds of per-core oracle drops for cpu_baseline")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

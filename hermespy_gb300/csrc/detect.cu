@@ -22,15 +22,14 @@ namespace {
 template <int n>
 __device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], float2 (&x)[n]) {
   bool ok = true;
+  float inv[n];  // reciprocal pivots 1 / L[j][j]
 #pragma unroll
   for (int j = 0; j < n; ++j) {
     float d = A[j][j].x;
 #pragma unroll
     for (int k = 0; k < j; ++k) d -= A[j][k].x * A[j][k].x + A[j][k].y * A[j][k].y;
     ok = ok && (d > 0.0f);
-    const float ljj = sqrtf(d);
-    const float inv = 1.0f / ljj;
-    A[j][j] = make_float2(ljj, 0.f);
+    inv[j] = rsqrtf(d);
 #pragma unroll
     for (int i = j + 1; i < n; ++i) {
       float2 s = A[i][j];
@@ -40,7 +39,7 @@ __device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], fl
         s.x -= A[i][k].x * A[j][k].x + A[i][k].y * A[j][k].y;
         s.y -= A[i][k].y * A[j][k].x - A[i][k].x * A[j][k].y;
       }
-      A[i][j] = cscale(s, inv);
+      A[i][j] = cscale(s, inv[j]);
     }
   }
   float2 z[n];
@@ -49,14 +48,14 @@ __device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], fl
     float2 s = b[i];
 #pragma unroll
     for (int k = 0; k < i; ++k) s = csub(s, cmul(A[i][k], z[k]));
-    z[i] = cscale(s, 1.0f / A[i][i].x);
+    z[i] = cscale(s, inv[i]);
   }
 #pragma unroll
   for (int i = n - 1; i >= 0; --i) {
     float2 s = z[i];
 #pragma unroll
     for (int k = i + 1; k < n; ++k) s = csub(s, cmulc(A[k][i], x[k]));
-    x[i] = cscale(s, 1.0f / A[i][i].x);
+    x[i] = cscale(s, inv[i]);
   }
   return ok;
 }
@@ -196,18 +195,23 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ideal(FadingConst fc, Fadin
                                                            uint32_t* __restrict__ errors) {
   extern __shared__ float4 smem4[];
   const int w = blockIdx.x, b = blockIdx.y;
-  const int BW = ((C * m) >> 5) + 8;
-  float2* hb = reinterpret_cast<float2*>(smem4);
+  const int BW = staged_bit_words(C, m);
+  float2* tws = reinterpret_cast<float2*>(smem4);  // [N] twiddle table
+  float2* hb = tws + N;
   float2* scratch = hb + fc.L;
   float2* Sm = scratch + fc.L * fc.S1;
   int* ds = reinterpret_cast<int*>(Sm + NRX * NTX);
   uint32_t* bitsm = reinterpret_cast<uint32_t*>(ds + fc.L + 4);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = __ldg(tw + i);
   const int64_t k0 = data_offset[w];
   const int nd = num_data_word[w];
   for (int l = threadIdx.x; l < fc.L; l += blockDim.x) ds[l] = fc.delay[l];
   for (int i = threadIdx.x; i < NRX * NTX; i += blockDim.x) Sm[i] = v.spatial(b)[i];
   stage_bits(bitsm, BW, NTX, seed, drop0 + b, k0, nd, m);
   tap_averages(fc, v.W(b), v.P0(b), window_start[w], N, hb, scratch);  // contains __syncthreads
+  __shared__ QamDemapTable sqt;
+  if (threadIdx.x == 0) sqt = qt;
+  __syncthreads();
   const int64_t wofs = (((k0 * m) >> 5) >> 2) * 4;
   const float s2 = nv ? nv[b] : 0.0f;
   const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
@@ -215,7 +219,7 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ideal(FadingConst fc, Fadin
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
     const int64_t k = k0 + j;
     const int c = data_column[k];
-    const float2 g = tap_response(fc, hb, ds, tw, bins[c], N);
+    const float2 g = tap_response(fc, hb, ds, tws, bins[c], N);
     float2 H[NRX][NTX], y[NRX], x[NTX];
 #pragma unroll
     for (int r = 0; r < NRX; ++r) {
@@ -227,7 +231,7 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ideal(FadingConst fc, Fadin
     for (int t = 0; t < NTX; ++t) {
       // streams the equalizer does not return are received as zero bits
       // (BitErrorEvaluator zero-pads the shorter sequence)
-      const uint32_t rx_v = t < out_streams ? qam_decide(qt, x[t]) : 0u;
+      const uint32_t rx_v = t < out_streams ? qam_decide(sqt, x[t]) : 0u;
       const uint32_t tx_v = extract_bits_msb(bitsm + t * BW - wofs, k * m, m);
       local += __popc(rx_v ^ tx_v);
     }
@@ -251,10 +255,12 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
   extern __shared__ float4 smem4[];
   uint32_t* bitsm = reinterpret_cast<uint32_t*>(smem4);
   const int w = blockIdx.x, b = blockIdx.y;
-  const int BW = ((C * m) >> 5) + 8;
+  const int BW = staged_bit_words(C, m);
   const int64_t k0 = data_offset[w];
   const int nd = num_data_word[w];
   stage_bits(bitsm, BW, 1, seed, drop0 + b, k0, nd, m);
+  __shared__ QamDemapTable sqt;
+  if (threadIdx.x == 0) sqt = qt;
   __syncthreads();
   const int64_t wofs = (((k0 * m) >> 5) >> 2) * 4;
   const float s2 = nv ? nv[b] : 0.0f;
@@ -275,7 +281,7 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
     }
     float2 H[1][1] = {{h}}, y[1] = {gb[w * gcols + c]}, x[1];
     equalize_one<1, 1>(mode, H, y, s2, x);
-    const uint32_t rx_v = qam_decide(qt, x[0]);
+    const uint32_t rx_v = qam_decide(sqt, x[0]);
     const uint32_t tx_v = extract_bits_msb(bitsm - wofs, k * m, m);
     local += __popc(rx_v ^ tx_v);
   }
@@ -328,9 +334,9 @@ hpx_status launch_detect_ideal(const hpx_fading* f, const void* state, const hpx
   HPX_TRY(qam_demap_table(fr->info.modulation_order, &qt));
   const FadingConst fc = fading_const(f);
   const int C = fr->info.num_columns, m = fr->info.bits_per_symbol;
-  const int BW = ((C * m) >> 5) + 8;
-  const size_t smem = (size_t)fc.L * sizeof(float2) * (1 + fc.S1) + NRX * NTX * sizeof(float2) +
-                      (fc.L + 4) * sizeof(int) + (size_t)NTX * BW * 4 + 16;
+  const int BW = staged_bit_words(C, m);
+  const size_t smem = (size_t)fr->info.num_subcarriers * sizeof(float2) + (size_t)fc.L * sizeof(float2) * (1 + fc.S1) +
+                      NRX * NTX * sizeof(float2) + (fc.L + 4) * sizeof(int) + (size_t)NTX * BW * 4 + 16;
   auto kern = k_detect_ideal<NRX, NTX>;
   if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid_dim(fr->info.num_words, B);
@@ -491,7 +497,7 @@ hpx_status hpx_detect_ls(const hpx_ls* ls, int32_t mode, const hpx_cf32* grid, i
   cudaStream_t s = as_stream(stream);
   HPX_CUDA(cudaMemsetAsync(errors, 0, sizeof(uint32_t) * B, s));
   const int C = ls->C, m = fr->info.bits_per_symbol;
-  const size_t smem = (size_t)(((fr->info.num_columns * m) >> 5) + 8) * 4 + 16;
+  const size_t smem = (size_t)staged_bit_words(C, m) * 4 + 16;
   dim3 grid_dim(fr->info.num_words, B);
   k_detect_ls<<<grid_dim, DTHREADS, smem, s>>>(fr->info.num_words, C, m, fr->d_data_offset, fr->d_num_data_word,
                                                fr->d_data_column, ls->d_indptr, ls->d_indices, ls->d_weights,

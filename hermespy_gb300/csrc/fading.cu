@@ -175,17 +175,25 @@ __global__ void k_fading_csi(FadingConst fc, FadingView v, int T, int ntaps, flo
 
 // ------------------------------------------------------------ propagation
 // One block computes BT output samples [m0, m0 + BT) of all receive antennas of
-// one drop; each thread owns RPT consecutive samples. The taps needed by the
-// tile, h_l(t) for t in [m0 - d_l, m0 + BT - d_l), are expanded per tap around
-// the tile centre as a degree-K Taylor polynomial in u = (m - m0 - BT/2) / (BT/2):
+// one drop. Thread t owns two sample pairs, (2t, 2t + 1) and (2t + BT/2,
+// 2t + BT/2 + 1), so that lanes read consecutive 16-byte chunks of the transmit
+// tile and one Philox block gives the AWGN of a pair. The taps needed by the tile,
+// h_l(t) for t in [m0 - d_l, m0 + BT - d_l), are expanded per tap around the tile
+// centre as a degree-K Taylor polynomial in u = (m - m0 - BT/2) / (BT/2):
 //   h_l = sum_k C_lk u^k,  C_lk = (i H)^k / k! sum_n a_n w_n^k exp(i theta_n(t_c)),
-// exact to |w H|^(K+1)/(K+1)! per sinusoid. MODE_DIRECT evaluates every sinusoid
-// at every sample instead (used when the Doppler rate makes the expansion long).
-constexpr int BT = 512;
-constexpr int PTHREADS = 256;
-constexpr int RPT = BT / PTHREADS;
+// exact to |w H|^(K+1)/(K+1)! per sinusoid; u depends on the output sample only,
+// so one set of powers serves every tap. DIRECT evaluates every sinusoid at every
+// sample instead (used when the Doppler rate makes the expansion long).
+// The transmit tile is staged twice, the second copy shifted by one sample, so a
+// pair starting at any tap delay is one aligned 16-byte load.
+// Tile length per transmit-antenna count (shared memory holds 2 NTX tile rows).
+template <int NTX>
+__host__ __device__ constexpr int tile_len() { return NTX <= 4 ? 1024 : (NTX <= 8 ? 512 : 256); }
+constexpr int RPT = 4;  // two pairs per thread: BT / 4 threads per block
 
-template <int NTX, int K, bool DIRECT>
+__host__ __device__ constexpr int tile_width(int BT, int D) { return (BT + D + 2) & ~1; }
+
+template <int NTX, int K, bool DIRECT, int BT = tile_len<NTX>(), int PTHREADS = tile_len<NTX>() / 4>
 __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingView v, int T, const float2* __restrict__ x,
                                                         float2* __restrict__ y, const float* __restrict__ noise_power,
                                                         uint64_t seed, int64_t drop0) {
@@ -193,21 +201,17 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
   const int b = blockIdx.y;
   const int m0 = blockIdx.x * BT;
   const int L = fc.L, S1 = fc.S1, D = fc.D, nrx = fc.nrx;
-  const int XW = BT + D;  // x tile width
-  float2* xs = reinterpret_cast<float2*>(smem4);         // [NTX][XW]
-  float2* coef = xs + NTX * XW;                          // [L][K+1]           (poly)
-  float2* terms = coef + L * (K + 1);                    // [L*S1][K+1]        (poly)
-  int64_t* wp = reinterpret_cast<int64_t*>(terms + (DIRECT ? 0 : L * S1 * (K + 1)));  // [2][L*S1] (direct)
-  float2* Sm = reinterpret_cast<float2*>(wp + (DIRECT ? 2 * L * S1 : 0));             // [nrx*NTX]
-  int* dl = reinterpret_cast<int*>(Sm + nrx * NTX);                                  // [L]
+  const int XW = tile_width(BT, D);                                   // even row width
+  float2* xe = reinterpret_cast<float2*>(smem4);                      // [NTX][XW]: x[m0 - D + i]
+  float2* xo = xe + NTX * XW;                                         // [NTX][XW]: x[m0 - D + i + 1]
+  float2* terms = xe;                                                 // [L*S1][K+1], before the tile load
+  const int region = DIRECT ? 2 * NTX * XW : max(2 * NTX * XW, L * S1 * (K + 1));
+  float2* coef = xe + region;                                         // [L][K+1]
+  int64_t* wp = reinterpret_cast<int64_t*>(coef + L * (K + 1));       // [2][L*S1] (direct)
+  float2* Sm = reinterpret_cast<float2*>(wp + (DIRECT ? 2 * L * S1 : 0));  // [nrx*NTX]
+  int* dl = reinterpret_cast<int*>(Sm + nrx * NTX);                   // [L]
   const int tid = threadIdx.x;
 
-  const float2* xb = x + (int64_t)b * NTX * T;
-  for (int i = tid; i < NTX * XW; i += PTHREADS) {
-    const int tx = i / XW, j = i - tx * XW;
-    const int t = m0 - D + j;
-    xs[i] = (t >= 0 && t < T) ? __ldg(xb + (int64_t)tx * T + t) : make_float2(0.f, 0.f);
-  }
   const float2* Sg = v.spatial(b);
   for (int i = tid; i < nrx * NTX; i += PTHREADS) Sm[i] = Sg[i];
   for (int l = tid; l < L; l += PTHREADS) dl[l] = fc.delay[l];
@@ -238,20 +242,30 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
         dst[k] = t;
       }
     }
-  }
-  __syncthreads();
-  if (!DIRECT) {
+    __syncthreads();
     for (int q = tid; q < L * (K + 1); q += PTHREADS) {
       const int l = q / (K + 1), k = q - l * (K + 1);
       float2 acc = make_float2(0.f, 0.f);
       for (int n = 0; n < S1; ++n) acc = cadd(acc, terms[(l * S1 + n) * (K + 1) + k]);
       coef[q] = acc;
     }
-    __syncthreads();
   }
+  __syncthreads();  // terms consumed: the tile may overwrite them
+  const float2* xb = x + (int64_t)b * NTX * T;
+#pragma unroll 1
+  for (int tx = 0; tx < NTX; ++tx) {
+    const float2* xr = xb + (int64_t)tx * T;
+    for (int j = tid; j <= XW; j += PTHREADS) {
+      const int t = m0 - D + j;
+      const float2 val = (t >= 0 && t < T) ? __ldg(xr + t) : make_float2(0.f, 0.f);
+      if (j < XW) xe[tx * XW + j] = val;
+      if (j > 0) xo[tx * XW + j - 1] = val;
+    }
+  }
+  __syncthreads();
 
   // ---- convolution: z_tx[m] = sum_l h_l[m - d_l] x_tx[m - d_l]
-  const int j0 = tid * RPT;  // first output of this thread within the tile
+  const int jp[2] = {2 * tid, 2 * tid + BT / 2};  // tile index of each pair's first sample
   float2 z[RPT][NTX];
 #pragma unroll
   for (int r = 0; r < RPT; ++r)
@@ -260,11 +274,12 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
   float up[RPT][K + 1];
 #pragma unroll
   for (int r = 0; r < RPT; ++r) {
-    const float u = ((float)(j0 + r) - 0.5f * BT) / (0.5f * BT);
+    const float u = ((float)(jp[r >> 1] + (r & 1)) - 0.5f * BT) / (0.5f * BT);
     up[r][0] = 1.0f;
 #pragma unroll
     for (int k = 1; k <= K; ++k) up[r][k] = up[r][k - 1] * u;
   }
+#pragma unroll 1
   for (int l = 0; l < L; ++l) {
     const int d = dl[l];
     float2 h[RPT];
@@ -272,26 +287,36 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
       const float an = fc.amp[2 * l], al = fc.amp[2 * l + 1];
 #pragma unroll
       for (int r = 0; r < RPT; ++r)
-        h[r] = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al, (int64_t)m0 + j0 + r - d);
+        h[r] = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al,
+                          (int64_t)m0 + jp[r >> 1] + (r & 1) - d);
     } else {
       const float2* cl = coef + l * (K + 1);
+      float2 ck[K + 1];
+#pragma unroll
+      for (int k = 0; k <= K; ++k) ck[k] = cl[k];
 #pragma unroll
       for (int r = 0; r < RPT; ++r) {
-        float2 acc = cl[0];
+        float2 acc = ck[0];
 #pragma unroll
         for (int k = 1; k <= K; ++k) {
-          const float2 ck = cl[k];
-          acc.x = fmaf(ck.x, up[r][k], acc.x);
-          acc.y = fmaf(ck.y, up[r][k], acc.y);
+          acc.x = fmaf(ck[k].x, up[r][k], acc.x);
+          acc.y = fmaf(ck[k].y, up[r][k], acc.y);
         }
         h[r] = acc;
       }
     }
+    // all lanes share the parity of D - d, hence the same copy: conflict-free
+    const int odd = (D - d) & 1;
+    const float2* src = odd ? xo - 1 : xe;
 #pragma unroll
-    for (int tx = 0; tx < NTX; ++tx) {
-      const float2* xr = xs + tx * XW + D + j0 - d;
+    for (int pr = 0; pr < 2; ++pr) {
+      const float2* base = src + jp[pr] - d + D;
 #pragma unroll
-      for (int r = 0; r < RPT; ++r) cfma(z[r][tx], h[r], xr[r]);
+      for (int tx = 0; tx < NTX; ++tx) {
+        const float4 q = *reinterpret_cast<const float4*>(base + tx * XW);
+        cfma(z[2 * pr][tx], h[2 * pr], make_float2(q.x, q.y));
+        cfma(z[2 * pr + 1][tx], h[2 * pr + 1], make_float2(q.z, q.w));
+      }
     }
   }
 
@@ -299,35 +324,31 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
   const int TD = T + D;
   const float np = noise_power ? noise_power[b] : 0.0f;
   const float sigma = sqrtf(0.5f * np);
+#pragma unroll 1
   for (int rx = 0; rx < nrx; ++rx) {
-    float2 out[RPT];
-#pragma unroll
-    for (int r = 0; r < RPT; ++r) {
-      float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int tx = 0; tx < NTX; ++tx) cfma(acc, Sm[rx * NTX + tx], z[r][tx]);
-      out[r] = acc;
-    }
-    const int m = m0 + j0;
-    if (noise_power && np > 0.0f) {
-      // complex sample k of antenna rx: block k/2, words (0,1) for even k, (2,3) for odd k
-#pragma unroll
-      for (int r = 0; r < RPT; r += 2) {
-        const uint4 w = hpx_random_block(seed, drop0 + b, (uint32_t)rx, HPX_DOMAIN_NOISE, (uint32_t)((m + r) >> 1));
-        const float2 n0 = box_muller(w.x, w.y);
-        const float2 n1 = box_muller(w.z, w.w);
-        out[r].x += sigma * n0.x;
-        out[r].y += sigma * n0.y;
-        if (r + 1 < RPT) {
-          out[r + 1].x += sigma * n1.x;
-          out[r + 1].y += sigma * n1.y;
-        }
-      }
-    }
     float2* yr = y + ((int64_t)b * nrx + rx) * TD;
 #pragma unroll
-    for (int r = 0; r < RPT; ++r)
-      if (m + r < TD) yr[m + r] = out[r];
+    for (int pr = 0; pr < 2; ++pr) {
+      float2 o0 = make_float2(0.f, 0.f), o1 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int tx = 0; tx < NTX; ++tx) {
+        cfma(o0, Sm[rx * NTX + tx], z[2 * pr][tx]);
+        cfma(o1, Sm[rx * NTX + tx], z[2 * pr + 1][tx]);
+      }
+      const int m = m0 + jp[pr];
+      if (noise_power && np > 0.0f) {
+        // complex sample k of antenna rx: block k/2, words (0,1) for even k, (2,3) for odd k
+        const uint4 w = hpx_random_block(seed, drop0 + b, (uint32_t)rx, HPX_DOMAIN_NOISE, (uint32_t)(m >> 1));
+        const float2 n0 = box_muller(w.x, w.y);
+        const float2 n1 = box_muller(w.z, w.w);
+        o0.x += sigma * n0.x;
+        o0.y += sigma * n0.y;
+        o1.x += sigma * n1.x;
+        o1.y += sigma * n1.y;
+      }
+      if (m < TD) yr[m] = o0;
+      if (m + 1 < TD) yr[m + 1] = o1;
+    }
   }
 }
 
@@ -336,15 +357,17 @@ __global__ void k_ideal_csi(FadingConst fc, FadingView v, int N, int W, const in
                             const int32_t* __restrict__ bins, const float2* __restrict__ tw, int ncols,
                             float2* __restrict__ csi) {
   extern __shared__ float4 smem4[];
-  float2* hb = reinterpret_cast<float2*>(smem4);
+  float2* tws = reinterpret_cast<float2*>(smem4);  // [N] twiddle table
+  float2* hb = tws + N;
   float2* scratch = hb + fc.L;
   int* ds = reinterpret_cast<int*>(scratch + fc.L * fc.S1);
   const int b = blockIdx.y, w = blockIdx.x;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = __ldg(tw + i);
   for (int l = threadIdx.x; l < fc.L; l += blockDim.x) ds[l] = fc.delay[l];
   tap_averages(fc, v.W(b), v.P0(b), window_start[w], N, hb, scratch);
   const float2* Sm = v.spatial(b);
   for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
-    const float2 g = tap_response(fc, hb, ds, tw, bins[c], N);
+    const float2 g = tap_response(fc, hb, ds, tws, bins[c], N);
     for (int r = 0; r < fc.nrx; ++r)
       for (int t = 0; t < fc.ntx; ++t)
         csi[((((int64_t)b * fc.nrx + r) * fc.ntx + t) * W + w) * ncols + c] = cmul(Sm[r * fc.ntx + t], g);
@@ -361,7 +384,7 @@ void release(hpx_fading* f) {
 }
 
 // Taylor degree for a tile half-width H = BT/2, or -1 for direct evaluation.
-int taylor_degree(const hpx_fading* f) {
+int taylor_degree(const hpx_fading* f, int BT) {
   const double rate = std::fmax(std::fabs(f->doppler), std::fabs(f->los_doppler)) / f->fs;  // rad/sample
   // reduce modulo 2 pi: exp(i w t) only depends on w mod 2 pi for integer t
   double wmax = std::fmod(rate, 2.0 * kPi);
@@ -382,8 +405,10 @@ hpx_status launch_propagate(const hpx_fading* f, const void* state, int B, const
                             const float* np, uint64_t seed, int64_t drop0, cudaStream_t s) {
   const FadingConst fc = fading_const(f);
   const FadingView v = fading_view(f, state);
-  const size_t smem = (size_t)NTX * (BT + fc.D) * sizeof(float2) + (size_t)fc.L * (K + 1) * sizeof(float2) +
-                      (DIRECT ? 0 : (size_t)fc.L * fc.S1 * (K + 1) * sizeof(float2)) +
+  constexpr int BT = tile_len<NTX>();
+  const size_t tile = 2 * (size_t)NTX * tile_width(BT, fc.D) * sizeof(float2);
+  const size_t terms = DIRECT ? 0 : (size_t)fc.L * fc.S1 * (K + 1) * sizeof(float2);
+  const size_t smem = (tile > terms ? tile : terms) + (size_t)fc.L * (K + 1) * sizeof(float2) +
                       (DIRECT ? 2 * (size_t)fc.L * fc.S1 * sizeof(int64_t) : 0) +
                       (size_t)fc.nrx * NTX * sizeof(float2) + (size_t)fc.L * sizeof(int) + 16;
   if (smem > 200 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "propagate: channel too long for one tile");
@@ -391,7 +416,7 @@ hpx_status launch_propagate(const hpx_fading* f, const void* state, int B, const
   if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int TD = T + fc.D;
   dim3 grid((TD + BT - 1) / BT, B);
-  kern<<<grid, PTHREADS, smem, s>>>(fc, v, T, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(y), np,
+  kern<<<grid, BT / 4, smem, s>>>(fc, v, T, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(y), np,
                                     seed, drop0);
   HPX_LAUNCHED("propagate");
   return HPX_OK;
@@ -400,7 +425,7 @@ hpx_status launch_propagate(const hpx_fading* f, const void* state, int B, const
 template <int NTX>
 hpx_status dispatch_degree(const hpx_fading* f, const void* state, int B, const hpx_cf32* x, int T, hpx_cf32* y,
                            const float* np, uint64_t seed, int64_t drop0, cudaStream_t s) {
-  switch (taylor_degree(f)) {
+  switch (taylor_degree(f, tile_len<NTX>())) {
     case 2: return launch_propagate<NTX, 2, false>(f, state, B, x, T, y, np, seed, drop0, s);
     case 4: return launch_propagate<NTX, 4, false>(f, state, B, x, T, y, np, seed, drop0, s);
     case 8: return launch_propagate<NTX, 8, false>(f, state, B, x, T, y, np, seed, drop0, s);
@@ -634,7 +659,7 @@ hpx_status hpx_fading_ideal_csi(const hpx_fading* f, const void* state, int32_t 
   if (B < 0 || ncols < 1 || ncols > N) return hpx_fail(HPX_ERR_ARG, "ideal_csi: bad size");
   if (B == 0) return HPX_OK;
   if (B > 65535) return hpx_fail(HPX_ERR_ARG, "ideal_csi: batch too large");
-  const size_t smem = (size_t)f->L * sizeof(float2) * (1 + f->S1) + f->L * sizeof(int) + 16;
+  const size_t smem = (size_t)N * sizeof(float2) + (size_t)f->L * sizeof(float2) * (1 + f->S1) + f->L * sizeof(int) + 16;
   dim3 grid(W, B);
   k_ideal_csi<<<grid, 256, smem, as_stream(stream)>>>(fading_const(f), fading_view(f, state), N, W,
                                                       frame->d_window_start, frame->d_bins, frame->d_twiddle, ncols,

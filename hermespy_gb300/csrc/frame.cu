@@ -38,7 +38,7 @@ static void release(hpx_frame* f) {
   if (!f) return;
   void* ptrs[] = {f->d_prefix, f->d_zero_prefix, f->d_word_start, f->d_window_start, f->d_data_offset,
                   f->d_num_data_word, f->d_kind, f->d_index, f->d_bins, f->d_data_column, f->d_data_word,
-                  f->d_twiddle, f->d_pilots};
+                  f->d_twiddle, f->d_stage_twiddle, f->d_pilots};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete f;
@@ -129,6 +129,33 @@ hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out) {
     const double a = -2.0 * M_PI * (double)t / (double)N;
     tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
   }
+  // Stockham stage twiddles of the OFDM FFT plans (radices per N as in fft.cuh):
+  // stage with span Ns and radix R stores exp(-2 pi i r k / (Ns R)) at r Ns + k.
+  std::vector<float2> stw(2 * (size_t)N, make_float2(1.f, 0.f));
+  {
+    int radix[3] = {0, 0, 0}, stages = 2;
+    switch (N) {
+      case 64: radix[0] = 8; radix[1] = 8; break;
+      case 128: radix[0] = 16; radix[1] = 8; break;
+      case 256: radix[0] = 16; radix[1] = 16; break;
+      case 512: radix[0] = 16; radix[1] = 16; radix[2] = 2; stages = 3; break;
+      case 1024: radix[0] = 16; radix[1] = 16; radix[2] = 4; stages = 3; break;
+      case 2048: radix[0] = 16; radix[1] = 16; radix[2] = 8; stages = 3; break;
+      default: radix[0] = 16; radix[1] = 16; radix[2] = 16; stages = 3; break;  // 4096
+    }
+    size_t off = 0;
+    int Ns = radix[0];
+    for (int st = 1; st < stages; ++st) {
+      const int R = radix[st];
+      for (int r = 0; r < R; ++r)
+        for (int k = 0; k < Ns; ++k) {
+          const double a = -2.0 * M_PI * (double)r * (double)k / ((double)Ns * R);
+          stw[off + (size_t)r * Ns + k] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+      off += (size_t)R * Ns;
+      Ns *= R;
+    }
+  }
   std::vector<float2> pilots(nr);
   for (int k = 0; k < nr; ++k) pilots[k] = qam_symbol(desc->modulation_order, (uint32_t)(k % desc->modulation_order));
 
@@ -141,7 +168,7 @@ hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out) {
       (s = upload(&f->d_num_data_word, num_data_word)) != HPX_OK ||
       (s = upload(&f->d_kind, f->h_kind)) != HPX_OK || (s = upload(&f->d_index, f->h_index)) != HPX_OK ||
       (s = upload(&f->d_bins, f->h_bins)) != HPX_OK || (s = upload(&f->d_data_column, data_column)) != HPX_OK ||
-      (s = upload(&f->d_data_word, data_word)) != HPX_OK || (s = upload(&f->d_twiddle, tw)) != HPX_OK ||
+      (s = upload(&f->d_data_word, data_word)) != HPX_OK || (s = upload(&f->d_twiddle, tw)) != HPX_OK || (s = upload(&f->d_stage_twiddle, stw)) != HPX_OK ||
       (s = upload(&f->d_pilots, pilots)) != HPX_OK) {
     release(f);
     return s;

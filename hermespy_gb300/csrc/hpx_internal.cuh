@@ -152,6 +152,7 @@ struct hpx_frame {
   int32_t* d_data_column = nullptr;    // [num_data] column of data element k (word via search)
   int32_t* d_data_word = nullptr;      // [num_data] word of data element k
   float2* d_twiddle = nullptr;         // [N] exp(-2 pi i t / N)
+  float2* d_stage_twiddle = nullptr;   // [2N] per-stage tables of the OFDM FFT (fft.cuh)
   float2* d_pilots = nullptr;          // [num_refs]
 };
 
@@ -269,13 +270,18 @@ __device__ __forceinline__ uint32_t qam_decide(const QamDemapTable& t, float2 y)
   return v;
 }
 
+// Words of packed Philox bits staged for the data elements of one OFDM word with
+// C columns and m bits per symbol: the covered words, rounding to whole Philox
+// blocks of 4 words at both ends, and one spare word for 64-bit windows.
+__host__ __device__ inline int staged_bit_words(int C, int m) { return ((C * m) >> 5) + 9; }
+
 // Extract `nb` (<= 8) bits MSB-first starting at stream bit position `pos` from
-// packed little-endian-in-word bit storage (bit b = bit b%32 of word b/32).
+// packed bit storage (stream bit b = bit b%32 of word b/32): one 64-bit window,
+// then a bit reversal puts the first stream bit in the most significant place.
+// `words` must hold one readable word past the last one touched.
 __device__ __forceinline__ uint32_t extract_bits_msb(const uint32_t* words, int64_t pos, int nb) {
-  uint32_t v = 0;
-  for (int i = 0; i < nb; ++i) {
-    const int64_t b = pos + i;
-    v = (v << 1) | ((words[b >> 5] >> (b & 31)) & 1u);
-  }
-  return v;
+  const int64_t w = pos >> 5;
+  const uint64_t win = (uint64_t)words[w] | ((uint64_t)words[w + 1] << 32);
+  const uint32_t raw = (uint32_t)(win >> (pos & 31)) & ((1u << nb) - 1u);
+  return __brev(raw) >> (32 - nb);
 }

@@ -1,15 +1,14 @@
 // OFDM transmit (bits -> QAM -> place -> IFFT -> prefix) and receive
 // (prefix strip -> FFT -> bin gather) kernels with a block-cooperative
 // Stockham FFT in shared memory.
+#include "fft.cuh"
 #include "hpx_internal.cuh"
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kMaxButterflies = 4;  // per thread and stage for N <= 4096 with 256 threads
 
 struct FrameDev {
-  int N, logN, W, C, m, order, T, num_data;
+  int N, W, C, m, order, T, num_data, dc;
   const int32_t* prefix;
   const int32_t* zero_prefix;
   const int32_t* word_start;
@@ -22,20 +21,20 @@ struct FrameDev {
   const int32_t* data_column;
   const int32_t* data_word;
   const float2* twiddle;
+  const float2* stage_twiddle;
   const float2* pilots;
 };
 
 FrameDev frame_dev(const hpx_frame* f) {
   FrameDev d;
   d.N = f->info.num_subcarriers;
-  d.logN = 0;
-  while ((1 << d.logN) < d.N) ++d.logN;
   d.W = f->info.num_words;
   d.C = f->info.num_columns;
   d.m = f->info.bits_per_symbol;
   d.order = f->info.modulation_order;
   d.T = f->info.samples_per_frame;
   d.num_data = f->info.num_data;
+  d.dc = f->dc_suppression;
   d.prefix = f->d_prefix;
   d.zero_prefix = f->d_zero_prefix;
   d.word_start = f->d_word_start;
@@ -48,226 +47,122 @@ FrameDev frame_dev(const hpx_frame* f) {
   d.data_column = f->d_data_column;
   d.data_word = f->d_data_word;
   d.twiddle = f->d_twiddle;
+  d.stage_twiddle = f->d_stage_twiddle;
   d.pilots = f->d_pilots;
   return d;
 }
 
-// Transforms per block: 1024 samples of shared memory work per block for N <= 1024.
-int transforms_per_block(int N) { return N >= 1024 ? 1 : 1024 / N; }
-
-// In-place Stockham autosort FFT of F transforms of length N = 2^logN stored
-// back to back in `buf`, executed by all threads of the block. Stage with radix R
-// and span Ns: butterfly j reads buf[j + r N/R], applies exp(-+2 pi i r k/(Ns R))
-// with k = j mod Ns, and writes buf[(j - k) R + k + r Ns]. Forward: exp(-2 pi i ...);
-// INVERSE: exp(+2 pi i ...), unscaled.
-template <bool INVERSE>
-__device__ void block_fft(float2* buf, int N, int logN, int F, const float2* __restrict__ tw) {
-  const int tid = threadIdx.x;
-  int Ns = 1;
-  if (logN & 1) {
-    const int half = N >> 1;
-    const int nb = F * half;
-    float2 y[kMaxButterflies][2];
-    int jj[kMaxButterflies], ff[kMaxButterflies];
-#pragma unroll
-    for (int i = 0; i < kMaxButterflies; ++i) {
-      const int q = tid + i * kThreads;
-      if (q < nb) {
-        const int f = q / half, j = q - f * half;
-        const float2 a0 = buf[f * N + j], a1 = buf[f * N + j + half];
-        y[i][0] = cadd(a0, a1);
-        y[i][1] = csub(a0, a1);
-        jj[i] = j;
-        ff[i] = f;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < kMaxButterflies; ++i) {
-      const int q = tid + i * kThreads;
-      if (q < nb) {
-        float2* b = buf + ff[i] * N;
-        b[2 * jj[i]] = y[i][0];
-        b[2 * jj[i] + 1] = y[i][1];
-      }
-    }
-    __syncthreads();
-    Ns = 2;
-  }
-  const int quarter = N >> 2;
-  const int nb = F * quarter;
-  for (; Ns < N; Ns <<= 2) {
-    const int stride = N / (Ns * 4);
-    float2 y[kMaxButterflies][4];
-    int jj[kMaxButterflies], ff[kMaxButterflies];
-#pragma unroll
-    for (int i = 0; i < kMaxButterflies; ++i) {
-      const int q = tid + i * kThreads;
-      if (q < nb) {
-        const int f = q / quarter, j = q - f * quarter;
-        const int k = j & (Ns - 1);
-        const float2* b = buf + f * N;
-        float2 a0 = b[j], a1 = b[j + quarter], a2 = b[j + 2 * quarter], a3 = b[j + 3 * quarter];
-        if (Ns > 1) {
-          const int t1 = (k * stride) & (N - 1);
-          const int t2 = (2 * k * stride) & (N - 1);
-          const int t3 = (3 * k * stride) & (N - 1);
-          float2 w1 = __ldg(tw + t1), w2 = __ldg(tw + t2), w3 = __ldg(tw + t3);
-          if (INVERSE) {
-            w1.y = -w1.y;
-            w2.y = -w2.y;
-            w3.y = -w3.y;
-          }
-          a1 = cmul(a1, w1);
-          a2 = cmul(a2, w2);
-          a3 = cmul(a3, w3);
-        }
-        const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3);
-        const float2 d = csub(a1, a3);
-        // forward: (a1 - a3) * (-i); inverse: (a1 - a3) * (+i)
-        const float2 t3 = INVERSE ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
-        y[i][0] = cadd(t0, t2);
-        y[i][1] = cadd(t1, t3);
-        y[i][2] = csub(t0, t2);
-        y[i][3] = csub(t1, t3);
-        jj[i] = (j - k) * 4 + k;
-        ff[i] = f;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < kMaxButterflies; ++i) {
-      const int q = tid + i * kThreads;
-      if (q < nb) {
-        float2* b = buf + ff[i] * N + jj[i];
-        b[0] = y[i][0];
-        b[Ns] = y[i][1];
-        b[2 * Ns] = y[i][2];
-        b[3 * Ns] = y[i][3];
-      }
-    }
-    __syncthreads();
-  }
+// Grid column of an FFT bin (inverse of hpx_frame::h_bins; ofdm.py:116-128, 146-151).
+__device__ __forceinline__ int column_of_bin(int b, int N, bool dc) {
+  if (!dc) return (b + N / 2) & (N - 1);
+  if (b >= N / 2) return b - N / 2;
+  return b == 0 ? N - 1 : b + N / 2 - 1;
 }
 
-// Words of packed Philox bits a block stages per transform.
-__host__ __device__ inline int bit_words(int C, int m) { return ((C * m) >> 5) + 8; }
 
-// MODE 0: data symbols from `data` [items][num_data]; MODE 1: Philox bits of
-// drop item / num_streams, stream item % num_streams; MODE 2: a placed grid
-// `data` [items][W][num_streams] (num_streams carries the grid width).
-template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_ofdm_tx(FrameDev fr, int F, int num_pairs, const float2* __restrict__ data,
-                                                      uint64_t seed, int64_t drop0, int num_streams,
-                                                      float2* __restrict__ out) {
+template <int N>
+constexpr int groups_per_block() {
+  return fft::Plan<N>::TP >= 128 ? 1 : 128 / fft::Plan<N>::TP;
+}
+
+// Symbol of data element k from staged packed bits.
+__device__ __forceinline__ float2 symbol_from_bits(const uint32_t* words, int64_t pos, int m, int order) {
+  return qam_symbol(order, extract_bits_msb(words, pos, m));
+}
+
+// MODE 0: data symbols `data` [items][num_data]; MODE 1: Philox bits of drop
+// item / num_streams, stream item % num_streams; MODE 2: a placed grid `data`
+// [items][W][G] with G = num_streams columns.
+template <int N, int MODE>
+__global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>())
+    k_ofdm_tx(FrameDev fr, int num_pairs, const float2* __restrict__ data, uint64_t seed, int64_t drop0,
+              int num_streams, float2* __restrict__ out) {
+  constexpr int TP = fft::Plan<N>::TP;
+  constexpr int F = groups_per_block<N>();
+  constexpr int PN = N + N / 32;
   extern __shared__ float4 smem4[];
-  float2* sm = reinterpret_cast<float2*>(smem4);
-  const int N = fr.N, W = fr.W, C = fr.C;
-  const int BW = bit_words(C, fr.m);
-  uint32_t* bitsm = reinterpret_cast<uint32_t*>(sm + F * N);
-  const int p0 = blockIdx.x * F;
-  const int tid = threadIdx.x;
-
-  for (int i = tid; i < F * N; i += kThreads) sm[i] = make_float2(0.f, 0.f);
-  if (MODE == 1) {
-    for (int f = 0; f < F; ++f) {
-      const int p = p0 + f;
-      if (p >= num_pairs) break;
-      const int item = p / W, w = p - item * W;
-      const int drop = item / num_streams, s = item - drop * num_streams;
-      const int64_t k0 = fr.data_offset[w];
-      const int nd = fr.num_data_word[w];
-      if (nd == 0) continue;
-      const int64_t wa = (k0 * fr.m) >> 5, wb = ((k0 + nd) * fr.m - 1) >> 5;
-      const int64_t blk0 = wa >> 2, blk1 = wb >> 2;
-      for (int64_t blk = blk0 + tid; blk <= blk1; blk += kThreads) {
+  const int g = threadIdx.x / TP, t = threadIdx.x - g * TP;
+  float2* buf = reinterpret_cast<float2*>(smem4) + g * PN;
+  const int BW = staged_bit_words(fr.C, fr.m);
+  uint32_t* bits = reinterpret_cast<uint32_t*>(reinterpret_cast<float2*>(smem4) + F * PN) + g * BW;
+  const int p = blockIdx.x * F + g;
+  const bool valid = p < num_pairs;
+  const int item = valid ? p / fr.W : 0, w = valid ? p - item * fr.W : 0;
+  const int C = fr.C;
+  const bool dc = fr.dc != 0;
+  const float scale = rsqrtf((float)N);
+  int64_t wofs = 0;
+  if (MODE == 1 && valid) {
+    const int drop = item / num_streams, s = item - drop * num_streams;
+    const int64_t k0 = fr.data_offset[w];
+    const int nd = fr.num_data_word[w];
+    if (nd > 0) {
+      const int64_t blk0 = ((k0 * fr.m) >> 5) >> 2, blk1 = (((k0 + nd) * fr.m - 1) >> 5) >> 2;
+      for (int64_t blk = blk0 + t; blk <= blk1; blk += TP) {
         const uint4 r = hpx_random_block(seed, drop0 + drop, (uint32_t)s, HPX_DOMAIN_BITS, (uint32_t)blk);
-        uint32_t* dst = bitsm + f * BW + (blk - blk0) * 4;
+        uint32_t* dst = bits + (blk - blk0) * 4;
         dst[0] = r.x;
         dst[1] = r.y;
         dst[2] = r.z;
         dst[3] = r.w;
       }
+      wofs = blk0 * 4;
     }
   }
-  __syncthreads();
-  const float inv_sqrt_n = rsqrtf((float)N);
-  if (MODE == 2) {
-    const int G = num_streams;
-    for (int q = tid; q < F * G; q += kThreads) {
-      const int f = q / G, c = q - f * G;
-      const int p = p0 + f;
-      if (p >= num_pairs) continue;
-      sm[f * N + fr.bins[c]] = cscale(data[(int64_t)p * G + c], inv_sqrt_n);
-    }
-  }
-  for (int q = tid; MODE != 2 && q < F * C; q += kThreads) {
-    const int f = q / C, c = q - f * C;
-    const int p = p0 + f;
-    if (p >= num_pairs) continue;
-    const int item = p / W, w = p - item * W;
-    const int kind = fr.kind[w * C + c];
+  if (MODE == 1) fft::sync_group<TP>();
+  const uint32_t* words = bits - wofs;
+  auto load = [&](int b) -> float2 {
+    if (!valid) return make_float2(0.f, 0.f);
+    const int c = column_of_bin(b, N, dc);
     float2 v = make_float2(0.f, 0.f);
-    if (kind == HPX_RE_DATA) {
-      const int k = fr.index[w * C + c];
-      if (MODE == 0) {
-        v = data[(int64_t)item * fr.num_data + k];
-      } else {
-        const int64_t k0 = fr.data_offset[w];
-        const int64_t blk0 = ((k0 * fr.m) >> 5) >> 2;
-        const uint32_t* words = bitsm + f * BW - blk0 * 4;
-        v = qam_symbol(fr.order, extract_bits_msb(words, (int64_t)k * fr.m, fr.m));
+    if (MODE == 2) {
+      if (c < num_streams) v = data[(int64_t)p * num_streams + c];
+    } else if (c < C) {
+      const int kind = fr.kind[w * C + c];
+      if (kind == HPX_RE_DATA) {
+        const int k = fr.index[w * C + c];
+        if (MODE == 0) v = data[(int64_t)item * fr.num_data + k];
+        else v = symbol_from_bits(words, (int64_t)k * fr.m, fr.m, fr.order);
+      } else if (kind == HPX_RE_REFERENCE) {
+        v = fr.pilots[fr.index[w * C + c]];
       }
-    } else if (kind == HPX_RE_REFERENCE) {
-      v = fr.pilots[fr.index[w * C + c]];
     }
-    sm[f * N + fr.bins[c]] = cscale(v, inv_sqrt_n);
-  }
-  __syncthreads();
-  block_fft<true>(sm, N, fr.logN, F, fr.twiddle);
-  for (int f = 0; f < F; ++f) {
-    const int p = p0 + f;
-    if (p >= num_pairs) break;
-    const int item = p / W, w = p - item * W;
-    const int P = fr.prefix[w];
-    const bool zp = fr.zero_prefix[w] != 0;
-    float2* dst = out + (int64_t)item * fr.T + fr.word_start[w];
-    const float2* src = sm + f * N;
-    for (int i = tid; i < P + N; i += kThreads) {
-      float2 v;
-      if (i < P) v = zp ? make_float2(0.f, 0.f) : src[N - P + i];
-      else v = src[i - P];
-      dst[i] = v;
-    }
-  }
+    return cscale(v, scale);
+  };
+  float2* dst = out + (int64_t)item * fr.T + fr.word_start[w];
+  const int P = valid ? fr.prefix[w] : 0;
+  const bool zp = valid && fr.zero_prefix[w] != 0;
+  auto store = [&](int n, float2 v) {
+    if (!valid) return;
+    dst[P + n] = v;
+    if (n >= N - P) dst[n - (N - P)] = zp ? make_float2(0.f, 0.f) : v;
+  };
+  fft::transform<N, true>(buf, t, fr.stage_twiddle, load, store);
 }
 
-__global__ void __launch_bounds__(kThreads) k_ofdm_rx(FrameDev fr, int F, int num_pairs, const float2* __restrict__ in,
-                                                      int64_t stride, int ncols, float2* __restrict__ grid) {
+template <int N>
+__global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>())
+    k_ofdm_rx(FrameDev fr, int num_pairs, const float2* __restrict__ in, int64_t stride, int ncols,
+              float2* __restrict__ grid) {
+  constexpr int TP = fft::Plan<N>::TP;
+  constexpr int F = groups_per_block<N>();
+  constexpr int PN = N + N / 32;
   extern __shared__ float4 smem4[];
-  float2* sm = reinterpret_cast<float2*>(smem4);
-  const int N = fr.N, W = fr.W;
-  const int p0 = blockIdx.x * F;
-  const int tid = threadIdx.x;
-  for (int f = 0; f < F; ++f) {
-    const int p = p0 + f;
-    if (p >= num_pairs) {
-      for (int i = tid; i < N; i += kThreads) sm[f * N + i] = make_float2(0.f, 0.f);
-      continue;
-    }
-    const int item = p / W, w = p - item * W;
-    const float2* src = in + (int64_t)item * stride + fr.window_start[w];
-    for (int i = tid; i < N; i += kThreads) sm[f * N + i] = __ldg(src + i);
-  }
-  __syncthreads();
-  block_fft<false>(sm, N, fr.logN, F, fr.twiddle);
-  const float inv_sqrt_n = rsqrtf((float)N);
-  for (int q = tid; q < F * ncols; q += kThreads) {
-    const int f = q / ncols, c = q - f * ncols;
-    const int p = p0 + f;
-    if (p >= num_pairs) continue;
-    grid[(int64_t)p * ncols + c] = cscale(sm[f * N + fr.bins[c]], inv_sqrt_n);
-  }
+  const int g = threadIdx.x / TP, t = threadIdx.x - g * TP;
+  float2* buf = reinterpret_cast<float2*>(smem4) + g * PN;
+  const int p = blockIdx.x * F + g;
+  const bool valid = p < num_pairs;
+  const int item = valid ? p / fr.W : 0, w = valid ? p - item * fr.W : 0;
+  const bool dc = fr.dc != 0;
+  const float scale = rsqrtf((float)N);
+  const float2* src = in + (int64_t)item * stride + fr.window_start[w];
+  float2* dst = grid + (int64_t)p * ncols;
+  auto load = [&](int n) -> float2 { return valid ? __ldg(src + n) : make_float2(0.f, 0.f); };
+  auto store = [&](int b, float2 v) {
+    const int c = column_of_bin(b, N, dc);
+    if (valid && c < ncols) dst[c] = cscale(v, scale);
+  };
+  fft::transform<N, false>(buf, t, fr.stage_twiddle, load, store);
 }
 
 __global__ void k_ofdm_pick(FrameDev fr, const float2* __restrict__ grid, int gcols, int batch, float2* __restrict__ out) {
@@ -279,8 +174,61 @@ __global__ void k_ofdm_pick(FrameDev fr, const float2* __restrict__ grid, int gc
   }
 }
 
-size_t tx_smem(const FrameDev& d, int F, int mode) {
-  return (size_t)F * d.N * sizeof(float2) + (mode == 1 ? (size_t)F * bit_words(d.C, d.m) * 4 : 0);
+template <int N, int MODE>
+hpx_status launch_tx_n(const FrameDev& d, int pairs, const float2* data, uint64_t seed, int64_t drop0, int ns,
+                       float2* out, cudaStream_t s) {
+  constexpr int F = groups_per_block<N>();
+  constexpr int threads = fft::Plan<N>::TP * F;
+  const size_t smem = (size_t)F * (N + N / 32) * sizeof(float2) + (MODE == 1 ? (size_t)F * staged_bit_words(d.C, d.m) * 4 : 0);
+  auto kern = k_ofdm_tx<N, MODE>;
+  if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int blocks = (pairs + F - 1) / F;
+  kern<<<blocks, threads, smem, s>>>(d, pairs, data, seed, drop0, ns, out);
+  HPX_LAUNCHED("ofdm_tx");
+  return HPX_OK;
+}
+
+template <int MODE>
+hpx_status launch_tx(const FrameDev& d, int pairs, const float2* data, uint64_t seed, int64_t drop0, int ns,
+                     float2* out, cudaStream_t s) {
+  switch (d.N) {
+    case 64: return launch_tx_n<64, MODE>(d, pairs, data, seed, drop0, ns, out, s);
+    case 128: return launch_tx_n<128, MODE>(d, pairs, data, seed, drop0, ns, out, s);
+    case 256: return launch_tx_n<256, MODE>(d, pairs, data, seed, drop0, ns, out, s);
+    case 512: return launch_tx_n<512, MODE>(d, pairs, data, seed, drop0, ns, out, s);
+    case 1024: return launch_tx_n<1024, MODE>(d, pairs, data, seed, drop0, ns, out, s);
+    case 2048: return launch_tx_n<2048, MODE>(d, pairs, data, seed, drop0, ns, out, s);
+    case 4096: return launch_tx_n<4096, MODE>(d, pairs, data, seed, drop0, ns, out, s);
+    default: return hpx_fail(HPX_ERR_UNSUPPORTED, "FFT size %d not supported", d.N);
+  }
+}
+
+template <int N>
+hpx_status launch_rx_n(const FrameDev& d, int pairs, const float2* in, int64_t stride, int ncols, float2* grid,
+                       cudaStream_t s) {
+  constexpr int F = groups_per_block<N>();
+  constexpr int threads = fft::Plan<N>::TP * F;
+  const size_t smem = (size_t)F * (N + N / 32) * sizeof(float2);
+  auto kern = k_ofdm_rx<N>;
+  if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int blocks = (pairs + F - 1) / F;
+  kern<<<blocks, threads, smem, s>>>(d, pairs, in, stride, ncols, grid);
+  HPX_LAUNCHED("ofdm_rx");
+  return HPX_OK;
+}
+
+hpx_status launch_rx(const FrameDev& d, int pairs, const float2* in, int64_t stride, int ncols, float2* grid,
+                     cudaStream_t s) {
+  switch (d.N) {
+    case 64: return launch_rx_n<64>(d, pairs, in, stride, ncols, grid, s);
+    case 128: return launch_rx_n<128>(d, pairs, in, stride, ncols, grid, s);
+    case 256: return launch_rx_n<256>(d, pairs, in, stride, ncols, grid, s);
+    case 512: return launch_rx_n<512>(d, pairs, in, stride, ncols, grid, s);
+    case 1024: return launch_rx_n<1024>(d, pairs, in, stride, ncols, grid, s);
+    case 2048: return launch_rx_n<2048>(d, pairs, in, stride, ncols, grid, s);
+    case 4096: return launch_rx_n<4096>(d, pairs, in, stride, ncols, grid, s);
+    default: return hpx_fail(HPX_ERR_UNSUPPORTED, "FFT size %d not supported", d.N);
+  }
 }
 
 }  // namespace
@@ -294,15 +242,10 @@ hpx_status hpx_ofdm_modulate(const hpx_frame* frame, const hpx_cf32* data, int32
   if (batch == 0) return HPX_OK;
   if (!samples || (!data && frame->info.num_data > 0)) return hpx_fail(HPX_ERR_ARG, "modulate: null pointer");
   const FrameDev d = frame_dev(frame);
-  const int F = transforms_per_block(d.N);
   const int64_t pairs = (int64_t)batch * d.W;
   if (pairs > (1ll << 31) - 1) return hpx_fail(HPX_ERR_ARG, "modulate: batch too large");
-  const size_t smem = tx_smem(d, F, 0);
-  const int blocks = (int)((pairs + F - 1) / F);
-  k_ofdm_tx<0><<<blocks, kThreads, smem, as_stream(stream)>>>(d, F, (int)pairs, reinterpret_cast<const float2*>(data),
-                                                                0, 0, 1, reinterpret_cast<float2*>(samples));
-  HPX_LAUNCHED("modulate");
-  return HPX_OK;
+  return launch_tx<0>(d, (int)pairs, reinterpret_cast<const float2*>(data), 0, 0, 1, reinterpret_cast<float2*>(samples),
+                      as_stream(stream));
 }
 
 hpx_status hpx_ofdm_modulate_grid(const hpx_frame* frame, const hpx_cf32* grid, int32_t grid_columns, int32_t batch,
@@ -313,15 +256,10 @@ hpx_status hpx_ofdm_modulate_grid(const hpx_frame* frame, const hpx_cf32* grid, 
   if (grid_columns < 1 || grid_columns > d.N) return hpx_fail(HPX_ERR_SHAPE, "modulate_grid: grid width out of range");
   if (batch == 0) return HPX_OK;
   if (!samples || !grid) return hpx_fail(HPX_ERR_ARG, "modulate_grid: null pointer");
-  const int F = transforms_per_block(d.N);
   const int64_t pairs = (int64_t)batch * d.W;
   if (pairs > (1ll << 31) - 1) return hpx_fail(HPX_ERR_ARG, "modulate_grid: batch too large");
-  const size_t smem = tx_smem(d, F, 0);
-  const int blocks = (int)((pairs + F - 1) / F);
-  k_ofdm_tx<2><<<blocks, kThreads, smem, as_stream(stream)>>>(d, F, (int)pairs, reinterpret_cast<const float2*>(grid),
-                                                                0, 0, grid_columns, reinterpret_cast<float2*>(samples));
-  HPX_LAUNCHED("modulate_grid");
-  return HPX_OK;
+  return launch_tx<2>(d, (int)pairs, reinterpret_cast<const float2*>(grid), 0, 0, grid_columns,
+                      reinterpret_cast<float2*>(samples), as_stream(stream));
 }
 
 hpx_status hpx_ofdm_modulate_bits(const hpx_frame* frame, uint64_t seed, int64_t drop0, int32_t num_drops,
@@ -331,17 +269,10 @@ hpx_status hpx_ofdm_modulate_bits(const hpx_frame* frame, uint64_t seed, int64_t
   if (num_drops == 0) return HPX_OK;
   if (!samples) return hpx_fail(HPX_ERR_ARG, "modulate_bits: null output");
   const FrameDev d = frame_dev(frame);
-  const int F = transforms_per_block(d.N);
   const int64_t pairs = (int64_t)num_drops * num_streams * d.W;
   if (pairs > (1ll << 31) - 1) return hpx_fail(HPX_ERR_ARG, "modulate_bits: batch too large");
-  const size_t smem = tx_smem(d, F, 1);
-  if (smem > 48 * 1024)
-    HPX_CUDA(cudaFuncSetAttribute(k_ofdm_tx<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int blocks = (int)((pairs + F - 1) / F);
-  k_ofdm_tx<1><<<blocks, kThreads, smem, as_stream(stream)>>>(d, F, (int)pairs, nullptr, seed, drop0, num_streams,
-                                                                reinterpret_cast<float2*>(samples));
-  HPX_LAUNCHED("modulate_bits");
-  return HPX_OK;
+  return launch_tx<1>(d, (int)pairs, nullptr, seed, drop0, num_streams, reinterpret_cast<float2*>(samples),
+                      as_stream(stream));
 }
 
 hpx_status hpx_ofdm_demodulate(const hpx_frame* frame, const hpx_cf32* samples, int64_t sample_stride, int32_t batch,
@@ -353,15 +284,10 @@ hpx_status hpx_ofdm_demodulate(const hpx_frame* frame, const hpx_cf32* samples, 
   if (num_columns < 1 || num_columns > d.N) return hpx_fail(HPX_ERR_ARG, "demodulate: num_columns out of range");
   if (sample_stride < d.T) return hpx_fail(HPX_ERR_SHAPE, "demodulate: fewer samples than one frame");
   if (!samples || !grid) return hpx_fail(HPX_ERR_ARG, "demodulate: null pointer");
-  const int F = transforms_per_block(d.N);
   const int64_t pairs = (int64_t)batch * d.W;
   if (pairs > (1ll << 31) - 1) return hpx_fail(HPX_ERR_ARG, "demodulate: batch too large");
-  const size_t smem = (size_t)F * d.N * sizeof(float2);
-  const int blocks = (int)((pairs + F - 1) / F);
-  k_ofdm_rx<<<blocks, kThreads, smem, as_stream(stream)>>>(d, F, (int)pairs, reinterpret_cast<const float2*>(samples),
-                                                           sample_stride, num_columns, reinterpret_cast<float2*>(grid));
-  HPX_LAUNCHED("demodulate");
-  return HPX_OK;
+  return launch_rx(d, (int)pairs, reinterpret_cast<const float2*>(samples), sample_stride, num_columns,
+                   reinterpret_cast<float2*>(grid), as_stream(stream));
 }
 
 hpx_status hpx_ofdm_pick(const hpx_frame* frame, const hpx_cf32* grid, int32_t grid_columns, int32_t batch,

@@ -71,6 +71,8 @@ class LinkEngine:
         self._fading = channel.handle(num_rx, num_tx, sampling_rate)
         self._frame = waveform._frame()
         self._ls = None
+        if estimator == "ls" and (num_tx != 1 or num_rx != 1):
+            raise NotImplementedError("Least-Squares channel estimation is only implemented for SISO links")
         if estimator == "ls":
             mask = waveform.resource_mask[0]
             indptr, indices, weights = ls_interpolation_table(mask[:, : waveform._layout()["num_columns"]])

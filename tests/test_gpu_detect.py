@@ -43,8 +43,8 @@ def test_zf_golden(golden, name):
     nrx, ntx, K = h.shape
     out_streams = 1 if nrx == 1 else ntx
     x = torch.empty((1, out_streams, K), dtype=torch.complex64, device="cuda")
-    _lib.call("hpx_equalize", _lib.EQ_ZF, nrx, ntx, K, 1, _lib.ptr(cf(h[None])), _lib.ptr(cf(y[None])), None,
-              _lib.ptr(x), stream())
+    hd, yd = cf(h[None]), cf(y[None])  # keep the inputs alive until the kernel has run
+    _lib.call("hpx_equalize", _lib.EQ_ZF, nrx, ntx, K, 1, _lib.ptr(hd), _lib.ptr(yd), None, _lib.ptr(x), stream())
     # random 4x4 matrices can be ill conditioned: float32 vs float64 pseudo-inverse
     assert rel_rms(host(x)[0], g[f"{name}_x"]) < 1e-4
 
@@ -59,8 +59,9 @@ def test_lmmse_matches_oracle(nrx, ntx):
     x = torch.empty((1, ntx, K), dtype=torch.complex64, device="cuda")
     nv = torch.tensor([s2], dtype=torch.float32, device="cuda")
     h32, y32 = h.astype(np.complex64), y.astype(np.complex64)
-    _lib.call("hpx_equalize", _lib.EQ_LMMSE, nrx, ntx, K, 1, _lib.ptr(cf(h32[None])), _lib.ptr(cf(y32[None])),
-              _lib.ptr(nv), _lib.ptr(x), stream())
+    hd, yd = cf(h32[None]), cf(y32[None])
+    _lib.call("hpx_equalize", _lib.EQ_LMMSE, nrx, ntx, K, 1, _lib.ptr(hd), _lib.ptr(yd), _lib.ptr(nv), _lib.ptr(x),
+              stream())
     ref = estimation.lmmse_equalize(y32.astype(np.complex128), h32.astype(np.complex128), s2)
     assert rel_rms(host(x)[0], ref) < 1e-5
 

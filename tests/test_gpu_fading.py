@@ -155,7 +155,7 @@ def test_correlated_massive_spatial():
     rng = np.random.default_rng(2)
     x = ((rng.standard_normal((16, T)) + 1j * rng.standard_normal((16, T))) / np.sqrt(2)).astype(np.complex64)
     y = torch.empty((1, 64, T + h.max_delay), dtype=torch.complex64, device="cuda")
-    _lib.call("hpx_fading_propagate", h.handle, _lib.ptr(st), 1, _lib.ptr(cf(x)), T, _lib.ptr(y), None, 0, 0,
-              stream())
+    xd = cf(x)
+    _lib.call("hpx_fading_propagate", h.handle, _lib.ptr(st), 1, _lib.ptr(xd), T, _lib.ptr(y), None, 0, 0, stream())
     smp = fading.realize(cfg, SEED, 1, 64, 16)
     assert rel_rms(host(y)[0], fading.propagate(smp, x.astype(np.complex128), fs)) < TOL
