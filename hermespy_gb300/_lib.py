@@ -111,6 +111,8 @@ _SIGNATURES = {
     "hpx_link_create": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, ctypes.POINTER(c_void_p)],
     "hpx_link_destroy": [c_void_p],
     "hpx_link_run": [c_void_p, c_uint64, c_int64, c_int32, c_void_p, c_void_p, c_void_p],
+    "hpx_link_run_static": [c_void_p, c_void_p, c_void_p, c_int32, c_uint64, c_int64, c_int32, c_void_p, c_void_p,
+                            c_void_p],
     "hpx_detect_ls": [c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64, c_int64, c_int32, c_void_p, c_void_p],
 }
 

@@ -288,6 +288,23 @@ hpx_status hpx_link_destroy(hpx_link* link);
 hpx_status hpx_link_run(const hpx_link* link, uint64_t seed, int64_t drop0, int32_t num_drops,
                         const float* noise_power, uint32_t* errors, void* stream);
 
+/* The batched drop loop of hpx_link_run for callers that cannot allocate device
+ * memory (a host whose device memory is reserved by its own pool allocator,
+ * latency-critical loops that must not call cudaMalloc after start-up, plugins
+ * that may not own device allocations). No counterpart in the reference: it is an
+ * allocation-free variant of this library's own hpx_link_run. Its scratch is one
+ * fixed 64 MiB array in the library's device image, held by every GPU that loads
+ * the library until the process exits; the largest batch is what fits in it
+ * (about 50 drops of the 4x4, 1024-subcarrier link), larger batches fail with
+ * HPX_ERR_ARG and a message giving the limit. `ls` selects LS estimation (SISO,
+ * table built on the frame's columns); NULL selects ideal CSI. The first call on a
+ * device looks up the array's device address and must come before any stream
+ * capture. Calls share the array: calls that overlap on the GPU race. Never calls
+ * cudaMalloc or cudaFree. */
+hpx_status hpx_link_run_static(const hpx_frame* frame, const hpx_fading* fading, const hpx_ls* ls,
+                               int32_t equalizer, uint64_t seed, int64_t drop0, int32_t num_drops,
+                               const float* noise_power, uint32_t* errors, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
