@@ -38,6 +38,7 @@ class FrameDesc(ctypes.Structure):
         ("prefix", ctypes.POINTER(c_int32)),
         ("zero_prefix", ctypes.POINTER(c_int32)),
         ("kind", ctypes.POINTER(ctypes.c_int8)),
+        ("pilot_comb", c_int32),
     ]
 
 
@@ -114,6 +115,8 @@ _SIGNATURES = {
     "hpx_link_run_static": [c_void_p, c_void_p, c_void_p, c_int32, c_uint64, c_int64, c_int32, c_void_p, c_void_p,
                             c_void_p],
     "hpx_detect_ls": [c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64, c_int64, c_int32, c_void_p, c_void_p],
+    "hpx_detect_csi": [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64,
+                       c_int64, c_int32, c_void_p, c_void_p],
 }
 
 _lock = threading.Lock()

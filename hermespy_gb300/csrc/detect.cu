@@ -179,39 +179,48 @@ __device__ __forceinline__ void block_count(unsigned int local, uint32_t* out) {
   }
 }
 
-constexpr int DTHREADS = 256;
+// Fused receivers run one block per (word, drop) whose threads stride over the
+// word's data elements. The block size is picked per frame so that the strides
+// cover the most data elements of a word with little idle tail, up to a cap that
+// keeps the large MIMO instantiations within the register file.
+constexpr int DTHREADS = 384;
+template <int NRX, int NTX>
+constexpr int detect_max_threads() { return NRX * NTX >= 32 ? 128 : DTHREADS; }
+
+int detect_threads(int max_nd, int cap) {
+  const int iters = max_nd > cap ? (max_nd + cap - 1) / cap : 1;
+  int t = (max_nd + iters - 1) / iters;
+  t = (t + 31) / 32 * 32;
+  return t < 32 ? 32 : (t > cap ? cap : t);
+}
 
 // Fused ideal-CSI receiver, one block per (word, drop).
 template <int NRX, int NTX>
-__global__ void __launch_bounds__(DTHREADS) k_detect_ideal(FadingConst fc, FadingView v, int N, int W, int C, int m,
+__global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_ideal(FadingConst fc, FadingView v, int N, int W, int C, int m,
                                                            const int32_t* __restrict__ window_start,
                                                            const int32_t* __restrict__ data_offset,
                                                            const int32_t* __restrict__ num_data_word,
                                                            const int32_t* __restrict__ data_column,
                                                            const int32_t* __restrict__ bins,
-                                                           const float2* __restrict__ tw, QamDemapTable qt, int mode,
+                                                           const float2* __restrict__ tw, const __grid_constant__ QamDemapTable qt, int mode,
                                                            const float2* __restrict__ grid, int gcols,
                                                            const float* __restrict__ nv, uint64_t seed, int64_t drop0,
                                                            uint32_t* __restrict__ errors) {
   extern __shared__ float4 smem4[];
   const int w = blockIdx.x, b = blockIdx.y;
   const int BW = staged_bit_words(C, m);
-  float2* tws = reinterpret_cast<float2*>(smem4);  // [N] twiddle table
-  float2* hb = tws + N;
+  float2* hb = reinterpret_cast<float2*>(smem4);
   float2* scratch = hb + fc.L;
   float2* Sm = scratch + fc.L * fc.S1;
   int* ds = reinterpret_cast<int*>(Sm + NRX * NTX);
   uint32_t* bitsm = reinterpret_cast<uint32_t*>(ds + fc.L + 4);
-  for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = __ldg(tw + i);
   const int64_t k0 = data_offset[w];
   const int nd = num_data_word[w];
   for (int l = threadIdx.x; l < fc.L; l += blockDim.x) ds[l] = fc.delay[l];
-  for (int i = threadIdx.x; i < NRX * NTX; i += blockDim.x) Sm[i] = v.spatial(b)[i];
+  const float2* Sg = v.spatial(b);
+  for (int i = threadIdx.x; i < NRX * NTX; i += blockDim.x) Sm[i] = Sg[i];
   stage_bits(bitsm, BW, NTX, seed, drop0 + b, k0, nd, m);
-  tap_averages(fc, v.W(b), v.P0(b), window_start[w], N, hb, scratch);  // contains __syncthreads
-  __shared__ QamDemapTable sqt;
-  if (threadIdx.x == 0) sqt = qt;
-  __syncthreads();
+  tap_averages(fc, v.W(b), v.P0(b), window_start[w], N, hb, scratch);  // ends with __syncthreads
   const int64_t wofs = (((k0 * m) >> 5) >> 2) * 4;
   const float s2 = nv ? nv[b] : 0.0f;
   const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
@@ -219,19 +228,64 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ideal(FadingConst fc, Fadin
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
     const int64_t k = k0 + j;
     const int c = data_column[k];
-    const float2 g = tap_response(fc, hb, ds, tws, bins[c], N);
+    const float2 g = tap_response(fc, hb, ds, tw, bins[c], N);
     float2 H[NRX][NTX], y[NRX], x[NTX];
 #pragma unroll
     for (int r = 0; r < NRX; ++r) {
       y[r] = grid[(((int64_t)b * NRX + r) * W + w) * gcols + c];
 #pragma unroll
-      for (int t = 0; t < NTX; ++t) H[r][t] = cmul(Sm[r * NTX + t], g);
+      for (int t = 0; t < NTX; ++t) H[r][t] = cmul(Sm[r * NTX + t], g);  // the ideal CSI of hpx_fading_ideal_csi
     }
     equalize_one<NRX, NTX>(mode, H, y, s2, x);
+#pragma unroll
     for (int t = 0; t < NTX; ++t) {
       // streams the equalizer does not return are received as zero bits
       // (BitErrorEvaluator zero-pads the shorter sequence)
-      const uint32_t rx_v = t < out_streams ? qam_decide(sqt, x[t]) : 0u;
+      const uint32_t rx_v = t < out_streams ? qam_decide(qt, x[t]) : 0u;
+      const uint32_t tx_v = extract_bits_msb(bitsm + t * BW - wofs, k * m, m);
+      local += __popc(rx_v ^ tx_v);
+    }
+  }
+  block_count(local, errors + b);
+}
+
+// Fused receiver for a given CSI grid (any estimator), one block per (word, drop):
+// H from csi[B][NRX][NTX][W][ccols], y from grid[B][NRX][W][gcols].
+template <int NRX, int NTX>
+__global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_csi(
+    int W, int C, int m, const int32_t* __restrict__ data_offset, const int32_t* __restrict__ num_data_word,
+    const int32_t* __restrict__ data_column, const __grid_constant__ QamDemapTable qt, int mode,
+    const float2* __restrict__ grid, int gcols, const float2* __restrict__ csi, int ccols,
+    const float* __restrict__ nv, uint64_t seed, int64_t drop0, uint32_t* __restrict__ errors) {
+  extern __shared__ float4 smem4[];
+  uint32_t* bitsm = reinterpret_cast<uint32_t*>(smem4);
+  const int w = blockIdx.x, b = blockIdx.y;
+  const int BW = staged_bit_words(C, m);
+  const int64_t k0 = data_offset[w];
+  const int nd = num_data_word[w];
+  stage_bits(bitsm, BW, NTX, seed, drop0 + b, k0, nd, m);
+  __syncthreads();
+  const int64_t wofs = (((k0 * m) >> 5) >> 2) * 4;
+  const float s2 = nv ? nv[b] : 0.0f;
+  const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
+  const int64_t hplane = (int64_t)W * ccols;  // one (rx, tx) pair of the CSI grid
+  const float2* hb = csi + (int64_t)b * NRX * NTX * hplane + (int64_t)w * ccols;
+  const float2* yb = grid + (int64_t)b * NRX * W * gcols + (int64_t)w * gcols;
+  unsigned int local = 0;
+  for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+    const int64_t k = k0 + j;
+    const int c = data_column[k];
+    float2 H[NRX][NTX], y[NRX], x[NTX];
+#pragma unroll
+    for (int r = 0; r < NRX; ++r) {
+      y[r] = yb[(int64_t)r * W * gcols + c];
+#pragma unroll
+      for (int t = 0; t < NTX; ++t) H[r][t] = hb[(int64_t)(r * NTX + t) * hplane + c];
+    }
+    equalize_one<NRX, NTX>(mode, H, y, s2, x);
+#pragma unroll
+    for (int t = 0; t < NTX; ++t) {
+      const uint32_t rx_v = t < out_streams ? qam_decide(qt, x[t]) : 0u;
       const uint32_t tx_v = extract_bits_msb(bitsm + t * BW - wofs, k * m, m);
       local += __popc(rx_v ^ tx_v);
     }
@@ -248,7 +302,7 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
                                                         const float* __restrict__ weights,
                                                         const int32_t* __restrict__ ref_word,
                                                         const int32_t* __restrict__ ref_column,
-                                                        const float2* __restrict__ pilots, QamDemapTable qt, int mode,
+                                                        const float2* __restrict__ pilots, const __grid_constant__ QamDemapTable qt, int mode,
                                                         const float2* __restrict__ grid, int gcols,
                                                         const float* __restrict__ nv, uint64_t seed, int64_t drop0,
                                                         uint32_t* __restrict__ errors) {
@@ -259,8 +313,6 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
   const int64_t k0 = data_offset[w];
   const int nd = num_data_word[w];
   stage_bits(bitsm, BW, 1, seed, drop0 + b, k0, nd, m);
-  __shared__ QamDemapTable sqt;
-  if (threadIdx.x == 0) sqt = qt;
   __syncthreads();
   const int64_t wofs = (((k0 * m) >> 5) >> 2) * 4;
   const float s2 = nv ? nv[b] : 0.0f;
@@ -281,7 +333,7 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
     }
     float2 H[1][1] = {{h}}, y[1] = {gb[w * gcols + c]}, x[1];
     equalize_one<1, 1>(mode, H, y, s2, x);
-    const uint32_t rx_v = qam_decide(sqt, x[0]);
+    const uint32_t rx_v = qam_decide(qt, x[0]);
     const uint32_t tx_v = extract_bits_msb(bitsm - wofs, k * m, m);
     local += __popc(rx_v ^ tx_v);
   }
@@ -335,17 +387,50 @@ hpx_status launch_detect_ideal(const hpx_fading* f, const void* state, const hpx
   const FadingConst fc = fading_const(f);
   const int C = fr->info.num_columns, m = fr->info.bits_per_symbol;
   const int BW = staged_bit_words(C, m);
-  const size_t smem = (size_t)fr->info.num_subcarriers * sizeof(float2) + (size_t)fc.L * sizeof(float2) * (1 + fc.S1) +
-                      NRX * NTX * sizeof(float2) + (fc.L + 4) * sizeof(int) + (size_t)NTX * BW * 4 + 16;
+  const size_t smem = (size_t)fc.L * sizeof(float2) * (1 + fc.S1) + NRX * NTX * sizeof(float2) +
+                      (fc.L + 4) * sizeof(int) + (size_t)NTX * BW * 4 + 16;
   auto kern = k_detect_ideal<NRX, NTX>;
   if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid_dim(fr->info.num_words, B);
-  kern<<<grid_dim, DTHREADS, smem, s>>>(fc, fading_view(f, state), fr->info.num_subcarriers, fr->info.num_words, C, m,
+  const int threads = detect_threads(fr->max_data_word, detect_max_threads<NRX, NTX>());
+  kern<<<grid_dim, threads, smem, s>>>(fc, fading_view(f, state), fr->info.num_subcarriers, fr->info.num_words, C, m,
                                         fr->d_window_start, fr->d_data_offset, fr->d_num_data_word, fr->d_data_column,
                                         fr->d_bins, fr->d_twiddle, qt, mode, reinterpret_cast<const float2*>(grid),
                                         gcols, nv, seed, drop0, errors);
   HPX_LAUNCHED("detect_ideal");
   return HPX_OK;
+}
+
+template <int NRX, int NTX>
+hpx_status launch_detect_csi(const hpx_frame* fr, int mode, const hpx_cf32* grid, int gcols, const hpx_cf32* csi,
+                             int ccols, const float* nv, uint64_t seed, int64_t drop0, int B, uint32_t* errors,
+                             cudaStream_t s) {
+  QamDemapTable qt;
+  HPX_TRY(qam_demap_table(fr->info.modulation_order, &qt));
+  const int C = fr->info.num_columns, m = fr->info.bits_per_symbol;
+  const size_t smem = (size_t)NTX * staged_bit_words(C, m) * 4 + 16;
+  auto kern = k_detect_csi<NRX, NTX>;
+  if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid_dim(fr->info.num_words, B);
+  const int threads = detect_threads(fr->max_data_word, detect_max_threads<NRX, NTX>());
+  kern<<<grid_dim, threads, smem, s>>>(fr->info.num_words, C, m, fr->d_data_offset, fr->d_num_data_word,
+                                       fr->d_data_column, qt, mode, reinterpret_cast<const float2*>(grid), gcols,
+                                       reinterpret_cast<const float2*>(csi), ccols, nv, seed, drop0, errors);
+  HPX_LAUNCHED("detect_csi");
+  return HPX_OK;
+}
+
+template <int NRX>
+hpx_status detect_csi_tx(int ntx, const hpx_frame* fr, int mode, const hpx_cf32* grid, int gcols,
+                         const hpx_cf32* csi, int ccols, const float* nv, uint64_t seed, int64_t drop0, int B,
+                         uint32_t* errors, cudaStream_t s) {
+  switch (ntx) {
+    case 1: return launch_detect_csi<NRX, 1>(fr, mode, grid, gcols, csi, ccols, nv, seed, drop0, B, errors, s);
+    case 2: return launch_detect_csi<NRX, 2>(fr, mode, grid, gcols, csi, ccols, nv, seed, drop0, B, errors, s);
+    case 4: return launch_detect_csi<NRX, 4>(fr, mode, grid, gcols, csi, ccols, nv, seed, drop0, B, errors, s);
+    case 8: return launch_detect_csi<NRX, 8>(fr, mode, grid, gcols, csi, ccols, nv, seed, drop0, B, errors, s);
+    default: return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_csi: %d transmit streams not supported (1, 2, 4, 8)", ntx);
+  }
 }
 
 template <int NRX>
@@ -482,6 +567,28 @@ hpx_status hpx_detect_ideal(const hpx_fading* f, const void* state, const hpx_fr
   }
 }
 
+hpx_status hpx_detect_csi(const hpx_frame* fr, int32_t nrx, int32_t ntx, int32_t mode, const hpx_cf32* grid,
+                          int32_t gcols, const hpx_cf32* csi, int32_t ccols, const float* nv, uint64_t seed,
+                          int64_t drop0, int32_t B, uint32_t* errors, void* stream) {
+  if (!fr || !grid || !csi || !errors) return hpx_fail(HPX_ERR_ARG, "detect_csi: null argument");
+  if (mode != HPX_EQ_ZF && mode != HPX_EQ_LMMSE) return hpx_fail(HPX_ERR_ARG, "detect_csi: unknown mode");
+  if (mode == HPX_EQ_LMMSE && !nv) return hpx_fail(HPX_ERR_ARG, "detect_csi: LMMSE needs noise variances");
+  if (B < 0 || drop0 < 0) return hpx_fail(HPX_ERR_ARG, "detect_csi: bad drop range");
+  if (gcols < fr->info.num_columns || ccols < fr->info.num_columns)
+    return hpx_fail(HPX_ERR_SHAPE, "detect_csi: grid or CSI narrower than the frame");
+  if (B == 0) return HPX_OK;
+  if (B > 65535) return hpx_fail(HPX_ERR_ARG, "detect_csi: batch above 65535 drops per call");
+  cudaStream_t s = as_stream(stream);
+  HPX_CUDA(cudaMemsetAsync(errors, 0, sizeof(uint32_t) * B, s));
+  switch (nrx) {
+    case 1: return detect_csi_tx<1>(ntx, fr, mode, grid, gcols, csi, ccols, nv, seed, drop0, B, errors, s);
+    case 2: return detect_csi_tx<2>(ntx, fr, mode, grid, gcols, csi, ccols, nv, seed, drop0, B, errors, s);
+    case 4: return detect_csi_tx<4>(ntx, fr, mode, grid, gcols, csi, ccols, nv, seed, drop0, B, errors, s);
+    case 8: return detect_csi_tx<8>(ntx, fr, mode, grid, gcols, csi, ccols, nv, seed, drop0, B, errors, s);
+    default: return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_csi: %d receive streams not supported (1, 2, 4, 8)", nrx);
+  }
+}
+
 hpx_status hpx_detect_ls(const hpx_ls* ls, int32_t mode, const hpx_cf32* grid, int32_t gcols, const float* nv,
                          uint64_t seed, int64_t drop0, int32_t B, uint32_t* errors, void* stream) {
   if (!ls || !grid || !errors) return hpx_fail(HPX_ERR_ARG, "detect_ls: null argument");
@@ -499,7 +606,7 @@ hpx_status hpx_detect_ls(const hpx_ls* ls, int32_t mode, const hpx_cf32* grid, i
   const int C = ls->C, m = fr->info.bits_per_symbol;
   const size_t smem = (size_t)staged_bit_words(C, m) * 4 + 16;
   dim3 grid_dim(fr->info.num_words, B);
-  k_detect_ls<<<grid_dim, DTHREADS, smem, s>>>(fr->info.num_words, C, m, fr->d_data_offset, fr->d_num_data_word,
+  k_detect_ls<<<grid_dim, detect_threads(fr->max_data_word, DTHREADS), smem, s>>>(fr->info.num_words, C, m, fr->d_data_offset, fr->d_num_data_word,
                                                fr->d_data_column, ls->d_indptr, ls->d_indices, ls->d_weights,
                                                ls->d_ref_word, ls->d_ref_column, fr->d_pilots, qt, mode,
                                                reinterpret_cast<const float2*>(grid), gcols, nv, seed, drop0, errors);

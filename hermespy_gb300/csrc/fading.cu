@@ -189,7 +189,6 @@ __global__ void k_fading_csi(FadingConst fc, FadingView v, int T, int ntaps, flo
 // Tile length per transmit-antenna count (shared memory holds 2 NTX tile rows).
 template <int NTX>
 __host__ __device__ constexpr int tile_len() { return NTX <= 4 ? 1024 : (NTX <= 8 ? 512 : 256); }
-constexpr int RPT = 4;  // two pairs per thread: BT / 4 threads per block
 
 __host__ __device__ constexpr int tile_width(int BT, int D) { return (BT + D + 2) & ~1; }
 
@@ -201,12 +200,14 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
   const int b = blockIdx.y;
   const int m0 = blockIdx.x * BT;
   const int L = fc.L, S1 = fc.S1, D = fc.D, nrx = fc.nrx;
-  const int XW = tile_width(BT, D);                                   // even row width
-  float2* xe = reinterpret_cast<float2*>(smem4);                      // [NTX][XW]: x[m0 - D + i]
-  float2* xo = xe + NTX * XW;                                         // [NTX][XW]: x[m0 - D + i + 1]
-  float2* terms = xe;                                                 // [L*S1][K+1], before the tile load
-  const int region = DIRECT ? 2 * NTX * XW : max(2 * NTX * XW, L * S1 * (K + 1));
-  float2* coef = xe + region;                                         // [L][K+1]
+  const int XW = tile_width(BT, D);  // even row width
+  // Transmit tile as planes of real and imaginary parts, each stored twice: plane
+  // (tx, q) with q = 0 re even, 1 im even, 2 re odd, 3 im odd; even copies hold
+  // x[m0 - D + i], odd copies x[m0 - D + i + 1].
+  float* xp = reinterpret_cast<float*>(smem4);                        // [NTX][4][XW]
+  float2* terms = reinterpret_cast<float2*>(smem4);                   // [L*S1][K+1], before the tile load
+  const int region = DIRECT ? 2 * NTX * XW : max(2 * NTX * XW, L * S1 * (K + 1));  // in float2
+  float2* coef = reinterpret_cast<float2*>(smem4) + region;           // [L][K+1]
   int64_t* wp = reinterpret_cast<int64_t*>(coef + L * (K + 1));       // [2][L*S1] (direct)
   float2* Sm = reinterpret_cast<float2*>(wp + (DIRECT ? 2 * L * S1 : 0));  // [nrx*NTX]
   int* dl = reinterpret_cast<int*>(Sm + nrx * NTX);                   // [L]
@@ -255,67 +256,85 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
 #pragma unroll 1
   for (int tx = 0; tx < NTX; ++tx) {
     const float2* xr = xb + (int64_t)tx * T;
+    float* pl = xp + tx * 4 * XW;
     for (int j = tid; j <= XW; j += PTHREADS) {
       const int t = m0 - D + j;
       const float2 val = (t >= 0 && t < T) ? __ldg(xr + t) : make_float2(0.f, 0.f);
-      if (j < XW) xe[tx * XW + j] = val;
-      if (j > 0) xo[tx * XW + j - 1] = val;
+      if (j < XW) {
+        pl[j] = val.x;
+        pl[XW + j] = val.y;
+      }
+      if (j > 0) {
+        pl[2 * XW + j - 1] = val.x;
+        pl[3 * XW + j - 1] = val.y;
+      }
     }
   }
   __syncthreads();
 
-  // ---- convolution: z_tx[m] = sum_l h_l[m - d_l] x_tx[m - d_l]
+  // ---- convolution: z_tx[m] = sum_l h_l[m - d_l] x_tx[m - d_l], two samples per
+  // packed FP32x2 FMA: zr/zi hold the real/imaginary parts of a pair of samples.
   const int jp[2] = {2 * tid, 2 * tid + BT / 2};  // tile index of each pair's first sample
-  float2 z[RPT][NTX];
+  float2 zr[2][NTX], zi[2][NTX];
 #pragma unroll
-  for (int r = 0; r < RPT; ++r)
+  for (int pr = 0; pr < 2; ++pr)
 #pragma unroll
-    for (int tx = 0; tx < NTX; ++tx) z[r][tx] = make_float2(0.f, 0.f);
-  float up[RPT][K + 1];
+    for (int tx = 0; tx < NTX; ++tx) zr[pr][tx] = zi[pr][tx] = make_float2(0.f, 0.f);
+  float2 up[2][K + 1];  // powers of u for both samples of a pair
 #pragma unroll
-  for (int r = 0; r < RPT; ++r) {
-    const float u = ((float)(jp[r >> 1] + (r & 1)) - 0.5f * BT) / (0.5f * BT);
-    up[r][0] = 1.0f;
+  for (int pr = 0; pr < 2; ++pr) {
+    const float u0 = ((float)jp[pr] - 0.5f * BT) / (0.5f * BT);
+    const float u1 = ((float)(jp[pr] + 1) - 0.5f * BT) / (0.5f * BT);
+    up[pr][0] = make_float2(1.0f, 1.0f);
 #pragma unroll
-    for (int k = 1; k <= K; ++k) up[r][k] = up[r][k - 1] * u;
+    for (int k = 1; k <= K; ++k) up[pr][k] = make_float2(up[pr][k - 1].x * u0, up[pr][k - 1].y * u1);
   }
 #pragma unroll 1
   for (int l = 0; l < L; ++l) {
     const int d = dl[l];
-    float2 h[RPT];
+    float2 hx[2], hy[2];
     if (DIRECT) {
       const float an = fc.amp[2 * l], al = fc.amp[2 * l + 1];
 #pragma unroll
-      for (int r = 0; r < RPT; ++r)
-        h[r] = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al,
-                          (int64_t)m0 + jp[r >> 1] + (r & 1) - d);
+      for (int pr = 0; pr < 2; ++pr) {
+        const float2 h0 = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al, (int64_t)m0 + jp[pr] - d);
+        const float2 h1 = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al, (int64_t)m0 + jp[pr] + 1 - d);
+        hx[pr] = make_float2(h0.x, h1.x);
+        hy[pr] = make_float2(h0.y, h1.y);
+      }
     } else {
       const float2* cl = coef + l * (K + 1);
       float2 ck[K + 1];
 #pragma unroll
       for (int k = 0; k <= K; ++k) ck[k] = cl[k];
 #pragma unroll
-      for (int r = 0; r < RPT; ++r) {
-        float2 acc = ck[0];
+      for (int pr = 0; pr < 2; ++pr) {
+        float2 ax = make_float2(ck[0].x, ck[0].x), ay = make_float2(ck[0].y, ck[0].y);
 #pragma unroll
         for (int k = 1; k <= K; ++k) {
-          acc.x = fmaf(ck[k].x, up[r][k], acc.x);
-          acc.y = fmaf(ck[k].y, up[r][k], acc.y);
+          ax = __ffma2_rn(make_float2(ck[k].x, ck[k].x), up[pr][k], ax);
+          ay = __ffma2_rn(make_float2(ck[k].y, ck[k].y), up[pr][k], ay);
         }
-        h[r] = acc;
+        hx[pr] = ax;
+        hy[pr] = ay;
       }
     }
     // all lanes share the parity of D - d, hence the same copy: conflict-free
     const int odd = (D - d) & 1;
-    const float2* src = odd ? xo - 1 : xe;
+    const float* src = xp + 2 * odd * XW - odd;  // plane offset of the even/odd copy, index shifted by one
 #pragma unroll
     for (int pr = 0; pr < 2; ++pr) {
-      const float2* base = src + jp[pr] - d + D;
+      const int s0 = jp[pr] - d + D;
+      const float2 nhy = make_float2(-hy[pr].x, -hy[pr].y);
 #pragma unroll
       for (int tx = 0; tx < NTX; ++tx) {
-        const float4 q = *reinterpret_cast<const float4*>(base + tx * XW);
-        cfma(z[2 * pr][tx], h[2 * pr], make_float2(q.x, q.y));
-        cfma(z[2 * pr + 1][tx], h[2 * pr + 1], make_float2(q.z, q.w));
+        const float* pl = src + tx * 4 * XW + s0;
+        const float2 re = *reinterpret_cast<const float2*>(pl);
+        const float2 im = *reinterpret_cast<const float2*>(pl + XW);
+        zr[pr][tx] = __ffma2_rn(hx[pr], re, zr[pr][tx]);
+        zr[pr][tx] = __ffma2_rn(nhy, im, zr[pr][tx]);
+        zi[pr][tx] = __ffma2_rn(hx[pr], im, zi[pr][tx]);
+        zi[pr][tx] = __ffma2_rn(hy[pr], re, zi[pr][tx]);
       }
     }
   }
@@ -329,11 +348,15 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
     float2* yr = y + ((int64_t)b * nrx + rx) * TD;
 #pragma unroll
     for (int pr = 0; pr < 2; ++pr) {
-      float2 o0 = make_float2(0.f, 0.f), o1 = make_float2(0.f, 0.f);
+      float2 ore = make_float2(0.f, 0.f), oim = make_float2(0.f, 0.f);
 #pragma unroll
       for (int tx = 0; tx < NTX; ++tx) {
-        cfma(o0, Sm[rx * NTX + tx], z[2 * pr][tx]);
-        cfma(o1, Sm[rx * NTX + tx], z[2 * pr + 1][tx]);
+        const float2 sv = Sm[rx * NTX + tx];
+        const float2 sr = make_float2(sv.x, sv.x), si = make_float2(sv.y, sv.y), nsi = make_float2(-sv.y, -sv.y);
+        ore = __ffma2_rn(sr, zr[pr][tx], ore);
+        ore = __ffma2_rn(nsi, zi[pr][tx], ore);
+        oim = __ffma2_rn(sr, zi[pr][tx], oim);
+        oim = __ffma2_rn(si, zr[pr][tx], oim);
       }
       const int m = m0 + jp[pr];
       if (noise_power && np > 0.0f) {
@@ -341,13 +364,11 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
         const uint4 w = hpx_random_block(seed, drop0 + b, (uint32_t)rx, HPX_DOMAIN_NOISE, (uint32_t)(m >> 1));
         const float2 n0 = box_muller(w.x, w.y);
         const float2 n1 = box_muller(w.z, w.w);
-        o0.x += sigma * n0.x;
-        o0.y += sigma * n0.y;
-        o1.x += sigma * n1.x;
-        o1.y += sigma * n1.y;
+        ore = __ffma2_rn(make_float2(sigma, sigma), make_float2(n0.x, n1.x), ore);
+        oim = __ffma2_rn(make_float2(sigma, sigma), make_float2(n0.y, n1.y), oim);
       }
-      if (m < TD) yr[m] = o0;
-      if (m + 1 < TD) yr[m + 1] = o1;
+      if (m < TD) yr[m] = make_float2(ore.x, oim.x);
+      if (m + 1 < TD) yr[m + 1] = make_float2(ore.y, oim.y);
     }
   }
 }
@@ -357,17 +378,15 @@ __global__ void k_ideal_csi(FadingConst fc, FadingView v, int N, int W, const in
                             const int32_t* __restrict__ bins, const float2* __restrict__ tw, int ncols,
                             float2* __restrict__ csi) {
   extern __shared__ float4 smem4[];
-  float2* tws = reinterpret_cast<float2*>(smem4);  // [N] twiddle table
-  float2* hb = tws + N;
+  float2* hb = reinterpret_cast<float2*>(smem4);
   float2* scratch = hb + fc.L;
   int* ds = reinterpret_cast<int*>(scratch + fc.L * fc.S1);
   const int b = blockIdx.y, w = blockIdx.x;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = __ldg(tw + i);
   for (int l = threadIdx.x; l < fc.L; l += blockDim.x) ds[l] = fc.delay[l];
   tap_averages(fc, v.W(b), v.P0(b), window_start[w], N, hb, scratch);
   const float2* Sm = v.spatial(b);
   for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
-    const float2 g = tap_response(fc, hb, ds, tws, bins[c], N);
+    const float2 g = tap_response(fc, hb, ds, tw, bins[c], N);
     for (int r = 0; r < fc.nrx; ++r)
       for (int t = 0; t < fc.ntx; ++t)
         csi[((((int64_t)b * fc.nrx + r) * fc.ntx + t) * W + w) * ncols + c] = cmul(Sm[r * fc.ntx + t], g);
@@ -659,7 +678,7 @@ hpx_status hpx_fading_ideal_csi(const hpx_fading* f, const void* state, int32_t 
   if (B < 0 || ncols < 1 || ncols > N) return hpx_fail(HPX_ERR_ARG, "ideal_csi: bad size");
   if (B == 0) return HPX_OK;
   if (B > 65535) return hpx_fail(HPX_ERR_ARG, "ideal_csi: batch too large");
-  const size_t smem = (size_t)N * sizeof(float2) + (size_t)f->L * sizeof(float2) * (1 + f->S1) + f->L * sizeof(int) + 16;
+  const size_t smem = (size_t)f->L * sizeof(float2) * (1 + f->S1) + f->L * sizeof(int) + 16;
   dim3 grid(W, B);
   k_ideal_csi<<<grid, 256, smem, as_stream(stream)>>>(fading_const(f), fading_view(f, state), N, W,
                                                       frame->d_window_start, frame->d_bins, frame->d_twiddle, ncols,

@@ -61,15 +61,14 @@ __device__ __forceinline__ void tap_averages(const FadingConst& fc, const int64_
 }
 
 // Frequency response sum_l hb[l] exp(-2 pi i bin d_l / N) at one FFT bin, for taps
-// with delays below N (longer delays fall outside the N-point transform). `tw` is
-// the N-point twiddle table, read from shared memory by the callers.
+// with delays below N (longer delays fall outside the N-point transform).
 __device__ __forceinline__ float2 tap_response(const FadingConst& fc, const float2* hb, const int32_t* delay_s,
-                                               const float2* tw, int bin, int N) {
+                                               const float2* __restrict__ tw, int bin, int N) {
   float2 g = make_float2(0.f, 0.f);
   for (int l = 0; l < fc.L; ++l) {
     const int d = delay_s[l];
     if (d >= N) continue;
-    cfma(g, hb[l], tw[(bin * d) & (N - 1)]);
+    cfma(g, hb[l], __ldg(tw + ((bin * d) & (N - 1))));
   }
   return g;
 }

@@ -1,4 +1,6 @@
 // Frame layout tables and the library's error state.
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -38,7 +40,7 @@ static void release(hpx_frame* f) {
   if (!f) return;
   void* ptrs[] = {f->d_prefix, f->d_zero_prefix, f->d_word_start, f->d_window_start, f->d_data_offset,
                   f->d_num_data_word, f->d_kind, f->d_index, f->d_bins, f->d_data_column, f->d_data_word,
-                  f->d_twiddle, f->d_stage_twiddle, f->d_pilots};
+                  f->d_twiddle, f->d_stage_twiddle, f->d_pilots, f->d_bin_code, f->d_constellation};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete f;
@@ -65,6 +67,11 @@ hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out) {
 
   hpx_frame* f = new hpx_frame();
   f->dc_suppression = desc->dc_suppression ? 1 : 0;
+  if (desc->pilot_comb < 0 || desc->pilot_comb > 64) {
+    delete f;
+    return hpx_fail(HPX_ERR_ARG, "frame: pilot_comb must be in [0, 64] (got %d)", desc->pilot_comb);
+  }
+  f->pilot_comb = desc->pilot_comb;
   f->h_prefix.assign(desc->prefix, desc->prefix + W);
   f->h_zero_prefix.assign(W, 0);
   if (desc->zero_prefix) f->h_zero_prefix.assign(desc->zero_prefix, desc->zero_prefix + W);
@@ -115,6 +122,7 @@ hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out) {
   f->info.num_data = nd;
   f->info.num_refs = nr;
   f->info.samples_per_frame = (int32_t)start;
+  for (int w = 0; w < W; ++w) f->max_data_word = std::max(f->max_data_word, num_data_word[w]);
 
   // grid column -> FFT bin (ofdm.py:116-128 and 146-151)
   f->h_bins.resize(N);
@@ -158,6 +166,18 @@ hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out) {
   }
   std::vector<float2> pilots(nr);
   for (int k = 0; k < nr; ++k) pilots[k] = qam_symbol(desc->modulation_order, (uint32_t)(k % desc->modulation_order));
+  std::vector<float2> constellation(desc->modulation_order);
+  for (int v = 0; v < desc->modulation_order; ++v) constellation[v] = qam_symbol(desc->modulation_order, (uint32_t)v);
+  // What the transmitter places at FFT bin b of word w: data element k (>= 0),
+  // reference element r (encoded ~r), or nothing.
+  std::vector<int32_t> bin_code((size_t)W * N, INT32_MIN);
+  for (int w = 0; w < W; ++w)
+    for (int c = 0; c < C; ++c) {
+      const int8_t k = f->h_kind[(size_t)w * C + c];
+      const int32_t idx = f->h_index[(size_t)w * C + c];
+      if (k == HPX_RE_DATA) bin_code[(size_t)w * N + f->h_bins[c]] = idx;
+      else if (k == HPX_RE_REFERENCE) bin_code[(size_t)w * N + f->h_bins[c]] = ~idx;
+    }
 
   hpx_status s = HPX_OK;
   if ((s = upload(&f->d_prefix, f->h_prefix)) != HPX_OK ||
@@ -169,7 +189,8 @@ hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out) {
       (s = upload(&f->d_kind, f->h_kind)) != HPX_OK || (s = upload(&f->d_index, f->h_index)) != HPX_OK ||
       (s = upload(&f->d_bins, f->h_bins)) != HPX_OK || (s = upload(&f->d_data_column, data_column)) != HPX_OK ||
       (s = upload(&f->d_data_word, data_word)) != HPX_OK || (s = upload(&f->d_twiddle, tw)) != HPX_OK || (s = upload(&f->d_stage_twiddle, stw)) != HPX_OK ||
-      (s = upload(&f->d_pilots, pilots)) != HPX_OK) {
+      (s = upload(&f->d_pilots, pilots)) != HPX_OK || (s = upload(&f->d_bin_code, bin_code)) != HPX_OK ||
+      (s = upload(&f->d_constellation, constellation)) != HPX_OK) {
     release(f);
     return s;
   }

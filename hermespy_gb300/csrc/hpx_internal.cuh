@@ -101,14 +101,16 @@ __host__ __device__ __forceinline__ uint32_t uint4_get(const uint4& v, int i) {
 __host__ __device__ __forceinline__ double u01_f64(uint32_t w) { return ((double)w + 0.5) * 2.3283064365386963e-10; }
 __device__ __forceinline__ float u01_f32(uint32_t w) { return ((float)(w >> 8) + 0.5f) * 5.9604644775390625e-08f; }
 
-// Box-Muller pair of unit normals from two words.
+// Box-Muller pair of unit normals from two words: r (cos 2 pi u2, sin 2 pi u2),
+// evaluated as -r (cos a, sin a) with a = 2 pi (u2 - 1/2) in (-pi, pi), where the
+// fast hardware sine and cosine are accurate to a few 1e-7.
 __device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b) {
   const float u1 = u01_f32(a);
   const float u2 = u01_f32(b);
   const float r = sqrtf(-2.0f * logf(u1));
   float s, c;
-  sincospif(2.0f * u2, &s, &c);
-  return make_float2(r * c, r * s);
+  __sincosf(6.283185307179586f * (u2 - 0.5f), &s, &c);
+  return make_float2(-r * c, -r * s);
 }
 
 // ------------------------------------------------------ fixed-point phases
@@ -133,12 +135,14 @@ __device__ __forceinline__ float fixed_to_angle(uint64_t p) {
 struct hpx_frame {
   hpx_frame_info info;
   int dc_suppression;
+  int pilot_comb;  // 0/1: all streams send every reference element; P > 1: stream s only on columns c % P == s % P
   // host copies
   std::vector<int32_t> h_prefix, h_zero_prefix, h_word_start, h_window_start;
   std::vector<int32_t> h_data_offset, h_ref_offset;  // first data / ref index of each word
   std::vector<int8_t> h_kind;                        // [W * C]
   std::vector<int32_t> h_index;                      // [W * C] data or ref index within the frame
   std::vector<int32_t> h_bins;                       // [N] FFT bin of grid column c
+  int32_t max_data_word = 0;                         // most data elements in one word
   // device copies
   int32_t* d_prefix = nullptr;
   int32_t* d_zero_prefix = nullptr;
@@ -154,6 +158,8 @@ struct hpx_frame {
   float2* d_twiddle = nullptr;         // [N] exp(-2 pi i t / N)
   float2* d_stage_twiddle = nullptr;   // [2N] per-stage tables of the OFDM FFT (fft.cuh)
   float2* d_pilots = nullptr;          // [num_refs]
+  int32_t* d_bin_code = nullptr;       // [W * N] per (word, FFT bin): data index, ~pilot index, or INT32_MIN (null)
+  float2* d_constellation = nullptr;   // [M] symbols in MSB-first bit-value order
 };
 
 // ------------------------------------------------------------ fading state
@@ -207,9 +213,14 @@ static inline FadingView fading_view(const hpx_fading* f, const void* state) {
 
 // QAM tables (mapping.cu)
 hpx_status qam_bits_per_symbol(int32_t order, int* bits);
+// Exact hard decisions of PskQamMapping.detect_bits on float32 amplitudes. The
+// reference's scaled amplitude r(x) = (x sqrt 2) sqrt c is odd and monotone, so per
+// real dimension the first bit is the sign and every further bit is 1 exactly when
+// |x| lies in one of up to three open intervals (lo, hi) of float32 cut points
+// (lo = -1 encodes an interval closed at 0).
 struct QamDemapTable {
   int order, bits, pam_bits;  // pam_bits: bits per real dimension
-  float lo[4][8], hi[4][8];   // per PAM bit: up to 8 open intervals (lo, hi) in float32 x
+  float lo[4][3], hi[4][3];   // PAM bits 1..pam_bits-1 over |x|
   int count[4];
 };
 hpx_status qam_demap_table(int32_t order, QamDemapTable* table);
@@ -253,21 +264,42 @@ __host__ __device__ __forceinline__ float2 qam_symbol(int order, uint32_t v) {
 // Hard decisions of one symbol with a demap table; returns MSB-first bit value.
 // BPSK and QPSK LLRs are plain linear functions of the amplitude (no masked
 // pieces), so -inf decides 1 there, while the masked piecewise LLRs of the larger
-// constellations turn any infinity into NaN and decide 0 (open intervals).
-__device__ __forceinline__ uint32_t qam_decide(const QamDemapTable& t, float2 y) {
-  if (t.order == 2) return (y.x < 0.0f) ? 1u : 0u;
-  if (t.order == 4) return ((y.x < 0.0f) ? 2u : 0u) | ((y.y < 0.0f) ? 1u : 0u);
-  uint32_t v = 0;
-  const int h = t.pam_bits;
-  for (int i = 0; i < h; ++i) {
-    uint32_t br = 0, bi = 0;
-    for (int k = 0; k < t.count[i]; ++k) {
-      br |= (y.x > t.lo[i][k] && y.x < t.hi[i][k]) ? 1u : 0u;
-      bi |= (y.y > t.lo[i][k] && y.y < t.hi[i][k]) ? 1u : 0u;
-    }
-    v = (v << 2) | (br << 1) | bi;
+// constellations turn any infinity into NaN and decide 0 for every bit.
+// Bit i (1 <= i < PB) of a PAM axis is 1 on i open intervals of |x|. Kernels pass
+// the table as a __grid_constant__ parameter, so every bound is a constant-bank
+// operand of its compare.
+template <int PB>
+__device__ __forceinline__ uint32_t pam_decide(const QamDemapTable& t, float x) {
+  const float ax = fabsf(x);
+  uint32_t v = (x < 0.0f && ax < INFINITY) ? 1u : 0u;
+#pragma unroll
+  for (int i = 1; i < PB; ++i) {
+    bool in = false;
+#pragma unroll
+    for (int k = 0; k < i; ++k) in = in || (ax > t.lo[i][k] && ax < t.hi[i][k]);
+    v = (v << 1) | (in ? 1u : 0u);
   }
   return v;
+}
+
+template <int PB>
+__device__ __forceinline__ uint32_t qam_decide_pb(const QamDemapTable& t, float2 y) {
+  const uint32_t re = pam_decide<PB>(t, y.x), im = pam_decide<PB>(t, y.y);
+  // interleave: b0 = re0, b1 = im0, b2 = re1, ... (MSB first)
+  uint32_t v = 0;
+#pragma unroll
+  for (int i = PB - 1; i >= 0; --i) v = (v << 2) | (((re >> i) & 1u) << 1) | ((im >> i) & 1u);
+  return v;
+}
+
+__device__ __forceinline__ uint32_t qam_decide(const QamDemapTable& t, float2 y) {
+  switch (t.order) {
+    case 2: return (y.x < 0.0f) ? 1u : 0u;
+    case 4: return ((y.x < 0.0f) ? 2u : 0u) | ((y.y < 0.0f) ? 1u : 0u);
+    case 16: return qam_decide_pb<2>(t, y);
+    case 64: return qam_decide_pb<3>(t, y);
+    default: return qam_decide_pb<4>(t, y);
+  }
 }
 
 // Words of packed Philox bits staged for the data elements of one OFDM word with

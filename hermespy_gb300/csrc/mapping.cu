@@ -61,21 +61,18 @@ float x_lower(double e, double c) {
   return ord2f(hi);
 }
 
-// Open intervals of the scaled amplitude where a PAM bit's LLR is positive
-// (psk_qam_mapping.py:331-497; every sign change of those piecewise-linear LLRs
-// sits on an exact zero, so ties give bit 0). INF marks an unbounded end.
+// Open intervals of |r| (r the scaled amplitude) where PAM bit i >= 1 has a positive
+// LLR (psk_qam_mapping.py:331-497). Every sign change of those piecewise-linear LLRs
+// sits on an exact zero, so ties give bit 0; a = -1 marks an interval closed at 0
+// and b = INF an unbounded one. Bit 0 is the sign of r.
 const double INF = 1e300;
 struct Iv { double a, b; };
-const Iv PAM2[1][1] = {{{-INF, 0}}};
-const Iv PAM4[2][2] = {{{-INF, 0}, {0, 0}}, {{-INF, -2}, {2, INF}}};
-const Iv PAM8[3][3] = {{{-INF, 0}}, {{-INF, -4}, {4, INF}}, {{-INF, -6}, {-2, 2}, {6, INF}}};
-const Iv PAM16[4][5] = {{{-INF, 0}},
-                        {{-INF, -8}, {8, INF}},
-                        {{-INF, -12}, {-4, 4}, {12, INF}},
-                        {{-INF, -14}, {-10, -6}, {-2, 2}, {6, 10}, {14, INF}}};
-const int PAM4_N[2] = {1, 2};
-const int PAM8_N[3] = {1, 2, 3};
-const int PAM16_N[4] = {1, 2, 3, 5};
+const Iv PAM4[2][3] = {{}, {{2, INF}}};
+const Iv PAM8[3][3] = {{}, {{4, INF}}, {{-1, 2}, {6, INF}}};
+const Iv PAM16[4][3] = {{}, {{8, INF}}, {{-1, 4}, {12, INF}}, {{-1, 2}, {6, 10}, {14, INF}}};
+const int PAM4_N[2] = {0, 1};
+const int PAM8_N[3] = {0, 1, 2};
+const int PAM16_N[4] = {0, 1, 2, 3};
 
 std::mutex g_table_mutex;
 QamDemapTable g_tables[9];
@@ -95,16 +92,15 @@ hpx_status qam_demap_table(int32_t order, QamDemapTable* out) {
     t.bits = m;
     t.pam_bits = order == 2 ? 1 : m / 2;
     const double c = order == 16 ? 5.0 : (order == 64 ? 21.0 : (order == 256 ? 85.0 : 1.0));
-    for (int i = 0; i < t.pam_bits; ++i) {
+    for (int i = 1; i < t.pam_bits; ++i) {
       const Iv* ivs;
       int n;
-      if (order == 2 || order == 4) { ivs = PAM2[0]; n = 1; }
-      else if (order == 16) { ivs = PAM4[i]; n = PAM4_N[i]; }
+      if (order == 16) { ivs = PAM4[i]; n = PAM4_N[i]; }
       else if (order == 64) { ivs = PAM8[i]; n = PAM8_N[i]; }
       else { ivs = PAM16[i]; n = PAM16_N[i]; }
       t.count[i] = n;
       for (int k = 0; k < n; ++k) {
-        t.lo[i][k] = ivs[k].a <= -INF ? -INFINITY : x_upper(ivs[k].a, c);
+        t.lo[i][k] = ivs[k].a < 0 ? -1.0f : x_upper(ivs[k].a, c);
         t.hi[i][k] = ivs[k].b >= INF ? INFINITY : x_lower(ivs[k].b, c);
       }
     }
@@ -146,7 +142,7 @@ __global__ void k_qam_map(int order, int m, const uint8_t* __restrict__ bits, in
   }
 }
 
-__global__ void k_qam_demap(QamDemapTable t, const float2* __restrict__ sym, int64_t n, uint8_t* __restrict__ bits) {
+__global__ void k_qam_demap(const __grid_constant__ QamDemapTable t, const float2* __restrict__ sym, int64_t n, uint8_t* __restrict__ bits) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t v = qam_decide(t, sym[k]);
     for (int i = 0; i < t.bits; ++i) bits[k * t.bits + i] = (uint8_t)((v >> (t.bits - 1 - i)) & 1u);

@@ -1,6 +1,8 @@
 // OFDM transmit (bits -> QAM -> place -> IFFT -> prefix) and receive
 // (prefix strip -> FFT -> bin gather) kernels with a block-cooperative
 // Stockham FFT in shared memory.
+#include <climits>
+
 #include "fft.cuh"
 #include "hpx_internal.cuh"
 
@@ -9,6 +11,7 @@ namespace {
 
 struct FrameDev {
   int N, W, C, m, order, T, num_data, dc;
+  int comb;  // pilot comb (0/1: every stream sends every reference element)
   const int32_t* prefix;
   const int32_t* zero_prefix;
   const int32_t* word_start;
@@ -23,6 +26,8 @@ struct FrameDev {
   const float2* twiddle;
   const float2* stage_twiddle;
   const float2* pilots;
+  const int32_t* bin_code;
+  const float2* constellation;
 };
 
 FrameDev frame_dev(const hpx_frame* f) {
@@ -35,6 +40,7 @@ FrameDev frame_dev(const hpx_frame* f) {
   d.T = f->info.samples_per_frame;
   d.num_data = f->info.num_data;
   d.dc = f->dc_suppression;
+  d.comb = f->pilot_comb;
   d.prefix = f->d_prefix;
   d.zero_prefix = f->d_zero_prefix;
   d.word_start = f->d_word_start;
@@ -49,6 +55,8 @@ FrameDev frame_dev(const hpx_frame* f) {
   d.twiddle = f->d_twiddle;
   d.stage_twiddle = f->d_stage_twiddle;
   d.pilots = f->d_pilots;
+  d.bin_code = f->d_bin_code;
+  d.constellation = f->d_constellation;
   return d;
 }
 
@@ -65,11 +73,6 @@ constexpr int groups_per_block() {
   return fft::Plan<N>::TP >= 128 ? 1 : 128 / fft::Plan<N>::TP;
 }
 
-// Symbol of data element k from staged packed bits.
-__device__ __forceinline__ float2 symbol_from_bits(const uint32_t* words, int64_t pos, int m, int order) {
-  return qam_symbol(order, extract_bits_msb(words, pos, m));
-}
-
 // MODE 0: data symbols `data` [items][num_data]; MODE 1: Philox bits of drop
 // item / num_streams, stream item % num_streams; MODE 2: a placed grid `data`
 // [items][W][G] with G = num_streams columns.
@@ -84,11 +87,11 @@ __global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>())
   const int g = threadIdx.x / TP, t = threadIdx.x - g * TP;
   float2* buf = reinterpret_cast<float2*>(smem4) + g * PN;
   const int BW = staged_bit_words(fr.C, fr.m);
-  uint32_t* bits = reinterpret_cast<uint32_t*>(reinterpret_cast<float2*>(smem4) + F * PN) + g * BW;
+  float2* cons = reinterpret_cast<float2*>(smem4) + F * PN;  // [M] constellation (MODE 1)
+  uint32_t* bits = reinterpret_cast<uint32_t*>(cons + (MODE == 1 ? fr.order : 0)) + g * BW;
   const int p = blockIdx.x * F + g;
   const bool valid = p < num_pairs;
   const int item = valid ? p / fr.W : 0, w = valid ? p - item * fr.W : 0;
-  const int C = fr.C;
   const bool dc = fr.dc != 0;
   const float scale = rsqrtf((float)N);
   int64_t wofs = 0;
@@ -109,22 +112,27 @@ __global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>())
       wofs = blk0 * 4;
     }
   }
-  if (MODE == 1) fft::sync_group<TP>();
+  if (MODE == 1) {
+    for (int i = threadIdx.x; i < fr.order; i += blockDim.x) cons[i] = fr.constellation[i];
+    __syncthreads();
+  }
   const uint32_t* words = bits - wofs;
+  const int32_t* codes = fr.bin_code + (int64_t)w * N;
+  // stream of this item (MODE 1: items are (drop, stream); MODE 0: stream 0)
+  const int stream = MODE == 1 ? item % num_streams : 0;
   auto load = [&](int b) -> float2 {
     if (!valid) return make_float2(0.f, 0.f);
-    const int c = column_of_bin(b, N, dc);
     float2 v = make_float2(0.f, 0.f);
     if (MODE == 2) {
+      const int c = column_of_bin(b, N, dc);
       if (c < num_streams) v = data[(int64_t)p * num_streams + c];
-    } else if (c < C) {
-      const int kind = fr.kind[w * C + c];
-      if (kind == HPX_RE_DATA) {
-        const int k = fr.index[w * C + c];
-        if (MODE == 0) v = data[(int64_t)item * fr.num_data + k];
-        else v = symbol_from_bits(words, (int64_t)k * fr.m, fr.m, fr.order);
-      } else if (kind == HPX_RE_REFERENCE) {
-        v = fr.pilots[fr.index[w * C + c]];
+    } else {
+      const int32_t code = __ldg(codes + b);
+      if (code >= 0) {
+        if (MODE == 0) v = data[(int64_t)item * fr.num_data + code];
+        else v = cons[extract_bits_msb(words, (int64_t)code * fr.m, fr.m)];
+      } else if (code != INT32_MIN) {
+        if (fr.comb <= 1 || column_of_bin(b, N, dc) % fr.comb == stream % fr.comb) v = fr.pilots[~code];
       }
     }
     return cscale(v, scale);
@@ -179,7 +187,8 @@ hpx_status launch_tx_n(const FrameDev& d, int pairs, const float2* data, uint64_
                        float2* out, cudaStream_t s) {
   constexpr int F = groups_per_block<N>();
   constexpr int threads = fft::Plan<N>::TP * F;
-  const size_t smem = (size_t)F * (N + N / 32) * sizeof(float2) + (MODE == 1 ? (size_t)F * staged_bit_words(d.C, d.m) * 4 : 0);
+  const size_t smem = (size_t)F * (N + N / 32) * sizeof(float2) +
+                      (MODE == 1 ? (size_t)d.order * sizeof(float2) + (size_t)F * staged_bit_words(d.C, d.m) * 4 : 0);
   auto kern = k_ofdm_tx<N, MODE>;
   if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int blocks = (pairs + F - 1) / F;

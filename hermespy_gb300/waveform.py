@@ -106,7 +106,7 @@ class OFDMWaveform:
     def __init__(self, grid_resources: Sequence[GridResource], grid_structure: Sequence[SymbolSection],
                  num_subcarriers: int = 1024, dc_suppression: bool = True, pilot_section=None,
                  pilot_sequence=None, repeat_pilot_sequence: bool = True, modulation_order: int = 16,
-                 oversampling_factor: int = 1, **kwargs) -> None:
+                 oversampling_factor: int = 1, pilot_comb: int = 0, **kwargs) -> None:
         if num_subcarriers < 1:
             raise ValueError("Number of subcarriers must be greater or equal to one")
         if pilot_section is not None or pilot_sequence is not None:
@@ -119,6 +119,10 @@ class OFDMWaveform:
         self.dc_suppression = bool(dc_suppression)
         self.modulation_order = int(modulation_order)
         self.oversampling_factor = int(oversampling_factor)
+        # Engine extension for MIMO channel estimation (no counterpart in the
+        # reference): with pilot_comb = P > 1 stream s sends the reference element
+        # of grid column c only if c % P == s % P.
+        self.pilot_comb = int(pilot_comb)
         self._channel_estimation = None
         self._channel_equalization = None
         self._handle = None
@@ -140,7 +144,7 @@ class OFDMWaveform:
 
     # ------------------------------------------------------------------ frame
     def _layout(self) -> dict:
-        key = (self.num_subcarriers, self.dc_suppression, self.modulation_order,
+        key = (self.num_subcarriers, self.dc_suppression, self.modulation_order, self.pilot_comb,
                tuple((r.repetitions, r.prefix_ratio, r.prefix_type, tuple((e.type, e.repetitions) for e in r.elements))
                      for r in self.grid_resources),
                tuple((s.num_repetitions, tuple(s.pattern)) for s in self.grid_structure))
@@ -186,7 +190,7 @@ class OFDMWaveform:
             desc = _lib.FrameDesc(self.num_subcarriers, t["num_words"], t["num_columns"], self.modulation_order,
                                   int(self.dc_suppression), prefix.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                                   zero.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
-                                  kind.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)))
+                                  kind.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), self.pilot_comb)
             h = ctypes.c_void_p()
             _lib.check(_lib.load().hpx_frame_create(ctypes.byref(desc), ctypes.byref(h)))
             self._handle = h

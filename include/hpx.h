@@ -61,6 +61,10 @@ typedef struct {
   const int32_t* prefix;     /* [num_words] prefix length in samples */
   const int32_t* zero_prefix;/* [num_words] 1 = zero padding, 0 = cyclic prefix (may be NULL) */
   const int8_t* kind;        /* [num_words * num_columns] HPX_RE_* per resource element */
+  int32_t pilot_comb;        /* 0 or 1: every stream sends every reference element (the reference's
+                              * behaviour); P > 1: stream s sends the reference element of grid
+                              * column c only if c % P == s % P and zero otherwise (per-stream
+                              * pilots for MIMO estimation; no counterpart in the reference) */
 } hpx_frame_desc;
 
 typedef struct hpx_frame hpx_frame;
@@ -251,6 +255,16 @@ hpx_status hpx_detect_ideal(const hpx_fading* fading, const void* state, const h
                             int32_t mode, const hpx_cf32* grid, int32_t grid_columns,
                             const float* noise_var, uint64_t seed, int64_t drop0, int32_t num_drops,
                             uint32_t* errors, void* stream);
+
+/* Fused receiver for a CSI grid from any estimator: grid[B][Nrx][num_words][grid_columns]
+ * and csi[B][Nrx][Ntx][num_words][csi_columns] -> pick -> equalize (ZF or LMMSE) -> hard
+ * demap -> compare with the regenerated Philox bits -> errors[B]. The same chain as
+ * hpx_detect_ideal (modem/modem.py:1192-1267, modem/evaluators.py:239-258) with the
+ * channel read instead of computed; serves the LS, LMMSE and learned estimators. */
+hpx_status hpx_detect_csi(const hpx_frame* frame, int32_t num_rx, int32_t num_tx, int32_t mode,
+                          const hpx_cf32* grid, int32_t grid_columns, const hpx_cf32* csi,
+                          int32_t csi_columns, const float* noise_var, uint64_t seed, int64_t drop0,
+                          int32_t num_drops, uint32_t* errors, void* stream);
 
 /* Fused SISO receiver with LS estimation: grid[B][num_words][grid_columns] -> LS ->
  * pick -> ZF (or LMMSE) -> hard demap -> errors[B]. */

@@ -60,6 +60,11 @@ class FrameSpec:
     sections: list
     modulation_order: int = 16
     dc_suppression: bool = True
+    # Engine extension for MIMO pilots (the reference has no MIMO reference
+    # scheme): with pilot_comb = P > 1, stream s transmits the reference element at
+    # grid column c only if c % P == s % P and sends zero there otherwise, so each
+    # stream's pilots are alone on their subcarriers.
+    pilot_comb: int = 0
 
 
 class FrameLayout:
@@ -121,6 +126,21 @@ class FrameLayout:
         seq = mapping.get_mapping(self.order)
         reps = int(np.ceil(max(self.num_refs, 1) / seq.size))
         return np.tile(seq, reps)[: self.num_refs]
+
+    def stream_ref_mask(self, stream: int) -> np.ndarray:
+        """Reference elements stream ``stream`` actually transmits (``pilot_comb``)."""
+
+        comb = self.spec.pilot_comb
+        if comb <= 1:
+            return self.ref_mask.copy()
+        cols = np.arange(self.N)[None, :] % comb == stream % comb
+        return self.ref_mask & cols
+
+    def stream_pilot_symbols(self, stream: int) -> np.ndarray:
+        """Reference symbols of one stream in frame order, zero where it is silent."""
+
+        keep = self.stream_ref_mask(stream)[self.ref_mask]
+        return np.where(keep, self.pilot_symbols(), 0)
 
     def bits_per_frame(self) -> int:
         return self.num_data * self.bits_per_symbol

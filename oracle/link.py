@@ -37,7 +37,7 @@ class LinkConfig:
     sampling_rate: float
     num_tx: int = 1
     num_rx: int = 1
-    estimator: str = "ls"        # "ls" | "ideal"
+    estimator: str = "ls"        # "ls" | "ideal" | "lmmse" (tap-domain LMMSE, engine extension)
     equalizer: str = "zf"        # "zf" | "lmmse"
     noise: str = "ebn0"          # "ebn0" | "snr"
 
@@ -58,7 +58,7 @@ def simulate_drop(cfg: LinkConfig, seed: int, drop: int, level_db: float, keep: 
     M = layout.order
     nbits = layout.bits_per_frame()
     tx_bits = np.stack([streams.data_bits(seed, drop, s, nbits) for s in range(cfg.num_tx)])
-    x = np.stack([ofdm.modulate(layout, mapping.get_symbols(M, tx_bits[s])) for s in range(cfg.num_tx)])
+    x = np.stack([ofdm.modulate(layout, mapping.get_symbols(M, tx_bits[s]), s) for s in range(cfg.num_tx)])
     sample = fading.realize(cfg.channel, seed, drop, cfg.num_rx, cfg.num_tx)
     y = fading.propagate(sample, x, fs)
     p = noise_power(cfg, layout, level_db)
@@ -68,9 +68,11 @@ def simulate_drop(cfg: LinkConfig, seed: int, drop: int, level_db: float, keep: 
     frame = y[:, :T]
     grids = np.stack([ofdm.demodulate(layout, frame[r]) for r in range(cfg.num_rx)])  # (Nrx, W, N)
     if cfg.estimator == "ls":
-        if cfg.num_rx != 1 or cfg.num_tx != 1:
+        if (cfg.num_rx != 1 or cfg.num_tx != 1) and layout.spec.pilot_comb < max(cfg.num_tx, 2):
             raise NotImplementedError("Least-Squares channel estimation is only implemented for SISO links")
-        H = estimation.ls_estimate(layout, grids[0])[None, None]
+        H = estimation.mimo_ls_estimate(layout, grids, cfg.num_tx)
+    elif cfg.estimator == "lmmse":
+        H = estimation.tap_lmmse_estimate(layout, grids, cfg.channel, fs, p, cfg.num_tx)
     else:
         H = estimation.ideal_csi(layout, sample, fs)
     ydata = ofdm.pick(layout, grids)           # (Nrx, K)

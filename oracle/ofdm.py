@@ -19,8 +19,9 @@ import numpy as np
 from .frame import FrameLayout
 
 
-def place(layout: FrameLayout, data_symbols: np.ndarray) -> np.ndarray:
-    """Data symbols -> (words, N) grid with reference symbols inserted."""
+def place(layout: FrameLayout, data_symbols: np.ndarray, stream: int = 0) -> np.ndarray:
+    """Data symbols -> (words, N) grid with reference symbols inserted (the
+    stream's own under a pilot comb)."""
 
     data_symbols = np.asarray(data_symbols).reshape(-1)
     if data_symbols.size != layout.num_data:
@@ -29,7 +30,7 @@ def place(layout: FrameLayout, data_symbols: np.ndarray) -> np.ndarray:
             f"({data_symbols.size} != {layout.num_data})"
         )
     grid = np.zeros((layout.num_words, layout.N), dtype=np.complex128)
-    grid[layout.ref_mask] = layout.pilot_symbols()
+    grid[layout.ref_mask] = layout.stream_pilot_symbols(stream)
     grid[layout.data_mask] = data_symbols
     return grid
 
@@ -51,8 +52,8 @@ def modulate_grid(layout: FrameLayout, grid: np.ndarray) -> np.ndarray:
     return out
 
 
-def modulate(layout: FrameLayout, data_symbols: np.ndarray) -> np.ndarray:
-    return modulate_grid(layout, place(layout, data_symbols))
+def modulate(layout: FrameLayout, data_symbols: np.ndarray, stream: int = 0) -> np.ndarray:
+    return modulate_grid(layout, place(layout, data_symbols, stream))
 
 
 def demodulate(layout: FrameLayout, samples: np.ndarray) -> np.ndarray:

@@ -22,6 +22,16 @@ def mimo_frame(order: int = 64) -> FrameSpec:
     return FrameSpec(N, [Resource(1, CP / N, [(DATA, U)])], [Section(14, [0])], order, True)
 
 
+def pilot_frame(order: int = 64, comb: int = 4) -> FrameSpec:
+    """1024-point 4x4 frame with per-stream pilots: words 0 and 7 carry reference
+    elements on all 600 used subcarriers, stream s transmitting on columns
+    c % 4 == s (pilot comb 4); the other 12 words carry data."""
+
+    N, U, CP = 1024, 600, 72
+    res = [Resource(1, CP / N, [(DATA, U)]), Resource(1, CP / N, [(REFERENCE, U)])]
+    return FrameSpec(N, res, [Section(1, [1, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0])], order, True, comb)
+
+
 # name: (delays [samples], power, rice, S, doppler, los_doppler, gain, Nrx, Ntx, T, fs)
 FADING_CASES = {
     "c1": (np.arange(6), 10 ** (-0.3 * np.arange(6)), np.zeros(6), 20, 100.0, None, 1.0, 1, 1, 3836, 15.36e6),

@@ -41,7 +41,7 @@ def frame_handle(layout):
     desc = _lib.FrameDesc(layout.N, layout.num_words, layout.num_used, layout.order, int(layout.spec.dc_suppression),
                           prefix.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                           zero.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
-                          kind.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)))
+                          kind.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), int(layout.spec.pilot_comb))
     h = ctypes.c_void_p()
     _lib.check(_lib.load().hpx_frame_create(ctypes.byref(desc), ctypes.byref(h)))
     return h
