@@ -115,6 +115,12 @@ _SIGNATURES = {
     "hpx_link_run_static": [c_void_p, c_void_p, c_void_p, c_int32, c_uint64, c_int64, c_int32, c_void_p, c_void_p,
                             c_void_p],
     "hpx_detect_ls": [c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64, c_int64, c_int32, c_void_p, c_void_p],
+    "hpx_ls_create_streams": [c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p],
+    "hpx_ls_estimate_streams": [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p],
+    "hpx_lmmse_create": [c_void_p, c_void_p, c_int32, c_void_p],
+    "hpx_lmmse_destroy": [c_void_p],
+    "hpx_lmmse_estimate": [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
+    "hpx_csi_error": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
     "hpx_detect_csi": [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64,
                        c_int64, c_int32, c_void_p, c_void_p],
 }

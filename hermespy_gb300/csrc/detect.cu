@@ -5,6 +5,7 @@
 struct hpx_ls {
   const hpx_frame* frame;
   int C;          // columns of the estimate
+  int ntx = 1;    // streams: one interpolation table of W*C rows each
   int nnz;
   int32_t* d_indptr = nullptr;   // [W*C + 1]
   int32_t* d_indices = nullptr;  // [nnz] reference index
@@ -340,13 +341,14 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
   block_count(local, errors + b);
 }
 
-__global__ void k_ls_estimate(int W, int C, const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+// rows = streams * W * C (the stacked tables); blockIdx.y = received grid (drop, rx).
+__global__ void k_ls_estimate(int W, int rows, const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
                               const float* __restrict__ weights, const int32_t* __restrict__ ref_word,
                               const int32_t* __restrict__ ref_column, const float2* __restrict__ pilots,
                               const float2* __restrict__ grid, int gcols, float2* __restrict__ est) {
   const int b = blockIdx.y;
   const float2* gb = grid + (int64_t)b * W * gcols;
-  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < W * C; row += gridDim.x * blockDim.x) {
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < rows; row += gridDim.x * blockDim.x) {
     float2 h = make_float2(0.f, 0.f);
     for (int e = indptr[row]; e < indptr[row + 1]; ++e) {
       const int p = indices[e];
@@ -356,7 +358,7 @@ __global__ void k_ls_estimate(int W, int C, const int32_t* __restrict__ indptr, 
       const float2 ls = make_float2((yp.x * xp.x + yp.y * xp.y) / den, (yp.y * xp.x - yp.x * xp.y) / den);
       h = cadd(h, cscale(ls, weights[e]));
     }
-    est[(int64_t)b * W * C + row] = h;
+    est[(int64_t)b * rows + row] = h;
   }
 }
 
@@ -450,15 +452,19 @@ hpx_status detect_ideal_tx(int ntx, const hpx_fading* f, const void* state, cons
 
 extern "C" {
 
-hpx_status hpx_ls_create(const hpx_frame* frame, int32_t C, const int32_t* indptr, const int32_t* indices,
-                         const float* weights, hpx_ls** out) {
+hpx_status hpx_ls_create_streams(const hpx_frame* frame, int32_t C, int32_t num_streams, const int32_t* indptr,
+                                 const int32_t* indices, const float* weights, hpx_ls** out) {
   if (!frame || !out || !indptr) return hpx_fail(HPX_ERR_ARG, "ls: null argument");
   *out = nullptr;
   const int W = frame->info.num_words;
   if (C < frame->info.num_columns || C > frame->info.num_subcarriers)
     return hpx_fail(HPX_ERR_ARG, "ls: columns must cover the frame's resource columns");
   if (frame->info.num_refs < 1) return hpx_fail(HPX_ERR_ARG, "ls: frame has no reference elements");
-  const int rows = W * C;
+  if (num_streams < 1 || num_streams > 64) return hpx_fail(HPX_ERR_ARG, "ls: num_streams must be in [1, 64]");
+  if (num_streams > 1 && frame->pilot_comb < num_streams)
+    return hpx_fail(HPX_ERR_UNSUPPORTED, "Least-Squares channel estimation of %d streams needs a pilot comb of at "
+                                         "least %d (frame has %d)", num_streams, num_streams, frame->pilot_comb);
+  const int rows = W * C * num_streams;
   const int nnz = indptr[rows];
   if (indptr[0] != 0 || nnz < 0) return hpx_fail(HPX_ERR_ARG, "ls: malformed table");
   for (int r = 0; r < rows; ++r)
@@ -476,6 +482,7 @@ hpx_status hpx_ls_create(const hpx_frame* frame, int32_t C, const int32_t* indpt
   hpx_ls* ls = new hpx_ls();
   ls->frame = frame;
   ls->C = C;
+  ls->ntx = num_streams;
   ls->nnz = nnz;
   auto up = [](void** dst, const void* src, size_t bytes) -> cudaError_t {
     if (bytes == 0) {
@@ -499,6 +506,11 @@ hpx_status hpx_ls_create(const hpx_frame* frame, int32_t C, const int32_t* indpt
   return HPX_OK;
 }
 
+hpx_status hpx_ls_create(const hpx_frame* frame, int32_t C, const int32_t* indptr, const int32_t* indices,
+                         const float* weights, hpx_ls** out) {
+  return hpx_ls_create_streams(frame, C, 1, indptr, indices, weights, out);
+}
+
 hpx_status hpx_ls_destroy(hpx_ls* ls) {
   if (!ls) return HPX_OK;
   void* p[] = {ls->d_indptr, ls->d_indices, ls->d_weights, ls->d_ref_word, ls->d_ref_column};
@@ -515,9 +527,28 @@ hpx_status hpx_ls_estimate(const hpx_ls* ls, const hpx_cf32* grid, int32_t gcols
   if (gcols < ls->frame->info.num_columns) return hpx_fail(HPX_ERR_SHAPE, "ls_estimate: grid too narrow");
   if (B == 0) return HPX_OK;
   if (B > 65535) return hpx_fail(HPX_ERR_ARG, "ls_estimate: batch too large");
+  if (ls->ntx != 1) return hpx_fail(HPX_ERR_ARG, "ls_estimate: table of %d streams (use hpx_ls_estimate_streams)", ls->ntx);
   const int W = ls->frame->info.num_words;
   dim3 grid_dim((W * ls->C + 255) / 256, B);
-  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, ls->C, ls->d_indptr, ls->d_indices, ls->d_weights,
+  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, W * ls->C, ls->d_indptr, ls->d_indices, ls->d_weights,
+                                                         ls->d_ref_word, ls->d_ref_column, ls->frame->d_pilots,
+                                                         reinterpret_cast<const float2*>(grid), gcols,
+                                                         reinterpret_cast<float2*>(est));
+  HPX_LAUNCHED("ls_estimate");
+  return HPX_OK;
+}
+
+hpx_status hpx_ls_estimate_streams(const hpx_ls* ls, const hpx_cf32* grid, int32_t gcols, int32_t nrx, int32_t B,
+                                   hpx_cf32* est, void* stream) {
+  if (!ls || !grid || !est) return hpx_fail(HPX_ERR_ARG, "ls_estimate: null argument");
+  if (B < 0 || nrx < 1) return hpx_fail(HPX_ERR_ARG, "ls_estimate: bad batch");
+  if (gcols < ls->frame->info.num_columns) return hpx_fail(HPX_ERR_SHAPE, "ls_estimate: grid too narrow");
+  if (B == 0) return HPX_OK;
+  if ((int64_t)B * nrx > 65535) return hpx_fail(HPX_ERR_ARG, "ls_estimate: batch too large");
+  const int W = ls->frame->info.num_words;
+  const int rows = ls->ntx * W * ls->C;
+  dim3 grid_dim((rows + 255) / 256, B * nrx);
+  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, rows, ls->d_indptr, ls->d_indices, ls->d_weights,
                                                          ls->d_ref_word, ls->d_ref_column, ls->frame->d_pilots,
                                                          reinterpret_cast<const float2*>(grid), gcols,
                                                          reinterpret_cast<float2*>(est));
@@ -596,6 +627,7 @@ hpx_status hpx_detect_ls(const hpx_ls* ls, int32_t mode, const hpx_cf32* grid, i
   if (mode == HPX_EQ_LMMSE && !nv) return hpx_fail(HPX_ERR_ARG, "detect_ls: LMMSE needs noise variances");
   if (B < 0 || drop0 < 0) return hpx_fail(HPX_ERR_ARG, "detect_ls: bad drop range");
   const hpx_frame* fr = ls->frame;
+  if (ls->ntx != 1) return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_ls: SISO tables only (use hpx_detect_csi)");
   if (gcols < fr->info.num_columns) return hpx_fail(HPX_ERR_SHAPE, "detect_ls: grid too narrow");
   if (B == 0) return HPX_OK;
   if (B > 65535) return hpx_fail(HPX_ERR_ARG, "detect_ls: batch above 65535 drops per call");

@@ -1,10 +1,13 @@
 """Batched Monte Carlo drop engine.
 
 ``LinkEngine`` runs whole drops of a simplex OFDM link over a
-``MultipathFadingChannel`` in batches on the GPU through ``hpx_link_run``: one
-call realizes the channels, generates and modulates the Philox bits, propagates
-with AWGN, demodulates, estimates (ideal CSI or LS), equalizes (ZF or LMMSE),
-demaps and counts bit errors per drop. It replaces the reference's per-drop
+``MultipathFadingChannel`` in batches on the GPU. With ideal CSI or SISO LS one
+``hpx_link_run`` call realizes the channels, generates and modulates the Philox
+bits, propagates with AWGN, demodulates, estimates, equalizes (ZF or LMMSE),
+demaps and counts bit errors per drop. The MIMO estimators of a pilot-comb frame
+(per-stream LS, tap-domain LMMSE, the learned estimator) run the same stages as
+separate launches with the estimate materialized as a CSI grid, followed by
+``hpx_detect_csi``. It replaces the reference's per-drop
 Python loop (``MonteCarloActor.__run_batch``, core/pymonte/actors.py:367-452,
 running ``SimulationScenario._drop`` and ``BitErrorEvaluator`` per sample) for
 throughput runs; every drop is the same drop the per-drop API simulates for the
@@ -22,7 +25,7 @@ from scipy.stats import beta
 
 from . import _lib
 from .channel import MultipathFadingChannel
-from .estimation import ls_interpolation_table
+from .estimation import ls_interpolation_table, ls_stream_tables
 from .waveform import OFDMWaveform
 
 
@@ -53,9 +56,11 @@ class BerPoint:
 class LinkEngine:
     def __init__(self, waveform: OFDMWaveform, channel: MultipathFadingChannel, num_tx: int, num_rx: int,
                  sampling_rate: float, estimator: str = "ideal", equalizer: str = "lmmse", noise: str = "snr",
-                 max_drops: int = 4096, seed: int = 0) -> None:
-        if estimator not in ("ideal", "ls"):
-            raise ValueError("estimator must be 'ideal' or 'ls'")
+                 max_drops: int = 4096, seed: int = 0, model=None) -> None:
+        if estimator not in ("ideal", "ls", "lmmse", "learned"):
+            raise ValueError("estimator must be 'ideal', 'ls', 'lmmse' or 'learned'")
+        if estimator == "learned" and model is None:
+            raise ValueError("the learned estimator needs a model")
         if equalizer not in ("zf", "lmmse"):
             raise ValueError("equalizer must be 'zf' or 'lmmse'")
         if noise not in ("snr", "ebn0"):
@@ -71,33 +76,119 @@ class LinkEngine:
         self._fading = channel.handle(num_rx, num_tx, sampling_rate)
         self._frame = waveform._frame()
         self._ls = None
-        if estimator == "ls" and (num_tx != 1 or num_rx != 1):
+        self._lmmse = None
+        self._link = None
+        self.model = model
+        comb = waveform.pilot_comb
+        cols = waveform._layout()["num_columns"]
+        mask = waveform.resource_mask[0][:, :cols]
+        siso = num_tx == 1 and num_rx == 1
+        if estimator == "ls" and not siso and comb < max(num_tx, 2):
             raise NotImplementedError("Least-Squares channel estimation is only implemented for SISO links")
-        if estimator == "ls":
-            mask = waveform.resource_mask[0]
-            indptr, indices, weights = ls_interpolation_table(mask[:, : waveform._layout()["num_columns"]])
+        self.staged = estimator in ("lmmse", "learned") or (estimator == "ls" and not siso)
+        if estimator in ("ls", "learned"):
+            streams = num_tx if self.staged else 1
+            if self.staged:
+                indptr, indices, weights = ls_stream_tables(mask, comb, streams)
+            else:
+                indptr, indices, weights = ls_interpolation_table(mask)
             h = ctypes.c_void_p()
-            _lib.check(_lib.load().hpx_ls_create(self._frame, mask[:, : waveform._layout()["num_columns"]].shape[1],
-                                                 indptr.ctypes.data_as(ctypes.c_void_p),
-                                                 indices.ctypes.data_as(ctypes.c_void_p),
-                                                 weights.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h)))
+            _lib.check(_lib.load().hpx_ls_create_streams(self._frame, cols, streams,
+                                                         indptr.ctypes.data_as(ctypes.c_void_p),
+                                                         indices.ctypes.data_as(ctypes.c_void_p),
+                                                         weights.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h)))
             self._ls = h
-        h = ctypes.c_void_p()
-        _lib.check(_lib.load().hpx_link_create(self._frame, self._fading.handle, self._ls,
-                                               _lib.EST_IDEAL if estimator == "ideal" else _lib.EST_LS,
-                                               _lib.EQ_ZF if equalizer == "zf" else _lib.EQ_LMMSE, self.max_drops,
-                                               ctypes.byref(h)))
-        self._link = h
+        if estimator == "lmmse":
+            h = ctypes.c_void_p()
+            _lib.check(_lib.load().hpx_lmmse_create(self._frame, self._fading.handle, cols, ctypes.byref(h)))
+            self._lmmse = h
+        self.num_columns = cols
+        if self.staged:
+            self._alloc(self.max_drops)
+        else:
+            h = ctypes.c_void_p()
+            _lib.check(_lib.load().hpx_link_create(self._frame, self._fading.handle, self._ls,
+                                                   _lib.EST_IDEAL if estimator == "ideal" else _lib.EST_LS,
+                                                   _lib.EQ_ZF if equalizer == "zf" else _lib.EQ_LMMSE,
+                                                   self.max_drops, ctypes.byref(h)))
+            self._link = h
         self.bits_per_drop = waveform.bits_per_frame() * num_tx
+
+    def _alloc(self, n: int) -> None:
+        """Stage buffers of the staged estimators for batches of up to n drops."""
+
+        wf, dev = self.waveform, self.device
+        T = wf.samples_per_frame()
+        D = self._fading.max_delay
+        W = wf.words_per_frame
+        C = self.num_columns
+        self._T, self._D = T, D
+        self._state = self._fading.new_state(n)
+        self._x = torch.empty((n, self.num_tx, T), dtype=torch.complex64, device=dev)
+        self._y = torch.empty((n, self.num_rx, T + D), dtype=torch.complex64, device=dev)
+        self._grid = torch.empty((n, self.num_rx, W, C), dtype=torch.complex64, device=dev)
+        self._csi = torch.empty((n, self.num_rx, self.num_tx, W, C), dtype=torch.complex64, device=dev)
 
     def __del__(self):
         try:
             if _lib._lib is not None:
-                _lib._lib.hpx_link_destroy(self._link)
+                if self._link is not None:
+                    _lib._lib.hpx_link_destroy(self._link)
                 if self._ls is not None:
                     _lib._lib.hpx_ls_destroy(self._ls)
+                if self._lmmse is not None:
+                    _lib._lib.hpx_lmmse_destroy(self._lmmse)
         except Exception:
             pass
+
+    def receive(self, drop0: int, noise_power: torch.Tensor, stream: torch.cuda.Stream | None = None) -> None:
+        """Staged transmit, channel and receive of drops [drop0, drop0 + n): leaves the
+        received grids in ``self._grid[:n]`` (and the channel state in ``self._state``)."""
+
+        n = noise_power.numel()
+        if n > self.max_drops:
+            raise ValueError(f"at most {self.max_drops} drops per call")
+        sp = _lib.stream_ptr(stream)
+        fh = self._fading.handle
+        _lib.call("hpx_fading_realize", fh, self.seed, int(drop0), n, _lib.ptr(self._state), sp)
+        _lib.call("hpx_ofdm_modulate_bits", self._frame, self.seed, int(drop0), n, self.num_tx, _lib.ptr(self._x), sp)
+        _lib.call("hpx_fading_propagate", fh, _lib.ptr(self._state), n, _lib.ptr(self._x), self._T,
+                  _lib.ptr(self._y), _lib.ptr(noise_power), self.seed, int(drop0), sp)
+        _lib.call("hpx_ofdm_demodulate", self._frame, _lib.ptr(self._y), self._T + self._D, n * self.num_rx,
+                  self.num_columns, _lib.ptr(self._grid), sp)
+
+    def estimate(self, n: int, noise_power: torch.Tensor, stream: torch.cuda.Stream | None = None,
+                 estimator: str | None = None) -> torch.Tensor:
+        """Channel estimate of the received grids of the last ``receive`` call:
+        (n, Nrx, Ntx, W, C) on the device."""
+
+        est = estimator or self.estimator
+        sp = _lib.stream_ptr(stream)
+        C = self.num_columns
+        out = self._csi[:n]
+        if est == "ideal":
+            _lib.call("hpx_fading_ideal_csi", self._fading.handle, _lib.ptr(self._state), n, self._frame, C,
+                      _lib.ptr(out), sp)
+        elif est == "ls":
+            _lib.call("hpx_ls_estimate_streams", self._ls, _lib.ptr(self._grid), C, self.num_rx, n, _lib.ptr(out), sp)
+        elif est == "lmmse":
+            _lib.call("hpx_lmmse_estimate", self._lmmse, _lib.ptr(self._grid), C, self.num_rx, n,
+                      _lib.ptr(noise_power), _lib.ptr(out), sp)
+        elif est == "learned":
+            _lib.call("hpx_ls_estimate_streams", self._ls, _lib.ptr(self._grid), C, self.num_rx, n, _lib.ptr(out), sp)
+            self.model.refine(out, stream)
+        else:
+            raise ValueError(f"unknown estimator {est}")
+        return out
+
+    def detect(self, drop0: int, n: int, noise_power: torch.Tensor, errors: torch.Tensor,
+               stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+        C = self.num_columns
+        _lib.call("hpx_detect_csi", self._frame, self.num_rx, self.num_tx,
+                  _lib.EQ_ZF if self.equalizer == "zf" else _lib.EQ_LMMSE, _lib.ptr(self._grid), C,
+                  _lib.ptr(self._csi), C, _lib.ptr(noise_power), self.seed, int(drop0), n, _lib.ptr(errors),
+                  _lib.stream_ptr(stream))
+        return errors
 
     def noise_power(self, level_db) -> np.ndarray:
         """Noise power of EBN0 / SNR levels in dB (simulation/modem/noise.py:97-98,
@@ -117,6 +208,10 @@ class LinkEngine:
         n = noise_power.numel()
         if errors is None:
             errors = torch.empty(n, dtype=torch.int32, device=self.device)
+        if self.staged:
+            self.receive(drop0, noise_power, stream)
+            self.estimate(n, noise_power, stream)
+            return self.detect(drop0, n, noise_power, errors, stream)
         _lib.call("hpx_link_run", self._link, self.seed, int(drop0), n, _lib.ptr(noise_power), _lib.ptr(errors),
                   _lib.stream_ptr(stream))
         return errors

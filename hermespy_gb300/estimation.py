@@ -77,6 +77,31 @@ def ls_interpolation_table(ref_mask: np.ndarray) -> tuple[np.ndarray, np.ndarray
     return indptr, np.concatenate(indices).astype(np.int32), np.concatenate(weights).astype(np.float32)
 
 
+def ls_stream_tables(ref_mask: np.ndarray, comb: int, num_streams: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Stacked CSR tables of ``num_streams`` streams under a pilot comb.
+
+    Stream ``s`` owns the reference elements of grid columns ``c % comb == s % comb``;
+    its table is ``ls_interpolation_table`` of that sub-mask with the indices mapped
+    back to the frame's reference numbering (row-major over the grid).
+    """
+
+    W, C = ref_mask.shape
+    if num_streams > 1 and comb < num_streams:
+        raise NotImplementedError("Least-Squares channel estimation of several streams needs a pilot comb")
+    ptrs, idxs, wts = [np.zeros(1, dtype=np.int64)], [], []
+    base = 0
+    for s in range(num_streams):
+        sub = ref_mask & (np.arange(C)[None, :] % comb == s % comb) if comb > 1 else ref_mask
+        gidx = np.nonzero(sub[ref_mask])[0]
+        indptr, indices, weights = ls_interpolation_table(sub)
+        ptrs.append(indptr[1:].astype(np.int64) + base)
+        idxs.append(gidx[indices])
+        wts.append(weights)
+        base += int(indptr[-1])
+    return (np.concatenate(ptrs).astype(np.int32), np.concatenate(idxs).astype(np.int32),
+            np.concatenate(wts).astype(np.float32))
+
+
 class OrthogonalLeastSquaresChannelEstimation(ChannelEstimation):
     """Least-squares estimation with linear interpolation (SISO)."""
 

@@ -235,6 +235,40 @@ hpx_status hpx_ls_destroy(hpx_ls* ls);
 hpx_status hpx_ls_estimate(const hpx_ls* ls, const hpx_cf32* grid, int32_t grid_columns, int32_t batch,
                            hpx_cf32* estimate, void* stream);
 
+/* Least-squares interpolators of `num_streams` streams under a pilot comb: the CSR
+ * map stacks one table of num_words*num_columns rows per stream, each built from
+ * the stream's own reference elements like the SISO table (indices number the
+ * frame's reference elements). The reference's estimator stops at one stream
+ * (modem/waveforms/orthogonal/channel.py:32-35); this is its per-stream extension. */
+hpx_status hpx_ls_create_streams(const hpx_frame* frame, int32_t num_columns, int32_t num_streams,
+                                 const int32_t* indptr, const int32_t* indices, const float* weights,
+                                 hpx_ls** out);
+/* grid[B][Nrx][num_words][grid_columns] -> H[B][Nrx][num_streams][num_words][num_columns]. */
+hpx_status hpx_ls_estimate_streams(const hpx_ls* ls, const hpx_cf32* grid, int32_t grid_columns,
+                                   int32_t num_rx, int32_t batch, hpx_cf32* estimate, void* stream);
+
+/* Tap-domain LMMSE channel estimator with the channel's statistics (delays, powers,
+ * Doppler) known: weighted LS of the tap gains on each pilot word, per-tap LMMSE
+ * over the words with the Jakes correlation of the sum-of-sinusoids taps, then
+ * the tap DFT on every element. No counterpart in the reference. Tables are built
+ * at create time for one frame and one fading configuration. */
+typedef struct hpx_lmmse hpx_lmmse;
+hpx_status hpx_lmmse_create(const hpx_frame* frame, const hpx_fading* fading, int32_t num_columns,
+                            hpx_lmmse** out);
+hpx_status hpx_lmmse_destroy(hpx_lmmse* lmmse);
+/* grid[B][Nrx][num_words][grid_columns], noise_power[B] (per element) ->
+ * H[B][Nrx][Ntx][num_words][num_columns]. */
+hpx_status hpx_lmmse_estimate(const hpx_lmmse* lmmse, const hpx_cf32* grid, int32_t grid_columns,
+                              int32_t num_rx, int32_t batch, const float* noise_power, hpx_cf32* estimate,
+                              void* stream);
+
+/* Channel-estimate error over the frame's data elements, per drop:
+ * err[b] = sum |est - truth|^2, power[b] = sum |truth|^2 over pairs x data elements,
+ * est/truth[B][pairs][num_words][csi_columns]; NMSE = sum err / sum power. */
+hpx_status hpx_csi_error(const hpx_frame* frame, const hpx_cf32* estimate, const hpx_cf32* truth,
+                         int32_t csi_columns, int32_t pairs, int32_t batch, double* err, double* power,
+                         void* stream);
+
 enum { HPX_EQ_ZF = 0, HPX_EQ_LMMSE = 1 };
 
 /* Per-element equalization: H[B][Nrx][Ntx][K], y[B][Nrx][K] -> x[B][Ntx][K].
