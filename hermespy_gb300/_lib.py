@@ -121,6 +121,15 @@ _SIGNATURES = {
     "hpx_lmmse_destroy": [c_void_p],
     "hpx_lmmse_estimate": [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
     "hpx_csi_error": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
+    "hpx_cnn_num_params": [],
+    "hpx_cnn_create": [c_int32, c_int32, c_int32, c_void_p, c_uint64, c_void_p],
+    "hpx_cnn_destroy": [c_void_p],
+    "hpx_cnn_get_params": [c_void_p, c_void_p],
+    "hpx_cnn_get_grads": [c_void_p, c_void_p],
+    "hpx_cnn_refine": [c_void_p, c_void_p, c_int32, c_int32, c_void_p],
+    "hpx_cnn_train_step": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, ctypes.c_float, c_void_p, c_void_p],
+    "hpx_detect_massive": [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64, c_int64,
+                           c_int32, c_void_p, c_void_p, c_void_p, c_void_p],
     "hpx_detect_csi": [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64,
                        c_int64, c_int32, c_void_p, c_void_p],
 }

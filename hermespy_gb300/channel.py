@@ -59,16 +59,32 @@ class CustomAntennaCorrelation(AntennaCorrelation):
 
 
 class ExponentialAntennaCorrelation(AntennaCorrelation):
-    """Exponential correlation model: covariance entry (i, j) = rho^|i-j|."""
+    """Exponential correlation model: covariance entry (i, j) = rho^|i-j|.
 
-    def __init__(self, rho: float) -> None:
+    ``modes`` selects the array sides it describes, like the antenna mode the
+    reference passes to ``sample_covariance`` (fading.py:480-489): a base station
+    with correlated receive antennas serving independent single-antenna users
+    uses ``modes=("rx",)``; the other side is then uncorrelated (identity).
+    """
+
+    def __init__(self, rho: float, modes: tuple = ("rx", "tx")) -> None:
         if not 0.0 <= rho < 1.0:
             raise ValueError("correlation coefficient must be in [0, 1)")
         self.rho = float(rho)
+        self.modes = tuple(modes)
 
-    def sample_covariance(self, num_antennas: int) -> np.ndarray:
+    def sample_covariance(self, num_antennas: int, mode: str = "rx") -> np.ndarray:
         i = np.arange(num_antennas)
+        if mode not in self.modes:
+            return np.eye(num_antennas, dtype=np.complex128)
         return (self.rho ** np.abs(i[:, None] - i[None, :])).astype(np.complex128)
+
+
+def _covariance(model, num_antennas: int, mode: str) -> np.ndarray:
+    try:
+        return model.sample_covariance(num_antennas, mode)
+    except TypeError:  # models without an antenna-mode argument describe both sides
+        return model.sample_covariance(num_antennas)
 
 
 def _num_antennas(device) -> int:
@@ -350,8 +366,8 @@ class MultipathFadingChannel:
         if h is None:
             rx_cov = tx_cov = None
             if self.antenna_correlation is not None:
-                rx_cov = self.antenna_correlation.sample_covariance(num_rx)
-                tx_cov = self.antenna_correlation.sample_covariance(num_tx)
+                rx_cov = _covariance(self.antenna_correlation, num_rx, "rx")
+                tx_cov = _covariance(self.antenna_correlation, num_tx, "tx")
             h = _FadingHandle(self.delays, self.power_profile, self.rice_factors, self.num_sinusoids,
                               self.doppler_frequency, self.los_doppler_frequency, self.gain, num_rx, num_tx,
                               sampling_rate, rx_cov, tx_cov)
@@ -381,8 +397,8 @@ class MultipathFadingChannel:
         o = nrx * ntx
         spatial = np.exp(2j * np.pi * u[:o].reshape(nrx, ntx))
         if self.antenna_correlation is not None:
-            spatial = self.antenna_correlation.sample_covariance(nrx) @ spatial @ \
-                self.antenna_correlation.sample_covariance(ntx)
+            spatial = _covariance(self.antenna_correlation, nrx, "rx") @ spatial @ \
+                _covariance(self.antenna_correlation, ntx, "tx")
         los_angles = 2 * np.pi * u[o:o + L]
         nlos_angles = -np.pi + 2 * np.pi * u[o + L:o + L + L * S].reshape(L, S)
         los_phases = -np.pi + 2 * np.pi * u[o + L + L * S:o + 2 * L + L * S]

@@ -56,7 +56,7 @@ class BerPoint:
 class LinkEngine:
     def __init__(self, waveform: OFDMWaveform, channel: MultipathFadingChannel, num_tx: int, num_rx: int,
                  sampling_rate: float, estimator: str = "ideal", equalizer: str = "lmmse", noise: str = "snr",
-                 max_drops: int = 4096, seed: int = 0, model=None) -> None:
+                 max_drops: int = 4096, seed: int = 0, model=None, also: tuple = ()) -> None:
         if estimator not in ("ideal", "ls", "lmmse", "learned"):
             raise ValueError("estimator must be 'ideal', 'ls', 'lmmse' or 'learned'")
         if estimator == "learned" and model is None:
@@ -86,7 +86,9 @@ class LinkEngine:
         if estimator == "ls" and not siso and comb < max(num_tx, 2):
             raise NotImplementedError("Least-Squares channel estimation is only implemented for SISO links")
         self.staged = estimator in ("lmmse", "learned") or (estimator == "ls" and not siso)
-        if estimator in ("ls", "learned"):
+        # `also`: further estimators whose tables are built too, for estimate(estimator=...)
+        wanted = {estimator, *also}
+        if self.staged and wanted & {"ls", "learned"} or estimator in ("ls", "learned"):
             streams = num_tx if self.staged else 1
             if self.staged:
                 indptr, indices, weights = ls_stream_tables(mask, comb, streams)
@@ -98,7 +100,7 @@ class LinkEngine:
                                                          indices.ctypes.data_as(ctypes.c_void_p),
                                                          weights.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h)))
             self._ls = h
-        if estimator == "lmmse":
+        if "lmmse" in wanted:
             h = ctypes.c_void_p()
             _lib.check(_lib.load().hpx_lmmse_create(self._frame, self._fading.handle, cols, ctypes.byref(h)))
             self._lmmse = h

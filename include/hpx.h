@@ -306,6 +306,41 @@ hpx_status hpx_detect_ls(const hpx_ls* ls, int32_t mode, const hpx_cf32* grid, i
                          const float* noise_var, uint64_t seed, int64_t drop0, int32_t num_drops,
                          uint32_t* errors, void* stream);
 
+/* ------------------------------------------------- learned estimator (CNN) */
+
+/* Residual CNN that refines per-stream LS estimates of a 16-pair MIMO grid (4x4
+ * antennas) into the full channel: 6 conv layers, 3x3 kernels, 32 channels
+ * (16 pairs x re/im), ReLU between layers, output = LS + last layer. BF16 weights
+ * and activations, FP32 accumulation on the tensor cores. No counterpart in the
+ * reference. Parameters: weights [6][32 out][9 taps][32 in] then biases [6][32],
+ * FP32 (hpx_cnn_num_params values); `params` NULL initialises them from `seed`. */
+typedef struct hpx_cnn hpx_cnn;
+int32_t hpx_cnn_num_params(void);
+hpx_status hpx_cnn_create(int32_t num_words, int32_t num_columns, int32_t max_batch, const float* params,
+                          uint64_t seed, hpx_cnn** out);
+hpx_status hpx_cnn_destroy(hpx_cnn* cnn);
+hpx_status hpx_cnn_get_params(const hpx_cnn* cnn, float* params);
+/* Gradient sums of the last training step (host copy, same layout as the parameters). */
+hpx_status hpx_cnn_get_grads(const hpx_cnn* cnn, float* grads);
+/* In place: csi[B][16][num_words][csi_columns] (LS estimate) -> refined estimate. */
+hpx_status hpx_cnn_refine(const hpx_cnn* cnn, hpx_cf32* csi, int32_t csi_columns, int32_t batch, void* stream);
+/* One Adam step on ls/truth[B][16][num_words][num_columns] (B <= max_batch), loss =
+ * sum |out - truth|^2 written to the device double `loss` (may be NULL). */
+hpx_status hpx_cnn_train_step(hpx_cnn* cnn, const hpx_cf32* ls, const hpx_cf32* truth, int32_t csi_columns,
+                              int32_t batch, float learning_rate, double* loss, void* stream);
+
+/* Fused massive-MIMO receiver with ideal CSI (16 transmit streams, 16/32/64 receive
+ * antennas): per data element the Gram H^H H and matched filter H^H y on the BF16
+ * tensor cores with split (3-term) products and FP32 accumulation, FP32 Cholesky
+ * (LMMSE: + s2 I; ZF: none), FP64 re-factorization for elements whose condition
+ * estimate (max/min Cholesky pivot)^2 exceeds 1e6, hard demap, error count.
+ * errors[B]; fp64_count[B] (may be NULL) = elements solved in FP64; equalized
+ * (may be NULL) = x[B][16][num_data]. No counterpart in the reference. */
+hpx_status hpx_detect_massive(const hpx_fading* fading, const void* state, const hpx_frame* frame,
+                              int32_t mode, const hpx_cf32* grid, int32_t grid_columns,
+                              const float* noise_var, uint64_t seed, int64_t drop0, int32_t num_drops,
+                              uint32_t* errors, uint32_t* fp64_count, hpx_cf32* equalized, void* stream);
+
 /* ------------------------------------------------------------------- noise */
 
 /* Add complex AWGN of power noise_power[b] to samples[batch][num_streams][num_samples]

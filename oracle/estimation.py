@@ -174,18 +174,20 @@ def ideal_csi(layout: FrameLayout, sample: fading.FadingSample, fs: float) -> np
     """(Nrx, Ntx, words, N) frequency-domain channel state."""
 
     T = layout.samples_per_frame
-    csi = fading.state(sample, T, fs, T)  # (Nrx, Ntx, T, taps)
+    # state(...) = spatial (x) siso: average and transform the shared SISO response,
+    # then scale by every pair's spatial coefficient (same values, no Nrx*Ntx*T*taps array)
+    siso = fading.siso_state(sample, T, fs, T)  # (T, taps)
     n = layout.N
-    num_taps = csi.shape[3]
-    out = np.empty(csi.shape[:2] + (layout.num_words, n), dtype=np.complex128)
+    num_taps = siso.shape[1]
+    out = np.empty(sample.spatial.shape + (layout.num_words, n), dtype=np.complex128)
     bins = layout.bins()
     for w in range(layout.num_words):
         s = int(layout.window_start[w])
-        avg = csi[:, :, s : s + n, :].mean(axis=2)  # (Nrx, Ntx, taps)
-        padded = np.zeros(csi.shape[:2] + (n,), dtype=np.complex128)
-        padded[..., : min(num_taps, n)] = avg[..., :n]
-        spec = np.fft.fft(padded, axis=-1)
-        out[:, :, w, :] = spec[..., bins]
+        avg = siso[s : s + n, :].mean(axis=0)  # (taps,)
+        padded = np.zeros(n, dtype=np.complex128)
+        padded[: min(num_taps, n)] = avg[:n]
+        spec = np.fft.fft(padded)
+        out[:, :, w, :] = sample.spatial[:, :, None] * spec[bins][None, None, :]
     return out
 
 

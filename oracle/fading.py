@@ -170,6 +170,21 @@ def propagate(sample: FadingSample, x: np.ndarray, fs: float) -> np.ndarray:
     return sample.spatial @ z
 
 
+def siso_state(sample: FadingSample, num_samples: int, fs: float, max_num_taps: int | None = None) -> np.ndarray:
+    """(T, taps) impulse response shared by every antenna pair; ``state`` is its
+    outer product with the spatial matrix (fading.py:345-369)."""
+
+    max_num_taps = num_samples if max_num_taps is None else max_num_taps
+    num_taps = min(1 + sample.config.max_delay_samples(fs), max_num_taps)
+    siso = np.zeros((num_samples, num_taps), dtype=np.complex128)
+    h = path_impulses(sample, num_samples, fs)
+    for l, d in enumerate(sample.config.delay_samples(fs)):
+        if d > num_taps:
+            continue
+        siso[:, d] += h[l]
+    return siso
+
+
 def state(sample: FadingSample, num_samples: int, fs: float, max_num_taps: int | None = None) -> np.ndarray:
     """(Nrx, Ntx, T, taps) impulse-response CSI (fading.py:345-369)."""
 

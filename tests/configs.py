@@ -32,6 +32,23 @@ def pilot_frame(order: int = 64, comb: int = 4) -> FrameSpec:
     return FrameSpec(N, res, [Section(1, [1, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0])], order, True, comb)
 
 
+def massive_frame(N: int = 4096, used: int = 3300, cp: int = 288, order: int = 16) -> FrameSpec:
+    """Massive-MIMO uplink frame: 14 data words (ideal CSI, no pilots)."""
+
+    return FrameSpec(N, [Resource(1, cp / N, [(DATA, used)])], [Section(14, [0])], order, True)
+
+
+def massive_channel(nrx: int = 64, rho: float = 0.7, fs: float = 61.44e6, taps: int = 8,
+                    doppler: float = 50.0) -> ofad.FadingConfig:
+    """8 taps at one-sample spacing with an exponential profile (3 dB per tap),
+    receive correlation rho^|i-j| at the base station, 50 Hz Doppler."""
+
+    k = np.arange(taps)
+    i = np.arange(nrx)
+    rx = rho ** np.abs(i[:, None] - i[None, :]).astype(np.complex128)
+    return ofad.FadingConfig(k / fs, 10 ** (-0.3 * k), np.zeros(taps), 20, doppler, None, 1.0, rx, None)
+
+
 # name: (delays [samples], power, rice, S, doppler, los_doppler, gain, Nrx, Ntx, T, fs)
 FADING_CASES = {
     "c1": (np.arange(6), 10 ** (-0.3 * np.arange(6)), np.zeros(6), 20, 100.0, None, 1.0, 1, 1, 3836, 15.36e6),

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_symbols():
     text = open(os.path.join(ROOT, "include", "hpx.h")).read()
-    return sorted(set(re.findall(r"^(?:hpx_status|int|const char\*)\s+(hpx_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:hpx_status|int|int32_t|const char\*)\s+(hpx_\w+)\s*\(", text, re.M)))
 
 
 @pytest.fixture(scope="module")
