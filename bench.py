@@ -1,20 +1,32 @@
 """Throughput benchmark of the GB300 link engine (one JSON line on stdout).
 
-Workload: 4x4 MIMO spatial multiplexing, 1024-point FFT with 600 used
-subcarriers, CP 72, 14 words, 64-QAM, 30.72 MHz sampling, 23-tap Rayleigh
-channel (delays k*50 ns, power -0.4k dB, 20 sinusoids, Doppler 500 Hz),
-ideal CSI with per-subcarrier 4x4 LMMSE detection, SNR uniform in [0, 30] dB
-per drop, 4096 drops per step, complex64 samples. Synthetic data: every bit,
-channel draw and noise sample comes from the engine's Philox streams.
+Workloads (``--workload``):
 
-One step = one batch of 4096 whole drops: realize -> transmit -> propagate +
-AWGN -> demodulate -> ideal CSI + LMMSE + demap + bit-error count. ``value``
-is simulated bits/s with the per-drop noise powers already in HBM; ``e2e`` is
-the same through the public ``LinkEngine.simulate`` call with host buffers
-(noise powers copied in, error counts copied out, inside the timed region).
+* ``estimators`` (default): the learned-vs-LMMSE comparison. 4x4 MIMO, 1024-point
+  FFT with 600 used subcarriers, CP 72, 14 words (words 0 and 7 carry per-stream
+  pilots, comb 4), 64-QAM, 30.72 MHz, 23-tap Rayleigh channel (k*50 ns, -0.4k dB,
+  20 sinusoids, 500 Hz), SNR U[0, 30] dB, 8192 drops per step. Three receive paths
+  run the same drops: per-stream LS + residual CNN (learned), tap-domain LMMSE
+  estimation, and per-stream LS, each followed by 4x4 LMMSE detection, demap and
+  bit-error count. ``value`` is the simulated bits/s of the path the estimator
+  policy selects (the CNN when its validation NMSE is within 0.5 dB of LMMSE's,
+  else LMMSE); every path's bits/s, BER and NMSE are in ``comparison``.
+* ``link4x4``: ideal CSI with per-subcarrier 4x4 LMMSE on the 14 data words
+  (201 600 bits per drop), 4096 drops per step.
+* ``massive``: 64 x 16 uplink, 4096-point FFT, 3300 used, CP 288, 14 words,
+  16-QAM, 8 taps (one-sample spacing, 3 dB per tap), 50 Hz, receive correlation
+  0.7^|i-j|, 61.44 MHz, 512 drops per step; split-BF16 tensor-core Gram + FP32
+  Cholesky LMMSE, error against an FP64 solve of the same systems.
 
-``--impl reference`` times the CPU restatement of the reference's drop (float64
-numpy, one process per host core) on a bounded sample of the same workload.
+One step = one batch of whole drops (realize -> transmit -> propagate + AWGN ->
+demodulate -> estimate -> equalize -> demap -> count), timed with CUDA events on
+the launching stream with the per-drop noise powers resident in HBM; ``e2e`` runs
+the public ``LinkEngine.run`` with host noise powers copied in and host error
+counts copied out inside the timed region. Every buffer of a step is larger than
+the 129 MB L2, so no flush is needed.
+
+``--impl reference`` times the float64 CPU restatement of the reference's drop
+(one process per host core) on a bounded sample of the same workload.
 """
 
 from __future__ import annotations
@@ -32,30 +44,45 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FS = 30.72e6
-N, U, CP, WORDS, ORDER = 1024, 600, 72, 14, 64
-NTX = NRX = 4
-DROPS = 4096
-BITS_PER_DROP = WORDS * U * 6 * NTX  # 201 600
 METRIC = "simulated bits/sec on 1 GB300, learned vs LMMSE estimator at equal BER; NMSE dB"
-CONFIG = {
-    "workload": "4x4 MIMO OFDM 1024/600 CP72 14 sym 64-QAM, 23-tap Rayleigh (k*50ns, -0.4k dB, 500 Hz), "
-                "ideal CSI + per-subcarrier 4x4 LMMSE, SNR U[0,30] dB",
-    "drops_per_step": DROPS,
-    "bits_per_drop": BITS_PER_DROP,
-    "samples": "complex64",
-    "l2": "working set per step ~5.3 GB (tx/rx samples, grids) > 129 MB L2; no flush needed",
+SEED = 20261203
+
+
+# ----------------------------------------------------------------- workloads
+class Spec:
+    def __init__(self, name, drops, bits_per_drop, config, fs):
+        self.name, self.drops, self.bits_per_drop, self.config, self.fs = name, drops, bits_per_drop, config, fs
+
+
+SPECS = {
+    "estimators": Spec("estimators", 8192, 12 * 600 * 6 * 4, {
+        "workload": "4x4 MIMO OFDM 1024/600 CP72 14 sym (pilot words 0, 7; comb 4) 64-QAM, 23-tap Rayleigh "
+                    "(k*50ns, -0.4k dB, 500 Hz), SNR U[0,30] dB; per-stream LS + residual CNN vs tap-domain "
+                    "LMMSE estimation, 4x4 LMMSE detection", "samples": "complex64"}, 30.72e6),
+    "link4x4": Spec("link4x4", 4096, 14 * 600 * 6 * 4, {
+        "workload": "4x4 MIMO OFDM 1024/600 CP72 14 sym 64-QAM, 23-tap Rayleigh (k*50ns, -0.4k dB, 500 Hz), "
+                    "ideal CSI + per-subcarrier 4x4 LMMSE, SNR U[0,30] dB", "samples": "complex64"}, 30.72e6),
+    "massive": Spec("massive", 512, 14 * 3300 * 4 * 16, {
+        "workload": "64x16 massive-MIMO uplink OFDM 4096/3300 CP288 14 sym 16-QAM, 8 taps (1-sample spacing, "
+                    "3 dB/tap), 50 Hz, rx correlation 0.7^|i-j|, 61.44 MHz, SNR U[0,30] dB; split-BF16 "
+                    "tensor-core Gram + FP32 Cholesky LMMSE", "samples": "complex64"}, 61.44e6),
 }
 
 
 def oracle_drop(args):
-    """One float64 oracle drop (runs in a worker process)."""
+    """One float64 oracle drop of a workload (runs in a worker process)."""
 
-    seed, drop, level = args
+    name, seed, drop, level = args
     from oracle.link import LinkConfig, simulate_drop
-    from tests.configs import mimo_channel, mimo_frame
+    from tests.configs import massive_channel, massive_frame, mimo_channel, mimo_frame, pilot_frame
 
-    cfg = LinkConfig(mimo_frame(ORDER), mimo_channel(FS), FS, NTX, NRX, "ideal", "lmmse", "snr")
+    if name == "estimators":
+        cfg = LinkConfig(pilot_frame(64, 4), mimo_channel(30.72e6), 30.72e6, 4, 4, "lmmse", "lmmse", "snr")
+    elif name == "link4x4":
+        cfg = LinkConfig(mimo_frame(64), mimo_channel(30.72e6), 30.72e6, 4, 4, "ideal", "lmmse", "snr")
+    else:
+        cfg = LinkConfig(massive_frame(), massive_channel(64, 0.7, 61.44e6), 61.44e6, 16, 64, "ideal", "lmmse",
+                         "snr")
     return simulate_drop(cfg, seed, drop, level)["errors"]
 
 
@@ -68,43 +95,57 @@ def cpu_pool():
     return mp.get_context("spawn").Pool(cores), cores
 
 
-def time_cpu(pool, cores, rounds: int, seed: int = 11) -> tuple[float, int, float]:
-    """Run `rounds` rounds of `cores` parallel oracle drops; returns (bits/s, drops, seconds)."""
+def cpu_workers(spec: Spec, cores: int) -> int:
+    """Concurrent oracle drops: every core, except for the 64x16 drop whose float64
+    channel tensors take about 1 GB per process."""
+
+    return min(cores, 8) if spec.name == "massive" else cores
+
+
+def time_cpu(pool, cores, spec: Spec, rounds: int, seed: int = 11) -> tuple[float, int, float]:
+    """`rounds` rounds of parallel oracle drops; returns (bits/s, drops, seconds)."""
 
     rng = np.random.default_rng(seed)
-    drops = rounds * cores
-    work = [(seed, 1_000_000 + i, float(rng.uniform(0, 30))) for i in range(drops)]
-    pool.map(oracle_drop, work[:cores])  # warm the workers (imports)
+    par = cpu_workers(spec, cores)
+    drops = max(1, rounds) * par
+    work = [(spec.name, seed, 1_000_000 + i, float(rng.uniform(0, 30))) for i in range(drops)]
+    if spec.name != "massive":
+        pool.map(oracle_drop, work[:par])  # warm the workers (imports, first drop)
     t0 = time.perf_counter()
     pool.map(oracle_drop, work, chunksize=1)
     dt = time.perf_counter() - t0
-    return drops * BITS_PER_DROP / dt, drops, dt
+    return drops * spec.bits_per_drop / dt, drops, dt
 
 
-def run_reference(args) -> None:
+def cpu_sample_text(spec, drops, secs):
+    est = {"estimators": "tap-domain LMMSE estimation", "link4x4": "ideal CSI", "massive": "ideal CSI"}[spec.name]
+    return (f"{drops} drops of the workload ({est}, LMMSE detection) in {secs:.1f} s: float64 numpy restatement "
+            f"of the reference's drop, one process per core")
+
+
+def run_reference(args, spec: Spec) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     pool, cores = cpu_pool()
+    rounds = 1 if spec.name != "massive" else 1
     for _ in range(args.warmup):
-        time_cpu(pool, cores, 1)
-    vals, drops, secs = [], 0, 0.0
+        time_cpu(pool, cores, spec, rounds)
+    drops, secs = 0, 0.0
     for k in range(args.steps):
-        v, d, s = time_cpu(pool, cores, 1, seed=100 + k)
-        vals.append(v)
+        _, d, s = time_cpu(pool, cores, spec, rounds, seed=100 + k)
         drops += d
         secs += s
     pool.close()
-    value = drops * BITS_PER_DROP / secs
+    value = drops * spec.bits_per_drop / secs
     line = {
         "impl": "reference",
         "metric": METRIC, "value": value, "unit": "bits/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox draws)",
-        "config": dict(CONFIG, drops_per_step=cores),
-        "cpu_baseline": {"value": value, "unit": "bits/s", "cores": cores, "kind": "port",
-                         "sample": f"{drops} drops of the workload (float64 numpy restatement of the reference's "
-                                   f"drop, one process per core)"},
+        "config": dict(spec.config, drops_per_step=cpu_workers(spec, cores) * rounds, bits_per_drop=spec.bits_per_drop),
+        "cpu_baseline": {"value": value, "unit": "bits/s", "cores": cpu_workers(spec, cores), "kind": "port",
+                         "sample": cpu_sample_text(spec, drops, secs)},
         "e2e": {"value": value, "unit": "bits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -158,32 +199,346 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def stage_bytes(T: int, D: int, stride: int) -> dict:
-    """Algorithmic HBM bytes per drop of each stage."""
+def peaks() -> dict:
+    out = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        with open(pp) as f:
+            m = json.load(f)
+        out = {"hbm_gbs": float(m.get("hbm_gbs", 6800.0)), "bf16_tflops": float(m.get("bf16_tflops", 1900.0)),
+               "src": "measured"}
+    return out
 
-    C = U
-    return {
-        "fading_realize": stride,
-        "ofdm_modulate_bits": 8 * NTX * T,
-        "fading_propagate": 8 * (NTX * T + NRX * (T + D)),
-        "ofdm_demodulate": 8 * NRX * WORDS * (N + C),
-        "detect_ideal_lmmse": 8 * NRX * WORDS * C + 4,
+
+class Timer:
+    """Stage-wise CUDA-event timing of a step function over `steps` steps."""
+
+    def __init__(self, torch, stream):
+        self.torch, self.stream = torch, stream
+
+    def run(self, step, stages, steps, warmup, drop0, stride):
+        torch = self.torch
+        for w in range(warmup):
+            step(drop0 + w * stride, None)
+        torch.cuda.synchronize()
+        events = [[torch.cuda.Event(enable_timing=True) for _ in range(len(stages) + 1)] for _ in range(steps)]
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(self.stream)
+        for k in range(steps):
+            step(drop0 + (warmup + k) * stride, events[k])
+        t1.record(self.stream)
+        torch.cuda.synchronize()
+        stage_ms = {s: 0.0 for s in stages}
+        for ev in events:
+            for i, s in enumerate(stages):
+                stage_ms[s] += ev[i].elapsed_time(ev[i + 1])
+        return t0.elapsed_time(t1), stage_ms
+
+
+def staged(calls, ev, stream):
+    """Run (stage, fn) pairs, recording an event before each and one at the end."""
+
+    for i, (_, fn) in enumerate(calls):
+        if ev is not None:
+            ev[i].record(stream)
+        fn()
+    if ev is not None:
+        ev[len(calls)].record(stream)
+
+
+def stage_report(stage_ms, steps, work, drops, pk):
+    """Per-stage ms, share, achieved rate and fraction of the measured peak.
+    work[s] = (per-drop amount, 'hbm' bytes | 'tensor' flops)."""
+
+    total = max(sum(stage_ms.values()), 1e-9)
+    info = {}
+    for s, ms in stage_ms.items():
+        avg = ms / steps
+        amount, bound = work[s]
+        if bound == "tensor":
+            rate = amount * drops / (avg / 1e3) / 1e12 if avg > 0 else 0.0
+            info[s] = {"ms": round(avg, 4), "share": round(ms / total, 4), "bound": "tensor",
+                       "algorithmic_flops": amount * drops, "achieved_tflops": round(rate, 2),
+                       "frac": round(rate / pk["bf16_tflops"], 4)}
+        else:
+            rate = amount * drops / (avg / 1e3) / 1e9 if avg > 0 else 0.0
+            info[s] = {"ms": round(avg, 4), "share": round(ms / total, 4), "bound": "hbm",
+                       "algorithmic_bytes": amount * drops, "achieved_gbs": round(rate, 1),
+                       "frac": round(rate / pk["hbm_gbs"], 4)}
+    return info
+
+
+def roofline_of(info, pk, traffic_key_map=None):
+    dom = max(info, key=lambda s: info[s]["ms"])
+    d = info[dom]
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get(dom)
+    if d["bound"] == "tensor":
+        return {"kernel": dom, "bound": "tensor", "achieved": d["achieved_tflops"], "peak": pk["bf16_tflops"],
+                "unit": "TFLOP/s", "frac": d["frac"], "traffic": traffic, "peak_source": pk["src"]}
+    return {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": d["frac"], "traffic": traffic, "peak_source": pk["src"]}
+
+
+def e2e_time(torch, eng, p_host, dev, drop0, steps):
+    """Public API end to end: pinned host noise powers in, host error counts out."""
+
+    n = p_host.size
+    p_pin = torch.from_numpy(p_host).pin_memory()
+    out_pin = torch.empty(n, dtype=torch.int32).pin_memory()
+
+    def one(d0):
+        pd = p_pin.to(dev, non_blocking=True)
+        e = eng.run(d0, pd)
+        out_pin.copy_(e, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    for w in range(2):
+        one(drop0 + w * n)
+    torch.cuda.synchronize()
+    s0 = time.perf_counter()
+    for k in range(steps):
+        one(drop0 + (2 + k) * n)
+    return (time.perf_counter() - s0) / steps, 4 * n, 4 * n
+
+
+# ------------------------------------------------------------------ engine arm
+def bench_link4x4(ctx, spec, args):
+    torch, hg, _lib = ctx["torch"], ctx["hg"], ctx["lib"]
+    from hermespy_gb300.train_estimator import workload_channel
+
+    drops, dev, stream, sp = spec.drops if args.drops is None else args.drops, ctx["dev"], ctx["stream"], ctx["sp"]
+    wf = hg.OFDMWaveform([hg.GridResource(1, prefix_ratio=72 / 1024, elements=[hg.GridElement(hg.ElementType.DATA, 600)])],
+                         [hg.SymbolSection(14, [0])], num_subcarriers=1024, modulation_order=64)
+    eng = hg.LinkEngine(wf, workload_channel(), 4, 4, spec.fs, "ideal", "lmmse", "snr", max_drops=drops, seed=SEED)
+    fh, fd = eng._fading.handle, wf._frame()
+    T, D = wf.samples_per_frame(), eng._fading.max_delay
+    p_host = eng.noise_power(ctx["rng"].uniform(0.0, 30.0, size=drops)).astype(np.float32)
+    p = torch.from_numpy(p_host).to(dev)
+    st = eng._fading.new_state(drops)
+    x = torch.empty((drops, 4, T), dtype=torch.complex64, device=dev)
+    y = torch.empty((drops, 4, T + D), dtype=torch.complex64, device=dev)
+    grid = torch.empty((drops, 4, 14, 600), dtype=torch.complex64, device=dev)
+    errors = torch.empty(drops, dtype=torch.int32, device=dev)
+    stages = ["fading_realize", "ofdm_modulate_bits", "fading_propagate", "ofdm_demodulate", "detect_ideal_lmmse"]
+
+    def step(d0, ev):
+        staged([
+            ("r", lambda: _lib.call("hpx_fading_realize", fh, SEED, d0, drops, _lib.ptr(st), sp)),
+            ("t", lambda: _lib.call("hpx_ofdm_modulate_bits", fd, SEED, d0, drops, 4, _lib.ptr(x), sp)),
+            ("p", lambda: _lib.call("hpx_fading_propagate", fh, _lib.ptr(st), drops, _lib.ptr(x), T, _lib.ptr(y),
+                                    _lib.ptr(p), SEED, d0, sp)),
+            ("d", lambda: _lib.call("hpx_ofdm_demodulate", fd, _lib.ptr(y), T + D, drops * 4, 600, _lib.ptr(grid), sp)),
+            ("e", lambda: _lib.call("hpx_detect_ideal", fh, _lib.ptr(st), fd, _lib.EQ_LMMSE, _lib.ptr(grid), 600,
+                                    _lib.ptr(p), SEED, d0, drops, _lib.ptr(errors), sp)),
+        ], ev, stream)
+
+    total_ms, stage_ms = ctx["timer"].run(step, stages, args.steps, args.warmup, ctx["drop_base"], drops)
+    ber = float(errors.sum().item()) / (drops * spec.bits_per_drop)
+    work = {"fading_realize": (eng._fading.state_bytes, "hbm"), "ofdm_modulate_bits": (8 * 4 * T, "hbm"),
+            "fading_propagate": (8 * (4 * T + 4 * (T + D)), "hbm"), "ofdm_demodulate": (8 * 4 * 14 * (1024 + 600), "hbm"),
+            "detect_ideal_lmmse": (8 * 4 * 14 * 600 + 4, "hbm")}
+    e2e_s, hb, db = e2e_time(torch, eng, p_host, dev, ctx["drop_base"] + (1 << 34), max(3, args.steps // 2))
+    return {"drops": drops, "total_ms": total_ms, "stage_ms": stage_ms, "work": work, "ber": ber,
+            "e2e_s": e2e_s, "h2d": hb, "d2h": db, "launches": 5, "extra": {}}
+
+
+def bench_estimators(ctx, spec, args):
+    torch, hg, _lib = ctx["torch"], ctx["hg"], ctx["lib"]
+    from hermespy_gb300.learned import WEIGHTS_DIR, CnnChannelEstimator, csi_error, nmse_db
+    from hermespy_gb300.train_estimator import pilot_waveform, workload_channel
+
+    drops, dev, stream, sp = spec.drops if args.drops is None else args.drops, ctx["dev"], ctx["stream"], ctx["sp"]
+    wf = pilot_waveform()
+    W, C = wf.words_per_frame, wf._layout()["num_columns"]
+    wpath = os.path.join(WEIGHTS_DIR, "cnn_4x4_1024.npz")
+    chunk = min(drops, 1024)
+    model = CnnChannelEstimator.load(wpath, max_batch=chunk)
+    eng = hg.LinkEngine(wf, workload_channel(), 4, 4, spec.fs, "learned", "lmmse", "snr", max_drops=drops, seed=SEED,
+                        model=model, also=("lmmse",))
+    fh, fd = eng._fading.handle, eng._frame
+    T, D = eng._T, eng._D
+    p_host = eng.noise_power(ctx["rng"].uniform(0.0, 30.0, size=drops)).astype(np.float32)
+    p = torch.from_numpy(p_host).to(dev)
+    errors = torch.empty(drops, dtype=torch.int32, device=dev)
+    st, x, y, grid, csi = eng._state, eng._x, eng._y, eng._grid, eng._csi
+    front = [
+        ("fading_realize", lambda d0: _lib.call("hpx_fading_realize", fh, SEED, d0, drops, _lib.ptr(st), sp)),
+        ("ofdm_modulate_bits", lambda d0: _lib.call("hpx_ofdm_modulate_bits", fd, SEED, d0, drops, 4, _lib.ptr(x), sp)),
+        ("fading_propagate", lambda d0: _lib.call("hpx_fading_propagate", fh, _lib.ptr(st), drops, _lib.ptr(x), T,
+                                                  _lib.ptr(y), _lib.ptr(p), SEED, d0, sp)),
+        ("ofdm_demodulate", lambda d0: _lib.call("hpx_ofdm_demodulate", fd, _lib.ptr(y), T + D, drops * 4, C,
+                                                 _lib.ptr(grid), sp)),
+    ]
+    detect = ("detect_csi_lmmse", lambda d0: _lib.call("hpx_detect_csi", fd, 4, 4, _lib.EQ_LMMSE, _lib.ptr(grid), C,
+                                                       _lib.ptr(csi), C, _lib.ptr(p), SEED, d0, drops,
+                                                       _lib.ptr(errors), sp))
+    ls_est = ("ls_estimate", lambda d0: _lib.call("hpx_ls_estimate_streams", eng._ls, _lib.ptr(grid), C, 4, drops,
+                                                  _lib.ptr(csi), sp))
+    paths = {
+        "learned": front + [ls_est, ("cnn_refine", lambda d0: model.refine(csi, stream)), detect],
+        "lmmse": front + [("detect_lmmse_fused", lambda d0: _lib.call("hpx_detect_lmmse", eng._lmmse, 4, _lib.EQ_LMMSE,
+                                                                      _lib.ptr(grid), C, _lib.ptr(p), SEED, d0, drops,
+                                                                      _lib.ptr(errors), sp))],
+        "ls": front + [ls_est, detect],
     }
+    HWp = W * C
+    n_pilot = 2 * 600
+    work = {"fading_realize": (eng._fading.state_bytes, "hbm"), "ofdm_modulate_bits": (8 * 4 * T, "hbm"),
+            "fading_propagate": (8 * (4 * T + 4 * (T + D)), "hbm"), "ofdm_demodulate": (8 * 4 * W * (1024 + C), "hbm"),
+            "ls_estimate": (8 * 4 * n_pilot + 8 * 16 * HWp, "hbm"),
+            "lmmse_estimate": (8 * 4 * n_pilot + 8 * 16 * HWp, "hbm"),
+            "cnn_refine": (2 * 9 * 32 * 32 * HWp * 6, "tensor"),
+            "detect_csi_lmmse": (8 * 4 * HWp + 8 * 16 * HWp, "hbm"),
+            "detect_lmmse_fused": (8 * 4 * HWp, "hbm")}
+    results = {}
+    for k, (name, calls) in enumerate(paths.items()):
+        def step(d0, ev, calls=calls):
+            staged([(s, (lambda f=f, d0=d0: f(d0))) for s, f in calls], ev, stream)
+
+        stages = [s for s, _ in calls]
+        total_ms, stage_ms = ctx["timer"].run(step, stages, args.steps, args.warmup,
+                                              ctx["drop_base"] + (k << 36), drops)
+        ber = float(errors.sum().item()) / (drops * spec.bits_per_drop)
+        results[name] = {"total_ms": total_ms, "stage_ms": stage_ms, "ber": ber}
+    # channel-estimate quality on a validation batch (untimed): NMSE over data elements
+    nval = min(drops, 1024)
+    pv = p[:nval].contiguous()
+    eng.receive(ctx["drop_base"] + (1 << 38), pv)
+    truth = torch.empty((nval, 4, 4, W, C), dtype=torch.complex64, device=dev)
+    _lib.call("hpx_fading_ideal_csi", fh, _lib.ptr(st), nval, fd, C, _lib.ptr(truth), sp)
+    nm = {}
+    for est in ("ls", "lmmse", "learned"):
+        e = eng.estimate(nval, pv, estimator=est)
+        nm[est] = round(nmse_db(*csi_error(fd, e, truth)), 3)
+    selected = "learned" if nm["learned"] <= nm["lmmse"] + 0.5 else "lmmse"
+    # e2e of the selected path through the public API
+    eng.estimator = selected
+    e2e_s, hb, db = e2e_time(torch, eng, p_host, dev, ctx["drop_base"] + (1 << 39), max(3, args.steps // 2))
+    comparison = {}
+    for name, r in results.items():
+        ms = r["total_ms"] / args.steps
+        comparison[name] = {"bits_per_s": drops * spec.bits_per_drop / (ms / 1e3), "ms_per_step": round(ms, 4),
+                            "ber": r["ber"], "nmse_db": nm[name]}
+    sel = results[selected]
+    launches = {"learned": 4 + 1 + 8 * ((drops + chunk - 1) // chunk) + 1, "lmmse": 5, "ls": 6}[selected]
+    extra = {"comparison": comparison, "estimator_policy": {
+        "selected": selected, "rule": "learned if its validation NMSE <= LMMSE NMSE + 0.5 dB, else LMMSE",
+        "validation_drops": nval}, "weights": os.path.relpath(wpath, ROOT)}
+    return {"drops": drops, "total_ms": sel["total_ms"], "stage_ms": sel["stage_ms"], "work": work,
+            "ber": sel["ber"], "e2e_s": e2e_s, "h2d": hb, "d2h": db, "launches": launches, "extra": extra}
+
+
+def bench_massive(ctx, spec, args):
+    torch, hg, _lib = ctx["torch"], ctx["hg"], ctx["lib"]
+    drops, dev, stream, sp = spec.drops if args.drops is None else args.drops, ctx["dev"], ctx["stream"], ctx["sp"]
+    N, Cu, CP, NRX, NTX = 4096, 3300, 288, 64, 16
+    wf = hg.OFDMWaveform([hg.GridResource(1, prefix_ratio=CP / N, elements=[hg.GridElement(hg.ElementType.DATA, Cu)])],
+                         [hg.SymbolSection(14, [0])], num_subcarriers=N, modulation_order=16)
+    k = np.arange(8)
+    ch = hg.MultipathFadingChannel(list(k / spec.fs), list(10 ** (-0.3 * k)), [0.0] * 8, doppler_frequency=50.0,
+                                   antenna_correlation=hg.ExponentialAntennaCorrelation(0.7, modes=("rx",)))
+    fad = ch.handle(NRX, NTX, spec.fs)
+    fh, fd = fad.handle, wf._frame()
+    T, D = wf.samples_per_frame(), fad.max_delay
+    # SNR relative to the channel's expected energy (simulation/rf/noise/level.py:258-259)
+    snr = ctx["rng"].uniform(0.0, 30.0, size=drops)
+    p_host = (10.0 ** (-snr / 10.0) * float(np.sum(10 ** (-0.3 * k)))).astype(np.float32)
+    p = torch.from_numpy(p_host).to(dev)
+    st = fad.new_state(drops)
+    x = torch.empty((drops, NTX, T), dtype=torch.complex64, device=dev)
+    y = torch.empty((drops, NRX, T + D), dtype=torch.complex64, device=dev)
+    grid = torch.empty((drops, NRX, 14, Cu), dtype=torch.complex64, device=dev)
+    errors = torch.empty(drops, dtype=torch.int32, device=dev)
+    n64 = torch.empty(drops, dtype=torch.int32, device=dev)
+    stages = ["fading_realize", "ofdm_modulate_bits", "fading_propagate", "ofdm_demodulate", "detect_massive"]
+
+    def step(d0, ev):
+        staged([
+            ("r", lambda: _lib.call("hpx_fading_realize", fh, SEED, d0, drops, _lib.ptr(st), sp)),
+            ("t", lambda: _lib.call("hpx_ofdm_modulate_bits", fd, SEED, d0, drops, NTX, _lib.ptr(x), sp)),
+            ("p", lambda: _lib.call("hpx_fading_propagate", fh, _lib.ptr(st), drops, _lib.ptr(x), T, _lib.ptr(y),
+                                    _lib.ptr(p), SEED, d0, sp)),
+            ("d", lambda: _lib.call("hpx_ofdm_demodulate", fd, _lib.ptr(y), T + D, drops * NRX, Cu, _lib.ptr(grid), sp)),
+            ("m", lambda: _lib.call("hpx_detect_massive", fh, _lib.ptr(st), fd, _lib.EQ_LMMSE, _lib.ptr(grid), Cu,
+                                    _lib.ptr(p), SEED, d0, drops, _lib.ptr(errors), _lib.ptr(n64), None, sp)),
+        ], ev, stream)
+
+    total_ms, stage_ms = ctx["timer"].run(step, stages, args.steps, args.warmup, ctx["drop_base"], drops)
+    ber = float(errors.sum().item()) / (drops * spec.bits_per_drop)
+    fp64_frac = float(n64.sum().item()) / (drops * 14 * Cu)
+    REs = 14 * Cu
+    work = {"fading_realize": (fad.state_bytes, "hbm"), "ofdm_modulate_bits": (8 * NTX * T, "hbm"),
+            "fading_propagate": (8 * (NTX * T + NRX * (T + D)), "hbm"),
+            "ofdm_demodulate": (8 * NRX * 14 * (N + Cu), "hbm"),
+            "detect_massive": (3 * 8 * NRX * NTX * NTX * REs, "tensor")}
+    # error of the split-precision solve against an FP64 solve of the same systems
+    # (one drop: the engine's grid and ideal CSI, float64 numpy normal equations)
+    one_p = p[:1].contiguous()
+    xe = torch.empty((1, NTX, REs), dtype=torch.complex64, device=dev)
+    e1 = torch.empty(1, dtype=torch.int32, device=dev)
+    _lib.call("hpx_detect_massive", fh, _lib.ptr(st), fd, _lib.EQ_LMMSE, _lib.ptr(grid), Cu, _lib.ptr(one_p), SEED,
+              ctx["drop_base"] + (args.warmup + args.steps - 1) * drops, 1, _lib.ptr(e1), None, _lib.ptr(xe), sp)
+    H = torch.empty((1, NRX, NTX, 14, Cu), dtype=torch.complex64, device=dev)
+    _lib.call("hpx_fading_ideal_csi", fh, _lib.ptr(st), 1, fd, Cu, _lib.ptr(H), sp)
+    torch.cuda.synchronize()
+    Hk = H[0].reshape(NRX, NTX, REs).permute(2, 0, 1).cpu().numpy().astype(np.complex128)
+    yk = grid[0].reshape(NRX, REs).T.cpu().numpy().astype(np.complex128)
+    s2 = float(p_host[0])
+    G = np.conj(np.swapaxes(Hk, 1, 2)) @ Hk + s2 * np.eye(NTX)[None]
+    bv = np.einsum("kri,kr->ki", np.conj(Hk), yk)
+    x64 = np.linalg.solve(G, bv[..., None])[..., 0]
+    xg = xe[0].cpu().numpy().T.astype(np.complex128)
+    rel = float(np.sqrt(np.sum(np.abs(xg - x64) ** 2) / np.sum(np.abs(x64) ** 2)))
+    # e2e: host noise powers in, host error counts out, around the same five calls
+    p_pin = torch.from_numpy(p_host).pin_memory()
+    out_pin = torch.empty(drops, dtype=torch.int32).pin_memory()
+
+    def e2e_one(d0):
+        pd = p_pin.to(dev, non_blocking=True)
+        _lib.call("hpx_fading_realize", fh, SEED, d0, drops, _lib.ptr(st), sp)
+        _lib.call("hpx_ofdm_modulate_bits", fd, SEED, d0, drops, NTX, _lib.ptr(x), sp)
+        _lib.call("hpx_fading_propagate", fh, _lib.ptr(st), drops, _lib.ptr(x), T, _lib.ptr(y), _lib.ptr(pd), SEED,
+                  d0, sp)
+        _lib.call("hpx_ofdm_demodulate", fd, _lib.ptr(y), T + D, drops * NRX, Cu, _lib.ptr(grid), sp)
+        _lib.call("hpx_detect_massive", fh, _lib.ptr(st), fd, _lib.EQ_LMMSE, _lib.ptr(grid), Cu, _lib.ptr(pd), SEED,
+                  d0, drops, _lib.ptr(errors), None, None, sp)
+        out_pin.copy_(errors, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    for w in range(2):
+        e2e_one(ctx["drop_base"] + (1 << 34) + w * drops)
+    steps = max(3, args.steps // 2)
+    s0 = time.perf_counter()
+    for kk in range(steps):
+        e2e_one(ctx["drop_base"] + (1 << 35) + kk * drops)
+    e2e_s = (time.perf_counter() - s0) / steps
+    extra = {"error_vs_fp64": {"rel_rms_equalized": rel, "drops": 1,
+                               "reference": "float64 normal-equation solve of the same H, y, s2"},
+             "fp64_pivot_fraction": fp64_frac}
+    return {"drops": drops, "total_ms": total_ms, "stage_ms": stage_ms, "work": work, "ber": ber,
+            "e2e_s": e2e_s, "h2d": 4 * drops, "d2h": 4 * drops, "launches": 5, "extra": extra}
 
 
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--drops", type=int, default=DROPS)
-    ap.add_argument("--cpu-rounds", type=int, default=4, help="rounds of per-core oracle drops for cpu_baseline")
+    ap.add_argument("--workload", default="estimators", choices=list(SPECS))
+    ap.add_argument("--drops", type=int, default=None, help="drops per step (default: the workload's)")
+    ap.add_argument("--cpu-rounds", type=int, default=2, help="rounds of per-core oracle drops for cpu_baseline")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    spec = SPECS[args.workload]
     if args.impl == "reference":
-        run_reference(args)
+        run_reference(args, spec)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -202,148 +557,52 @@ def main() -> None:
     import hermespy_gb300 as hg
     from hermespy_gb300 import _lib
     from hermespy_gb300.build import build
-    from tests.configs import mimo_channel
 
     build()
-    drops = args.drops
-    cfg = mimo_channel(FS)
-    wf = hg.OFDMWaveform([hg.GridResource(1, prefix_ratio=CP / N, elements=[hg.GridElement(hg.ElementType.DATA, U)])],
-                         [hg.SymbolSection(WORDS, [0])], num_subcarriers=N, modulation_order=ORDER)
-    seed = 20261203
-    ch = hg.MultipathFadingChannel(cfg.delays, cfg.power_profile, cfg.rice_factors, num_sinusoids=20,
-                                   doppler_frequency=500.0, seed=seed)
-    eng = hg.LinkEngine(wf, ch, NTX, NRX, FS, "ideal", "lmmse", "snr", max_drops=drops, seed=seed)
-    fh, fd = eng._fading.handle, wf._frame()
-    T, D = wf.samples_per_frame(), eng._fading.max_delay
-    stride = eng._fading.state_bytes
     dev = torch.device("cuda", local)
-    rng = np.random.default_rng(seed + rank)
-    snr_db = rng.uniform(0.0, 30.0, size=drops)
-    p_host = eng.noise_power(snr_db).astype(np.float32)
-    p_dev = torch.from_numpy(p_host).to(dev)
-    state = eng._fading.new_state(drops)
-    x = torch.empty((drops, NTX, T), dtype=torch.complex64, device=dev)
-    y = torch.empty((drops, NRX, T + D), dtype=torch.complex64, device=dev)
-    grid = torch.empty((drops, NRX, WORDS, U), dtype=torch.complex64, device=dev)
-    errors = torch.empty(drops, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
-    sp = stream.cuda_stream
-    stages = list(stage_bytes(T, D, stride))
-
-    def step(drop0: int, ev=None):
-        calls = [
-            ("hpx_fading_realize", fh, seed, drop0, drops, _lib.ptr(state), sp),
-            ("hpx_ofdm_modulate_bits", fd, seed, drop0, drops, NTX, _lib.ptr(x), sp),
-            ("hpx_fading_propagate", fh, _lib.ptr(state), drops, _lib.ptr(x), T, _lib.ptr(y), _lib.ptr(p_dev), seed,
-             drop0, sp),
-            ("hpx_ofdm_demodulate", fd, _lib.ptr(y), T + D, drops * NRX, U, _lib.ptr(grid), sp),
-            ("hpx_detect_ideal", fh, _lib.ptr(state), fd, _lib.EQ_LMMSE, _lib.ptr(grid), U, _lib.ptr(p_dev), seed,
-             drop0, drops, _lib.ptr(errors), sp),
-        ]
-        for i, c in enumerate(calls):
-            if ev is not None:
-                ev[i].record(stream)
-            _lib.call(*c)
-        if ev is not None:
-            ev[len(calls)].record(stream)
-
-    drop_base = rank * (1 << 40)
-    for w in range(args.warmup):
-        step(drop_base + w * drops)
-    torch.cuda.synchronize()
+    ctx = {"torch": torch, "hg": hg, "lib": _lib, "dev": dev, "stream": stream, "sp": stream.cuda_stream,
+           "rng": np.random.default_rng(SEED + rank), "drop_base": rank * (1 << 44), "timer": Timer(torch, stream)}
     if world > 1:
         torch.distributed.barrier()
-    events = [[torch.cuda.Event(enable_timing=True) for _ in range(len(stages) + 1)] for _ in range(args.steps)]
     with Clocks(local) as clk:
-        t0 = torch.cuda.Event(enable_timing=True)
-        t1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        t0.record(stream)
-        for k in range(args.steps):
-            step(drop_base + (args.warmup + k) * drops, events[k])
-        t1.record(stream)
-        torch.cuda.synchronize()
-    total_ms = t0.elapsed_time(t1)
-    stage_ms = {s: 0.0 for s in stages}
-    for ev in events:
-        for i, s in enumerate(stages):
-            stage_ms[s] += ev[i].elapsed_time(ev[i + 1])
-    # per-drop bit errors of the last step, for a BER sanity value
-    ber = float(errors.sum().item()) / (drops * BITS_PER_DROP)
-
-    # end to end: public API, host noise powers in (pinned), host error counts out
-    p_pin = torch.from_numpy(p_host).pin_memory()
-    out_pin = torch.empty(drops, dtype=torch.int32).pin_memory()
-
-    def e2e_step(drop0: int):
-        pd = p_pin.to(dev, non_blocking=True)
-        e = eng.run(drop0, pd)
-        out_pin.copy_(e, non_blocking=True)
-        torch.cuda.current_stream().synchronize()
-        return out_pin
-
-    for w in range(2):
-        e2e_step(drop_base + (1 << 30) + w * drops)
-    e2e_steps = max(3, args.steps // 2)
-    torch.cuda.synchronize()
-    s0 = time.perf_counter()
-    for k in range(e2e_steps):
-        e2e_step(drop_base + (1 << 31) + k * drops)
-    e2e_s = (time.perf_counter() - s0) / e2e_steps
-
+        res = {"estimators": bench_estimators, "link4x4": bench_link4x4, "massive": bench_massive}[spec.name](
+            ctx, spec, args)
+    total_ms, e2e_s = res["total_ms"], res["e2e_s"]
     if world > 1:
         import torch.distributed as dist
 
         tt = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         total_ms, e2e_s = float(tt[0]), float(tt[1])
+    drops = res["drops"]
     ms_per_step = total_ms / args.steps
-    value = world * drops * BITS_PER_DROP / (ms_per_step / 1e3)
-    e2e_value = world * drops * BITS_PER_DROP / e2e_s
+    value = world * drops * spec.bits_per_drop / (ms_per_step / 1e3)
+    e2e_value = world * drops * spec.bits_per_drop / e2e_s
 
     if rank == 0:
-        import json as _json
-
-        peaks = {"hbm_gbs": 6800.0, "src": "fallback"}
-        pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
-        if os.path.exists(pp):
-            with open(pp) as f:
-                m = _json.load(f)
-            peaks = {"hbm_gbs": float(m["hbm_gbs"]), "src": "measured"}
-        bpd = stage_bytes(T, D, stride)
-        stage_info = {}
-        for s in stages:
-            avg_ms = stage_ms[s] / args.steps
-            gbs = bpd[s] * drops / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0.0
-            stage_info[s] = {"ms": round(avg_ms, 4), "share": round(stage_ms[s] / max(sum(stage_ms.values()), 1e-9), 4),
-                             "algorithmic_bytes": bpd[s] * drops, "achieved_gbs": round(gbs, 1),
-                             "frac_hbm": round(gbs / peaks["hbm_gbs"], 4)}
-        dom = max(stages, key=lambda s: stage_ms[s])
-        traffic = None
-        tp = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tp):
-            with open(tp) as f:
-                traffic = _json.load(f).get(dom)
-        roof = {"kernel": dom, "bound": "hbm", "achieved": stage_info[dom]["achieved_gbs"], "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": stage_info[dom]["frac_hbm"], "traffic": traffic,
-                "peak_source": peaks["src"]}
-        cpu_value, cpu_drops, cpu_s = time_cpu(pool, cores, args.cpu_rounds)
+        pk = peaks()
+        info = stage_report(res["stage_ms"], args.steps, res["work"], drops, pk)
+        roof = roofline_of(info, pk)
+        cpu_value, cpu_drops, cpu_s = time_cpu(pool, cores, spec, args.cpu_rounds if spec.name != "massive" else 1)
         pool.close()
         line = {
             "metric": METRIC, "value": value, "unit": "bits/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64", "data": "synthetic (Philox draws)",
-            "config": dict(CONFIG, drops_per_step=drops, parallelism=f"drop-sharded x{world}"),
-            "drops_per_s": world * drops / (ms_per_step / 1e3), "ber": ber,
-            "e2e": {"value": e2e_value, "unit": "bits/s", "h2d_bytes_per_step": 4 * drops,
-                    "d2h_bytes_per_step": 4 * drops},
-            "gpu_launches": len(stages) * args.steps,
-            "roofline": roof, "stages": stage_info,
-            "cpu_baseline": {"value": cpu_value, "unit": "bits/s", "cores": cores, "kind": "port",
-                             "sample": f"{cpu_drops} drops of the workload in {cpu_s:.1f} s (float64 numpy "
-                                       f"restatement of the reference's drop, one process per core)"},
+            "config": dict(spec.config, drops_per_step=drops, bits_per_drop=spec.bits_per_drop,
+                           l2="every buffer of a step exceeds the 129 MB L2; no flush needed",
+                           parallelism=f"drop-sharded x{world}"),
+            "drops_per_s": world * drops / (ms_per_step / 1e3), "ber": res["ber"],
+            "e2e": {"value": e2e_value, "unit": "bits/s", "h2d_bytes_per_step": res["h2d"],
+                    "d2h_bytes_per_step": res["d2h"]},
+            "gpu_launches": res["launches"] * args.steps,
+            "roofline": roof, "stages": info,
+            "cpu_baseline": {"value": cpu_value, "unit": "bits/s", "cores": cpu_workers(spec, cores), "kind": "port",
+                             "sample": cpu_sample_text(spec, cpu_drops, cpu_s)},
             "clocks": clk.summary(),
         }
+        line.update(res["extra"])
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -130,6 +130,14 @@ _SIGNATURES = {
     "hpx_cnn_train_step": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, ctypes.c_float, c_void_p, c_void_p],
     "hpx_detect_massive": [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64, c_int64,
                            c_int32, c_void_p, c_void_p, c_void_p, c_void_p],
+    "hpx_campaign_create": [c_int32, c_void_p, c_double, c_double, c_int32, c_int64, c_int32, c_double, c_void_p],
+    "hpx_campaign_destroy": [c_void_p],
+    "hpx_campaign_reset": [c_void_p],
+    "hpx_campaign_run": [c_void_p, c_void_p, c_uint64, c_int64, c_int32, c_int32, c_int32, c_void_p, c_void_p,
+                         c_void_p],
+    "hpx_campaign_results": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+    "hpx_detect_lmmse": [c_void_p, c_int32, c_int32, c_void_p, c_int32, c_void_p, c_uint64, c_int64, c_int32, c_void_p,
+                         c_void_p],
     "hpx_detect_csi": [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64,
                        c_int64, c_int32, c_void_p, c_void_p],
 }

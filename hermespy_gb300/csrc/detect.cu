@@ -1,6 +1,7 @@
 // Channel estimation (LS), per-element equalization (ZF / LMMSE) and the fused
 // receivers that end in bit-error counts.
 #include "fading_dev.cuh"
+#include "lmmse_dev.cuh"
 
 struct hpx_ls {
   const hpx_frame* frame;
@@ -294,6 +295,57 @@ __global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_csi(
   block_count(local, errors + b);
 }
 
+// Fused receiver with the tap-domain LMMSE channel estimate, one block per drop:
+// the drop's tap gains of every pair and word are estimated into shared memory
+// (lmmse_drop_taps) and every data element forms its channel from them, so the CSI
+// grid never reaches HBM. Same estimate, equalizer, demap and count as
+// hpx_lmmse_estimate + hpx_detect_csi.
+template <int NRX, int NTX>
+__global__ void __launch_bounds__(256) k_detect_lmmse(LmmseView e, int C, int m, int num_data,
+                                                      const int32_t* __restrict__ data_column,
+                                                      const int32_t* __restrict__ data_word,
+                                                      const int32_t* __restrict__ bins, const float2* __restrict__ tw,
+                                                      const __grid_constant__ QamDemapTable qt, int mode,
+                                                      const float2* __restrict__ grid, int gcols,
+                                                      const float* __restrict__ nv, uint64_t seed, int64_t drop0,
+                                                      uint32_t* __restrict__ errors) {
+  constexpr int NP = NRX * NTX;
+  extern __shared__ float4 smem4[];
+  const int b = blockIdx.x;
+  const int W = e.W, U = e.U;
+  float2* gt = reinterpret_cast<float2*>(smem4);
+  float2* gls = gt + (size_t)W * U * NP;
+  float* cw = reinterpret_cast<float*>(gls + NP * e.np * U);
+  int* ds = reinterpret_cast<int*>(cw + (size_t)e.ntx * U * W * e.np);
+  uint32_t* bitsm = reinterpret_cast<uint32_t*>(ds + U + 4);
+  const int BW = ((num_data * m) >> 5) + 9;  // staged words of one stream's whole frame
+  stage_bits(bitsm, BW, NTX, seed, drop0 + b, 0, num_data, m);
+  const float s2 = nv ? nv[b] : 0.0f;
+  lmmse_drop_taps<NP>(e, b, NRX, grid, gcols, s2, gt, gls, cw, ds);  // ends with __syncthreads
+  const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
+  unsigned int local = 0;
+  for (int k = threadIdx.x; k < num_data; k += blockDim.x) {
+    const int c = data_column[k], w = data_word[k];
+    float2 hp[NP];
+    lmmse_response<NP>(gt + (size_t)w * U * NP, ds, U, e.N, bins[c], tw, hp);
+    float2 H[NRX][NTX], y[NRX], x[NTX];
+#pragma unroll
+    for (int r = 0; r < NRX; ++r) {
+      y[r] = grid[(((int64_t)b * NRX + r) * W + w) * gcols + c];
+#pragma unroll
+      for (int t = 0; t < NTX; ++t) H[r][t] = hp[r * NTX + t];
+    }
+    equalize_one<NRX, NTX>(mode, H, y, s2, x);
+#pragma unroll
+    for (int t = 0; t < NTX; ++t) {
+      const uint32_t rx_v = t < out_streams ? qam_decide(qt, x[t]) : 0u;
+      const uint32_t tx_v = extract_bits_msb(bitsm + t * BW, (int64_t)k * m, m);
+      local += __popc(rx_v ^ tx_v);
+    }
+  }
+  block_count(local, errors + b);
+}
+
 // Fused SISO LS receiver, one block per (word, drop).
 __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, const int32_t* __restrict__ data_offset,
                                                         const int32_t* __restrict__ num_data_word,
@@ -341,24 +393,39 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
   block_count(local, errors + b);
 }
 
-// rows = streams * W * C (the stacked tables); blockIdx.y = received grid (drop, rx).
-__global__ void k_ls_estimate(int W, int rows, const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
-                              const float* __restrict__ weights, const int32_t* __restrict__ ref_word,
-                              const int32_t* __restrict__ ref_column, const float2* __restrict__ pilots,
-                              const float2* __restrict__ grid, int gcols, float2* __restrict__ est) {
-  const int b = blockIdx.y;
-  const float2* gb = grid + (int64_t)b * W * gcols;
+// rows = streams * W * C (the stacked tables); blockIdx.y covers LS_ITEMS received
+// grids (drop, rx), which share every table row a thread loads.
+constexpr int LS_ITEMS = 8;
+__global__ void k_ls_estimate(int W, int rows, int items, const int32_t* __restrict__ indptr,
+                              const int32_t* __restrict__ indices, const float* __restrict__ weights,
+                              const int32_t* __restrict__ ref_word, const int32_t* __restrict__ ref_column,
+                              const float2* __restrict__ pilots, const float2* __restrict__ grid, int gcols,
+                              float2* __restrict__ est) {
+  const int i0 = blockIdx.y * LS_ITEMS;
+  const int n = min(LS_ITEMS, items - i0);
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < rows; row += gridDim.x * blockDim.x) {
-    float2 h = make_float2(0.f, 0.f);
+    float2 h[LS_ITEMS];
+#pragma unroll
+    for (int i = 0; i < LS_ITEMS; ++i) h[i] = make_float2(0.f, 0.f);
     for (int e = indptr[row]; e < indptr[row + 1]; ++e) {
       const int p = indices[e];
-      const float2 yp = gb[ref_word[p] * gcols + ref_column[p]];
+      const float wgt = weights[e];
       const float2 xp = pilots[p];
       const float den = xp.x * xp.x + xp.y * xp.y;
-      const float2 ls = make_float2((yp.x * xp.x + yp.y * xp.y) / den, (yp.y * xp.x - yp.x * xp.y) / den);
-      h = cadd(h, cscale(ls, weights[e]));
+      const int64_t at = (int64_t)ref_word[p] * gcols + ref_column[p];
+#pragma unroll
+      for (int i = 0; i < LS_ITEMS; ++i) {
+        if (i >= n) break;
+        const float2 yp = grid[(int64_t)(i0 + i) * W * gcols + at];
+        const float2 ls = make_float2((yp.x * xp.x + yp.y * xp.y) / den, (yp.y * xp.x - yp.x * xp.y) / den);
+        h[i] = cadd(h[i], cscale(ls, wgt));
+      }
     }
-    est[(int64_t)b * rows + row] = h;
+#pragma unroll
+    for (int i = 0; i < LS_ITEMS; ++i) {
+      if (i >= n) break;
+      est[(int64_t)(i0 + i) * rows + row] = h[i];
+    }
   }
 }
 
@@ -529,8 +596,8 @@ hpx_status hpx_ls_estimate(const hpx_ls* ls, const hpx_cf32* grid, int32_t gcols
   if (B > 65535) return hpx_fail(HPX_ERR_ARG, "ls_estimate: batch too large");
   if (ls->ntx != 1) return hpx_fail(HPX_ERR_ARG, "ls_estimate: table of %d streams (use hpx_ls_estimate_streams)", ls->ntx);
   const int W = ls->frame->info.num_words;
-  dim3 grid_dim((W * ls->C + 255) / 256, B);
-  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, W * ls->C, ls->d_indptr, ls->d_indices, ls->d_weights,
+  dim3 grid_dim((W * ls->C + 255) / 256, (B + LS_ITEMS - 1) / LS_ITEMS);
+  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, W * ls->C, B, ls->d_indptr, ls->d_indices, ls->d_weights,
                                                          ls->d_ref_word, ls->d_ref_column, ls->frame->d_pilots,
                                                          reinterpret_cast<const float2*>(grid), gcols,
                                                          reinterpret_cast<float2*>(est));
@@ -547,8 +614,8 @@ hpx_status hpx_ls_estimate_streams(const hpx_ls* ls, const hpx_cf32* grid, int32
   if ((int64_t)B * nrx > 65535) return hpx_fail(HPX_ERR_ARG, "ls_estimate: batch too large");
   const int W = ls->frame->info.num_words;
   const int rows = ls->ntx * W * ls->C;
-  dim3 grid_dim((rows + 255) / 256, B * nrx);
-  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, rows, ls->d_indptr, ls->d_indices, ls->d_weights,
+  dim3 grid_dim((rows + 255) / 256, (B * nrx + LS_ITEMS - 1) / LS_ITEMS);
+  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, rows, B * nrx, ls->d_indptr, ls->d_indices, ls->d_weights,
                                                          ls->d_ref_word, ls->d_ref_column, ls->frame->d_pilots,
                                                          reinterpret_cast<const float2*>(grid), gcols,
                                                          reinterpret_cast<float2*>(est));
@@ -618,6 +685,44 @@ hpx_status hpx_detect_csi(const hpx_frame* fr, int32_t nrx, int32_t ntx, int32_t
     case 8: return detect_csi_tx<8>(ntx, fr, mode, grid, gcols, csi, ccols, nv, seed, drop0, B, errors, s);
     default: return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_csi: %d receive streams not supported (1, 2, 4, 8)", nrx);
   }
+}
+
+hpx_status hpx_detect_lmmse(const hpx_lmmse* lm, int32_t nrx, int32_t mode, const hpx_cf32* grid, int32_t gcols,
+                            const float* nv, uint64_t seed, int64_t drop0, int32_t B, uint32_t* errors,
+                            void* stream) {
+  if (!lm || !grid || !errors) return hpx_fail(HPX_ERR_ARG, "detect_lmmse: null argument");
+  if (mode != HPX_EQ_ZF && mode != HPX_EQ_LMMSE) return hpx_fail(HPX_ERR_ARG, "detect_lmmse: unknown mode");
+  if ((mode == HPX_EQ_LMMSE) && !nv) return hpx_fail(HPX_ERR_ARG, "detect_lmmse: LMMSE needs noise variances");
+  if (B < 0 || drop0 < 0) return hpx_fail(HPX_ERR_ARG, "detect_lmmse: bad drop range");
+  const hpx_frame* fr = lm->frame;
+  if (gcols < fr->info.num_columns) return hpx_fail(HPX_ERR_SHAPE, "detect_lmmse: grid too narrow");
+  if (B == 0) return HPX_OK;
+  if (B > 65535) return hpx_fail(HPX_ERR_ARG, "detect_lmmse: batch above 65535 drops per call");
+  const int ntx = lm->ntx, m = fr->info.bits_per_symbol, nd = fr->info.num_data;
+  if (!((nrx == 1 && ntx == 1) || (nrx == 2 && ntx == 2) || (nrx == 4 && ntx == 4) || (nrx == 4 && ntx == 2) ||
+        (nrx == 2 && ntx == 1) || (nrx == 4 && ntx == 1)))
+    return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_lmmse: %dx%d antennas not supported", nrx, ntx);
+  QamDemapTable qt;
+  HPX_TRY(qam_demap_table(fr->info.modulation_order, &qt));
+  const size_t smem = lmmse_taps_smem(lm->W, lm->U, lm->np, ntx, nrx * ntx) + 16 +
+                      (size_t)ntx * ((((size_t)nd * m) >> 5) + 9) * 4;
+  if (smem > 220 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_lmmse: frame needs %zu bytes of shared memory", smem);
+  cudaStream_t s = as_stream(stream);
+  HPX_CUDA(cudaMemsetAsync(errors, 0, sizeof(uint32_t) * B, s));
+  const LmmseView v = lmmse_view(lm);
+  auto launch = [&](auto kern) -> hpx_status {
+    HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<B, 256, smem, s>>>(v, fr->info.num_columns, m, nd, fr->d_data_column, fr->d_data_word, fr->d_bins,
+                              fr->d_twiddle, qt, mode, reinterpret_cast<const float2*>(grid), gcols, nv, seed, drop0,
+                              errors);
+    HPX_LAUNCHED("detect_lmmse");
+    return HPX_OK;
+  };
+  if (nrx == 1) return ntx == 1 ? launch(k_detect_lmmse<1, 1>) : hpx_fail(HPX_ERR_UNSUPPORTED, "detect_lmmse");
+  if (nrx == 2) return ntx == 1 ? launch(k_detect_lmmse<2, 1>) : launch(k_detect_lmmse<2, 2>);
+  if (ntx == 1) return launch(k_detect_lmmse<4, 1>);
+  if (ntx == 2) return launch(k_detect_lmmse<4, 2>);
+  return launch(k_detect_lmmse<4, 4>);
 }
 
 hpx_status hpx_detect_ls(const hpx_ls* ls, int32_t mode, const hpx_cf32* grid, int32_t gcols, const float* nv,

@@ -23,26 +23,12 @@
 #include <complex>
 #include <vector>
 
-#include "hpx_internal.cuh"
+#include "lmmse_dev.cuh"
 
-struct hpx_lmmse {
-  const hpx_frame* frame = nullptr;
-  int C = 0, ntx = 0, U = 0, P = 0, N = 0, W = 0;
-  int32_t* d_delay = nullptr;     // [U] distinct tap delays (samples)
-  int32_t* d_pw_word = nullptr;   // [ntx][P] word of pilot word p (-1: none)
-  int32_t* d_pw_count = nullptr;  // [ntx][P] pilots in that word
-  int32_t* d_pw_off = nullptr;    // [ntx][P] offset into d_pcol / d_G (in pilots)
-  int32_t* d_pcol = nullptr;      // [total pilots] grid column
-  float2* d_G = nullptr;          // per pilot word [U][count] weighted-LS rows
-  float* d_E = nullptr;           // [ntx][P][U] diag((A^H A)^-1)
-  float* d_R = nullptr;           // [U][P][P]
-  float* d_r = nullptr;           // [U][W][P]
-  int32_t* d_np = nullptr;        // [ntx] pilot words per stream
-};
+
 
 namespace {
 
-constexpr int kMaxPilotWords = 8;
 constexpr int kMaxTaps = 64;
 
 using cd = std::complex<double>;
@@ -189,6 +175,36 @@ __global__ void k_tap_lmmse(int W, int N, int U, int P, int ntx, int nrx, int cc
     float2 acc = make_float2(0.f, 0.f);
     for (int u = 0; u < U; ++u) cfma(acc, g[u], __ldg(tw + ((bin * ds[u]) & (N - 1))));
     out[q] = acc;
+  }
+}
+
+// The same estimator with one block per drop for NP = Nrx * Ntx antenna pairs: the
+// tap gains of all pairs stay in shared memory ([word][tap][pair]), so each twiddle
+// of the final tap DFT is gathered once and used by every pair (broadcast 16-byte
+// loads of two pairs' gains, NP accumulators per grid element in registers).
+template <int NP>
+__global__ void __launch_bounds__(256) k_tap_lmmse_drop(LmmseView e, int nrx, int ccols,
+                                                        const int32_t* __restrict__ bins,
+                                                        const float2* __restrict__ tw,
+                                                        const float2* __restrict__ grid, int gcols,
+                                                        const float* __restrict__ noise_power,
+                                                        float2* __restrict__ est) {
+  extern __shared__ float4 smem4[];
+  const int b = blockIdx.x;
+  const int W = e.W, U = e.U;
+  float2* gt = reinterpret_cast<float2*>(smem4);
+  float2* gls = gt + (size_t)W * U * NP;
+  float* cw = reinterpret_cast<float*>(gls + NP * e.np * U);
+  int* ds = reinterpret_cast<int*>(cw + (size_t)e.ntx * U * W * e.np);
+  lmmse_drop_taps<NP>(e, b, nrx, grid, gcols, noise_power ? noise_power[b] : 0.0f, gt, gls, cw, ds);
+  const int64_t plane = (int64_t)W * ccols;
+  float2* out = est + (int64_t)b * NP * plane;
+  for (int q = threadIdx.x; q < W * ccols; q += blockDim.x) {
+    const int w = q / ccols, c = q - w * ccols;
+    float2 acc[NP];
+    lmmse_response<NP>(gt + (size_t)w * U * NP, ds, U, e.N, bins[c], tw, acc);
+#pragma unroll
+    for (int i = 0; i < NP; ++i) out[i * plane + (int64_t)w * ccols + c] = acc[i];
   }
 }
 
@@ -364,6 +380,7 @@ hpx_status hpx_lmmse_create(const hpx_frame* frame, const hpx_fading* fading, in
   e->P = P;
   e->N = N;
   e->W = W;
+  e->np = np;
   std::vector<int32_t> dl(delays.begin(), delays.end());
   cudaError_t err;
   if ((err = upload(&e->d_delay, dl)) != cudaSuccess || (err = upload(&e->d_pw_word, pw_word)) != cudaSuccess ||
@@ -391,6 +408,29 @@ hpx_status hpx_lmmse_estimate(const hpx_lmmse* e, const hpx_cf32* grid, int32_t 
   if (B == 0) return HPX_OK;
   if (B > 65535) return hpx_fail(HPX_ERR_ARG, "lmmse_estimate: batch above 65535 drops per call");
   if (nrx * e->ntx > 65535) return hpx_fail(HPX_ERR_ARG, "lmmse_estimate: too many antenna pairs");
+  const int NPAIRS = nrx * e->ntx;
+  const size_t smem_drop = lmmse_taps_smem(e->W, e->U, e->np, e->ntx, NPAIRS);
+  const bool per_drop = (NPAIRS == 1 || NPAIRS == 2 || NPAIRS == 4 || NPAIRS == 8 || NPAIRS == 16) &&
+                        smem_drop <= 200 * 1024;
+  if (per_drop) {
+    const LmmseView v = lmmse_view(e);
+    auto launch = [&](auto kern) -> hpx_status {
+      if (smem_drop > 48 * 1024)
+        HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_drop));
+      kern<<<B, 256, smem_drop, as_stream(stream)>>>(v, nrx, e->C, e->frame->d_bins, e->frame->d_twiddle,
+                                                     reinterpret_cast<const float2*>(grid), gcols, noise_power,
+                                                     reinterpret_cast<float2*>(est));
+      HPX_LAUNCHED("tap_lmmse");
+      return HPX_OK;
+    };
+    switch (NPAIRS) {
+      case 1: return launch(k_tap_lmmse_drop<1>);
+      case 2: return launch(k_tap_lmmse_drop<2>);
+      case 4: return launch(k_tap_lmmse_drop<4>);
+      case 8: return launch(k_tap_lmmse_drop<8>);
+      default: return launch(k_tap_lmmse_drop<16>);
+    }
+  }
   const size_t smem = (size_t)(e->P * e->U + e->W * e->U) * sizeof(float2) +
                       (size_t)e->U * e->W * e->P * sizeof(float) + (size_t)e->U * sizeof(int) + 16;
   if (smem > 200 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "lmmse_estimate: frame too long for one block");

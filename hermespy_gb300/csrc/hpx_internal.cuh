@@ -181,6 +181,25 @@ struct hpx_fading {
   size_t off_w, off_p0, off_spatial, stride;
 };
 
+// Tap-domain LMMSE channel estimator tables (estimate.cu builds them, the fused
+// receiver in detect.cu reads them).
+constexpr int kMaxPilotWords = 8;
+struct hpx_lmmse {
+  const hpx_frame* frame = nullptr;
+  int C = 0, ntx = 0, U = 0, P = 0, N = 0, W = 0;
+  int np = 0;  // pilot words per stream (the same for every stream)
+  int32_t* d_delay = nullptr;     // [U] distinct tap delays (samples)
+  int32_t* d_pw_word = nullptr;   // [ntx][P] word of pilot word p (-1: none)
+  int32_t* d_pw_count = nullptr;  // [ntx][P] pilots in that word
+  int32_t* d_pw_off = nullptr;    // [ntx][P] offset into d_pcol / d_G (in pilots)
+  int32_t* d_pcol = nullptr;      // [total pilots] grid column
+  float2* d_G = nullptr;          // per pilot word [U][count] weighted-LS rows
+  float* d_E = nullptr;           // [ntx][P][U] diag((A^H A)^-1)
+  float* d_R = nullptr;           // [U][P][P]
+  float* d_r = nullptr;           // [U][W][P]
+  int32_t* d_np = nullptr;        // [ntx] pilot words per stream
+};
+
 // Per-drop realization state, read by the kernels.
 struct FadingView {
   const unsigned char* base;

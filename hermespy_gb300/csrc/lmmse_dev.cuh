@@ -1,0 +1,134 @@
+// Device side of the tap-domain LMMSE channel estimator, shared by the estimate
+// kernel (CSI grid output) and the fused LMMSE receiver.
+#pragma once
+
+#include "hpx_internal.cuh"
+
+struct LmmseView {
+  int W, N, U, P, ntx, np;
+  const int32_t* delay;
+  const int32_t* pw_word;
+  const int32_t* pw_count;
+  const int32_t* pw_off;
+  const int32_t* pcol;
+  const float2* G;
+  const float* E;
+  const float* R;
+  const float* rw;
+  const int32_t* np_stream;
+};
+
+static inline LmmseView lmmse_view(const hpx_lmmse* e) {
+  return LmmseView{e->W, e->N, e->U, e->P, e->ntx, e->np, e->d_delay, e->d_pw_word, e->d_pw_count, e->d_pw_off,
+                   e->d_pcol, e->d_G, e->d_E, e->d_R, e->d_r, e->d_np};
+}
+
+// Shared memory of lmmse_drop_taps: gt [W][U][NP] float2, gls [NP][np][U] float2,
+// cw [ntx][U][W][np] floats, ds [U] ints (np = pilot words per stream).
+__host__ __device__ inline size_t lmmse_taps_smem(int W, int U, int np, int ntx, int NP) {
+  return (size_t)W * U * NP * 8 + (size_t)NP * np * U * 8 + (size_t)ntx * U * W * np * 4 + (size_t)U * 4 + 16;
+}
+
+// Tap gains of every antenna pair and word of drop b into gt[W][U][NP] (pair =
+// rx * ntx + tx), all threads of the block:
+//   1. weighted LS of the tap gains on each pilot word (one warp per dot product),
+//   2. per stream and tap the LMMSE weights over the words (np x np Cholesky),
+//   3. gt[w][u][pair] = sum_p weight * LS gain.
+// ds receives the tap delays. Ends with __syncthreads.
+template <int NP>
+__device__ __forceinline__ void lmmse_drop_taps(const LmmseView& e, int b, int nrx, const float2* __restrict__ grid,
+                                                int gcols, float s2, float2* gt, float2* gls, float* cw, int* ds) {
+  const int W = e.W, U = e.U, P = e.P, ntx = e.ntx;
+  const int np = e.np;  // every stream has the same pilot words (checked at create time)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int u = threadIdx.x; u < U; u += blockDim.x) ds[u] = e.delay[u];
+  for (int q = warp; q < NP * np * U; q += nwarps) {
+    const int pair = q / (np * U), rem = q - pair * np * U, p = rem / U, u = rem - p * U;
+    const int t = pair % ntx, r = pair / ntx;
+    const int word = e.pw_word[t * P + p], cnt = e.pw_count[t * P + p], off = e.pw_off[t * P + p];
+    const float2* grow = e.G + (int64_t)off * U + (int64_t)u * cnt;
+    const float2* yw = grid + (((int64_t)b * nrx + r) * W + word) * gcols;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int k = lane; k < cnt; k += 32) cfma(acc, grow[k], yw[e.pcol[off + k]]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+    }
+    if (lane == 0) gls[(pair * np + p) * U + u] = acc;
+  }
+  for (int q = threadIdx.x; q < ntx * U; q += blockDim.x) {
+    const int t = q / U, u = q - t * U;
+    float m[kMaxPilotWords][kMaxPilotWords];
+    for (int i = 0; i < np; ++i)
+      for (int j = 0; j < np; ++j)
+        m[i][j] = e.R[((size_t)u * P + i) * P + j] + (i == j ? s2 * e.E[(t * P + i) * U + u] : 0.f);
+    bool ok = true;
+    for (int j = 0; j < np && ok; ++j) {
+      float d = m[j][j];
+      for (int k = 0; k < j; ++k) d -= m[j][k] * m[j][k];
+      if (!(d > 0.f)) {  // no signal power on this tap: its gains stay zero
+        ok = false;
+        break;
+      }
+      const float inv = rsqrtf(d);
+      m[j][j] = inv;
+      for (int i = j + 1; i < np; ++i) {
+        float sm = m[i][j];
+        for (int k = 0; k < j; ++k) sm -= m[i][k] * m[j][k];
+        m[i][j] = sm * inv;
+      }
+    }
+    for (int w = 0; w < W; ++w) {
+      float z[kMaxPilotWords];
+      for (int i = 0; i < np; ++i) {
+        float sm = ok ? e.rw[((size_t)u * W + w) * P + i] : 0.f;
+        for (int k = 0; k < i; ++k) sm -= m[i][k] * z[k];
+        z[i] = ok ? sm * m[i][i] : 0.f;
+      }
+      for (int i = np - 1; i >= 0; --i) {
+        float sm = z[i];
+        for (int k = i + 1; k < np; ++k) sm -= m[k][i] * z[k];
+        z[i] = ok ? sm * m[i][i] : 0.f;
+      }
+      for (int i = 0; i < np; ++i) cw[(((size_t)t * U + u) * W + w) * np + i] = z[i];
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < W * U * NP; q += blockDim.x) {
+    const int w = q / (U * NP), rem = q - w * U * NP, u = rem / NP, pair = rem - u * NP;
+    const int t = pair % ntx;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int p = 0; p < np; ++p) {
+      const float c = cw[(((size_t)t * U + u) * W + w) * np + p];
+      const float2 g = gls[(pair * np + p) * U + u];
+      acc.x = fmaf(c, g.x, acc.x);
+      acc.y = fmaf(c, g.y, acc.y);
+    }
+    gt[q] = acc;
+  }
+  __syncthreads();
+}
+
+// Channel of all NP pairs at one element: H[pair] = sum_u gt_w[u][pair] tw[bin d_u],
+// each twiddle gathered once (gt_w: the word's [U][NP] gains in shared memory).
+template <int NP>
+__device__ __forceinline__ void lmmse_response(const float2* gt_w, const int* ds, int U, int N, int bin,
+                                               const float2* __restrict__ tw, float2 (&acc)[NP]) {
+#pragma unroll
+  for (int i = 0; i < NP; ++i) acc[i] = make_float2(0.f, 0.f);
+  for (int u = 0; u < U; ++u) {
+    const float2 t = __ldg(tw + ((bin * ds[u]) & (N - 1)));
+    if (NP == 1) {
+      cfma(acc[0], gt_w[u], t);
+    } else {
+      const float4* g4 = reinterpret_cast<const float4*>(gt_w + u * NP);
+#pragma unroll
+      for (int i = 0; i < NP / 2; ++i) {
+        const float4 v = g4[i];
+        cfma(acc[2 * i], make_float2(v.x, v.y), t);
+        cfma(acc[2 * i + 1], make_float2(v.z, v.w), t);
+      }
+    }
+  }
+}

@@ -120,15 +120,16 @@ __device__ bool solve_fp64(double2* L, const double2* b, double reg, float2* x) 
 }
 
 // Per-warp shared memory: [P_hi | P_lo] (reused for the FP64 Gram and matched
-// filter of the two elements once the FP32 ones are formed), Y, G[2][16][16],
-// b[2][16], x[2][16], g[2], column[2].
+// filter of the two elements once the FP32 ones are formed), Y, G[2][16][17] (rows
+// padded: a half-warp reading one row per lane hits distinct banks), b[2][16],
+// x[2][16], Cholesky column broadcast [2][16], g[2], column[2].
 template <int NRX>
 struct MassiveSmem {
   static constexpr int KR = 2 * NRX;        // stacked real rows
   static constexpr int TILE = KR * 16 * 2;  // bytes of one [KR][16] bf16 tile
   static constexpr int FP64 = 2 * MT * MT * 16 + 2 * MT * 16;
   static constexpr int UNION = 2 * TILE > FP64 ? 2 * TILE : FP64;
-  static constexpr int WARP_BYTES = UNION + TILE + 2 * MT * MT * 8 + 2 * MT * 8 + 2 * MT * 8 + 2 * 8 + 2 * 8;
+  static constexpr int WARP_BYTES = UNION + TILE + 2 * MT * (MT + 1) * 8 + 2 * MT * 8 + 2 * MT * 8 + 2 * MT * 8 + 2 * 8 + 2 * 8;
 };
 
 // Fused ideal-CSI massive-MIMO receiver, one block (4 warps) per (word, drop).
@@ -158,10 +159,12 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
   unsigned char* Phi = my;
   unsigned char* Plo = my + SM::TILE;
   unsigned char* Yt = my + SM::UNION;
-  float2* Gs = reinterpret_cast<float2*>(my + SM::UNION + SM::TILE);  // [2][16][16]
-  float2* bs = Gs + 2 * MT * MT;                              // [2][16]
+  constexpr int GS = MT + 1;                                  // padded Gram row
+  float2* Gs = reinterpret_cast<float2*>(my + SM::UNION + SM::TILE);  // [2][16][17]
+  float2* bs = Gs + 2 * MT * GS;                              // [2][16]
   float2* xs = bs + 2 * MT;                                   // [2][16] FP64-path results
-  float2* gsave = xs + 2 * MT;                                // [2] tap response of each element
+  float2* colb = xs + 2 * MT;                                 // [2][16] column of L being broadcast
+  float2* gsave = colb + 2 * MT;                              // [2] tap response of each element
   int* csave = reinterpret_cast<int*>(gsave + 2);             // [2] grid column of each element
 
   const int64_t k0 = data_offset[w];
@@ -195,20 +198,47 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
   const int half = lane >> 4, row = lane & 15;
   unsigned int local = 0, n64 = 0;
 
+  // received samples of the next element pair are loaded one iteration ahead
+  constexpr int YR = (NRX + 31) / 32;
+  float2 ypf[2][YR];
+  int cpf[2];
+  auto prefetch = [&](int jbase) {
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int j = jbase + s;
+      cpf[s] = j < nd ? data_column[k0 + j] : 0;
+#pragma unroll
+      for (int q = 0; q < YR; ++q) {
+        const int r = lane + 32 * q;
+        ypf[s][q] = (j < nd && r < NRX) ? __ldg(grid + (((int64_t)b * NRX + r) * W + w) * gcols + cpf[s])
+                                        : make_float2(0.f, 0.f);
+      }
+    }
+  };
+  prefetch(warp * 2);
   for (int j0 = warp * 2; j0 < nd; j0 += 2 * MWARPS) {
+    float2 ycur[2][YR];
+    int ccur[2];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      ccur[s] = cpf[s];
+#pragma unroll
+      for (int q = 0; q < YR; ++q) ycur[s][q] = ypf[s][q];
+    }
+    if (j0 + 2 * MWARPS < nd) prefetch(j0 + 2 * MWARPS);
     // ---------------- Gram and matched filter of elements j0 and j0 + 1
-#pragma unroll 1
+#pragma unroll
     for (int s = 0; s < 2; ++s) {
       const int j = j0 + s;
-      float2* G = Gs + s * MT * MT;
+      float2* G = Gs + s * MT * GS;
       float2* bv = bs + s * MT;
       if (j >= nd) {  // no element: an identity system keeps the half-warp's arithmetic finite
-        for (int i = lane; i < MT * MT; i += 32) G[i] = make_float2((i % (MT + 1)) == 0 ? 1.f : 0.f, 0.f);
+        for (int i = lane; i < MT * MT; i += 32) G[(i / MT) * GS + i % MT] = make_float2((i % (MT + 1)) == 0 ? 1.f : 0.f, 0.f);
         if (lane < MT) bv[lane] = make_float2(0.f, 0.f);
         __syncwarp();
         continue;
       }
-      const int c = data_column[k0 + j];
+      const int c = ccur[s];
       const float2 g = tap_response(fc, hb, ds, tw, bins[c], N);
       if (lane == 0) {
         gsave[s] = g;
@@ -229,8 +259,11 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
         *reinterpret_cast<uint32_t*>(Plo + toff(NRX + r, t)) = pack2(c1, d1);
       }
       // Y tile: column 0 = [Re y; Im y], column 1 = [Im y; -Re y] (hi in 0-1, lo in 8-9)
-      for (int r = lane; r < NRX; r += 32) {
-        const float2 yv = grid[(((int64_t)b * NRX + r) * W + w) * gcols + c];
+#pragma unroll
+      for (int q = 0; q < YR; ++q) {
+        const int r = lane + 32 * q;
+        if (r >= NRX) continue;
+        const float2 yv = ycur[s][q];
         __nv_bfloat16 xr0, xr1, xi0, xi1, nr0, nr1;
         split_bf16(yv.x, xr0, xr1);
         split_bf16(yv.y, xi0, xi1);
@@ -291,7 +324,7 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
 #pragma unroll
           for (int e = 0; e < 2; ++e) {
             const int i = gm + hr * 8, jj = nt * 8 + gn + e;
-            G[i * MT + jj] = make_float2(gr[nt][hr * 2 + e], gi[nt][hr * 2 + e]);
+            G[i * GS + jj] = make_float2(gr[nt][hr * 2 + e], gi[nt][hr * 2 + e]);
           }
       if ((lane & 3) == 0) {
         bv[gm] = make_float2(by[0], by[1]);
@@ -303,15 +336,19 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
     // ---------------- FP32 Cholesky solve, one element per half-warp (lane i: row i)
     const int jme = j0 + half;
     const bool valid = jme < nd;
-    const float2* G = Gs + half * MT * MT;
+    const float2* G = Gs + half * MT * GS;
+    float2* col = colb + half * MT;
     float2 a[MT];
 #pragma unroll
-    for (int jj = 0; jj < MT; ++jj) a[jj] = G[row * MT + jj];
-    a[row].x += reg;
-    a[row].y = 0.f;
+    for (int jj = 0; jj < MT; ++jj) {
+      a[jj] = G[row * GS + jj];
+      if (jj == row) a[jj] = make_float2(a[jj].x + reg, 0.f);  // compile-time index: a[] stays in registers
+    }
     float2 bi = bs[half * MT + row];
     float pmin = INFINITY, pmax = 0.f, inv_i = 0.f;
     bool ok = true;
+    // right-looking Cholesky; column k of L goes through shared memory, every loop has
+    // a fixed trip count so that a[] stays in registers
 #pragma unroll
     for (int k = 0; k < MT; ++k) {
       const float dkk = __shfl_sync(0xffffffffu, a[k].x, k, 16);
@@ -323,14 +360,18 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
       if (row == k) inv_i = ik;
       const float2 lik = row > k ? cscale(a[k], ik) : (row == k ? make_float2(pk, 0.f) : make_float2(0.f, 0.f));
       a[k] = lik;
+      col[row] = lik;
+      __syncwarp();
 #pragma unroll
-      for (int jj = k + 1; jj < MT; ++jj) {
-        const float2 ljk = make_float2(__shfl_sync(0xffffffffu, lik.x, jj, 16), __shfl_sync(0xffffffffu, lik.y, jj, 16));
+      for (int jj = 0; jj < MT; ++jj) {
+        if (jj <= k) continue;
+        const float2 ljk = col[jj];
         if (row >= jj) {  // a[jj] -= lik conj(ljk)
           a[jj].x -= lik.x * ljk.x + lik.y * ljk.y;
           a[jj].y -= lik.y * ljk.x - lik.x * ljk.y;
         }
       }
+      __syncwarp();
     }
     // forward: L z = b
     float2 zi = make_float2(0.f, 0.f);

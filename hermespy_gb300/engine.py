@@ -43,6 +43,8 @@ class BerPoint:
     level_db: float
     errors: int
     bits: int
+    drops: int = 0
+    confident: bool = False
 
     @property
     def ber(self) -> float:
@@ -212,6 +214,13 @@ class LinkEngine:
             errors = torch.empty(n, dtype=torch.int32, device=self.device)
         if self.staged:
             self.receive(drop0, noise_power, stream)
+            if self.estimator == "lmmse" and self._lmmse is not None:
+                # fused: the LMMSE estimate stays on chip (hpx_detect_lmmse)
+                _lib.call("hpx_detect_lmmse", self._lmmse, self.num_rx,
+                          _lib.EQ_ZF if self.equalizer == "zf" else _lib.EQ_LMMSE, _lib.ptr(self._grid),
+                          self.num_columns, _lib.ptr(noise_power), self.seed, int(drop0), n, _lib.ptr(errors),
+                          _lib.stream_ptr(stream))
+                return errors
             self.estimate(n, noise_power, stream)
             return self.detect(drop0, n, noise_power, errors, stream)
         _lib.call("hpx_link_run", self._link, self.seed, int(drop0), n, _lib.ptr(noise_power), _lib.ptr(errors),
@@ -238,3 +247,43 @@ class LinkEngine:
             e = int(errs[i * drops_per_level:(i + 1) * drops_per_level].sum())
             pts.append(BerPoint(float(lv), e, drops_per_level * self.bits_per_drop))
         return pts
+
+    def ber_campaign(self, levels_db, accuracy: float = 1e-3, confidence: float = 0.05, min_samples: int = 64,
+                     max_drops_per_level: int = 1 << 20, batch: int | None = None, max_batches: int = 1 << 20,
+                     check_every: int = 4, drop0: int = 0) -> list[BerPoint]:
+        """Device-resident Monte Carlo over noise levels with the reference's
+        confidence stopping rule (``ScalarEvaluationResult.add_artifact``,
+        core/pymonte/scalar.py:101-125, on the per-drop BER): every level runs until
+        2 (1 - Phi(sqrt(n) accuracy / std)) < confidence or it holds
+        ``max_drops_per_level`` drops. The fused (ideal CSI, SISO LS) engines only."""
+
+        if self._link is None:
+            raise NotImplementedError("the campaign loop drives the fused drop pipeline (ideal CSI or SISO LS)")
+        levels_db = [float(v) for v in levels_db]
+        batch = min(self.max_drops, batch or self.max_drops)
+        power = np.ascontiguousarray(self.noise_power(levels_db).astype(np.float32))
+        h = ctypes.c_void_p()
+        _lib.check(_lib.load().hpx_campaign_create(len(levels_db), power.ctypes.data_as(ctypes.c_void_p),
+                                                   float(accuracy), float(confidence), int(min_samples),
+                                                   int(max_drops_per_level), batch, float(self.bits_per_drop),
+                                                   ctypes.byref(h)))
+        try:
+            done = ctypes.c_int64()
+            active = ctypes.c_int32()
+            _lib.call("hpx_campaign_run", h, self.link_handle, self.seed, int(drop0), batch, int(max_batches),
+                      int(check_every), ctypes.byref(done), ctypes.byref(active), _lib.stream_ptr())
+            L = len(levels_db)
+            drops = np.zeros(L, dtype=np.int64)
+            errors = np.zeros(L, dtype=np.int64)
+            conf = np.zeros(L, dtype=np.int32)
+            _lib.call("hpx_campaign_results", h, drops.ctypes.data_as(ctypes.c_void_p),
+                      errors.ctypes.data_as(ctypes.c_void_p), None, None, conf.ctypes.data_as(ctypes.c_void_p))
+        finally:
+            _lib.load().hpx_campaign_destroy(h)
+        return [BerPoint(lv, int(e), int(d) * self.bits_per_drop, int(d), bool(c))
+                for lv, e, d, c in zip(levels_db, errors, drops, conf)]
+
+    @property
+    def link_handle(self):
+        return self._link
+

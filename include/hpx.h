@@ -262,6 +262,15 @@ hpx_status hpx_lmmse_estimate(const hpx_lmmse* lmmse, const hpx_cf32* grid, int3
                               int32_t num_rx, int32_t batch, const float* noise_power, hpx_cf32* estimate,
                               void* stream);
 
+/* Fused receiver with the tap-domain LMMSE estimate: grid[B][Nrx][num_words][grid_columns]
+ * -> per drop the tap gains of every pair and word (as hpx_lmmse_estimate) in on-chip
+ * memory -> per data element the channel, equalization (ZF / LMMSE), hard demap and
+ * bit-error count -> errors[B]. Antenna pairs: 1x1, 2x1, 2x2, 4x1, 4x2, 4x4. The CSI
+ * grid never reaches HBM. No counterpart in the reference. */
+hpx_status hpx_detect_lmmse(const hpx_lmmse* lmmse, int32_t num_rx, int32_t mode, const hpx_cf32* grid,
+                            int32_t grid_columns, const float* noise_var, uint64_t seed, int64_t drop0,
+                            int32_t num_drops, uint32_t* errors, void* stream);
+
 /* Channel-estimate error over the frame's data elements, per drop:
  * err[b] = sum |est - truth|^2, power[b] = sum |truth|^2 over pairs x data elements,
  * est/truth[B][pairs][num_words][csi_columns]; NMSE = sum err / sum power. */
@@ -387,6 +396,31 @@ hpx_status hpx_link_run(const hpx_link* link, uint64_t seed, int64_t drop0, int3
 hpx_status hpx_link_run_static(const hpx_frame* frame, const hpx_fading* fading, const hpx_ls* ls,
                                int32_t equalizer, uint64_t seed, int64_t drop0, int32_t num_drops,
                                const float* noise_power, uint32_t* errors, void* stream);
+
+/* ------------------------------------------------- Monte Carlo campaign */
+
+/* Device-resident campaign over noise levels with the reference's confidence
+ * stopping rule (core/pymonte/scalar.py:101-125): per level the sums of the
+ * per-drop BER x and x^2 and the drop count stay on the GPU; a level stops once
+ * 2 (1 - Phi(sqrt(n) accuracy / std)) < confidence (std > 0, n >= min_samples) or
+ * it holds max_drops_per_level drops. Each batch assigns its drops round-robin to
+ * the levels still active and runs them through hpx_link_run. Replaces the
+ * actor/collector loop of core/pymonte/actors.py:23-253 for one link. */
+typedef struct hpx_campaign hpx_campaign;
+hpx_status hpx_campaign_create(int32_t num_levels, const float* noise_power, double accuracy, double confidence,
+                               int32_t min_samples, int64_t max_drops_per_level, int32_t max_batch,
+                               double bits_per_drop, hpx_campaign** out);
+hpx_status hpx_campaign_destroy(hpx_campaign* campaign);
+hpx_status hpx_campaign_reset(hpx_campaign* campaign);
+/* Up to max_batches batches of `batch` drops (drop indices drop0, drop0+1, ...);
+ * the host reads the number of active levels every `check_every` batches and
+ * returns when none is left. Synchronizes `stream` at those checks. */
+hpx_status hpx_campaign_run(hpx_campaign* campaign, hpx_link* link, uint64_t seed, int64_t drop0, int32_t batch,
+                            int32_t max_batches, int32_t check_every, int64_t* drops_run,
+                            int32_t* levels_active, void* stream);
+/* Host copies of the per-level drop counts, bit errors, BER sums and flags (any may be NULL). */
+hpx_status hpx_campaign_results(const hpx_campaign* campaign, int64_t* drops, int64_t* errors,
+                                double* ber_sum, double* ber_sq, int32_t* confident);
 
 #ifdef __cplusplus
 }

@@ -156,3 +156,26 @@ def test_engine_drops_match_oracle(est):
     for d, lv in enumerate(levels):
         ref = simulate_drop(lc, SEED, d, float(lv))
         assert abs(int(errs[d]) - ref["errors"]) <= max(3, 0.01 * ref["errors"])
+
+
+def test_fused_lmmse_receiver_matches_staged():
+    """hpx_detect_lmmse (estimate kept on chip) counts the same errors as
+    hpx_lmmse_estimate + hpx_detect_csi on the same drops."""
+
+    lay, cfg, fh, h, st, x, grid, p = _chain(nd=3, level=10 ** (-1.5))
+    C, W = lay.num_used, lay.num_words
+    lm = ctypes.c_void_p()
+    _lib.check(_lib.load().hpx_lmmse_create(fh, h.handle, C, ctypes.byref(lm)))
+    p3 = torch.full((3,), 10 ** (-1.5), dtype=torch.float32, device="cuda")
+    est = torch.empty((3, 4, 4, W, C), dtype=torch.complex64, device="cuda")
+    _lib.call("hpx_lmmse_estimate", lm, _lib.ptr(grid), C, 4, 3, _lib.ptr(p3), _lib.ptr(est), stream())
+    e1 = torch.empty(3, dtype=torch.int32, device="cuda")
+    _lib.call("hpx_detect_csi", fh, 4, 4, _lib.EQ_LMMSE, _lib.ptr(grid), C, _lib.ptr(est), C, _lib.ptr(p3), SEED, 0, 3,
+              _lib.ptr(e1), stream())
+    e2 = torch.empty(3, dtype=torch.int32, device="cuda")
+    _lib.call("hpx_detect_lmmse", lm, 4, _lib.EQ_LMMSE, _lib.ptr(grid), C, _lib.ptr(p3), SEED, 0, 3, _lib.ptr(e2),
+              stream())
+    a, b = host(e1), host(e2)
+    assert np.all(a > 0)
+    assert np.all(np.abs(a.astype(np.int64) - b.astype(np.int64)) <= np.maximum(2, a // 1000)), (a, b)
+    _lib.call("hpx_lmmse_destroy", lm)
