@@ -62,6 +62,12 @@ SPECS = {
     "link4x4": Spec("link4x4", 4096, 14 * 600 * 6 * 4, {
         "workload": "4x4 MIMO OFDM 1024/600 CP72 14 sym 64-QAM, 23-tap Rayleigh (k*50ns, -0.4k dB, 500 Hz), "
                     "ideal CSI + per-subcarrier 4x4 LMMSE, SNR U[0,30] dB", "samples": "complex64"}, 30.72e6),
+    "uneven": Spec("uneven", 16384, 0, {
+        "workload": "uneven batch in one persistent launch under a CUDA graph: 16384 drops with antennas uniform "
+                    "over {1,2,4,8}^2, FFT over {128,...,2048} (U = floor(0.586 N), CP N*72/1024, 30 kHz "
+                    "subcarriers), {4,7,14} words, QAM {4,16,64,256}, 1-23 taps 50 ns apart with exponential PDP "
+                    "(1-3 dB/tap), Doppler U[0,1000] Hz, SNR U[-5,30] dB; ideal CSI + LMMSE; launch shape by "
+                    "the autotuner", "samples": "complex64"}, 0.0),
     "massive": Spec("massive", 512, 14 * 3300 * 4 * 16, {
         "workload": "64x16 massive-MIMO uplink OFDM 4096/3300 CP288 14 sym 16-QAM, 8 taps (1-sample spacing, "
                     "3 dB/tap), 50 Hz, rx correlation 0.7^|i-j|, 61.44 MHz, SNR U[0,30] dB; split-BF16 "
@@ -80,10 +86,32 @@ def oracle_drop(args):
         cfg = LinkConfig(pilot_frame(64, 4), mimo_channel(30.72e6), 30.72e6, 4, 4, "lmmse", "lmmse", "snr")
     elif name == "link4x4":
         cfg = LinkConfig(mimo_frame(64), mimo_channel(30.72e6), 30.72e6, 4, 4, "ideal", "lmmse", "snr")
+    elif name == "uneven":
+        return uneven_oracle_drop(seed, drop)
     else:
         cfg = LinkConfig(massive_frame(), massive_channel(64, 0.7, 61.44e6), 61.44e6, 16, 64, "ideal", "lmmse",
                          "snr")
     return simulate_drop(cfg, seed, drop, level)["errors"]
+
+
+def uneven_oracle_drop(seed, drop):
+    """One float64 oracle drop of the uneven workload's distribution; returns its bits
+    (the sample's bits/s divides total bits by wall time)."""
+
+    from hermespy_gb300.uneven import random_drops
+    from oracle.fading import FadingConfig
+    from oracle.frame import DATA, FrameSpec, Resource, Section
+    from oracle.link import LinkConfig, simulate_drop
+
+    d = random_drops(1, 1000 + drop)[0]
+    N = d.fft_size
+    C, cp = int(np.floor(0.586 * N)), N * 72 // 1024
+    spec = FrameSpec(N, [Resource(1, cp / N, [(DATA, C)])], [Section(d.num_words, [0])], d.modulation_order, True)
+    k = np.arange(d.num_taps)
+    ch = FadingConfig(k * 50e-9, d.power_profile(), np.zeros(d.num_taps), 20, d.doppler_frequency)
+    cfg = LinkConfig(spec, ch, N * 30e3, d.num_tx, d.num_rx, "ideal", "lmmse", "snr")
+    simulate_drop(cfg, seed, drop, d.snr_db)
+    return d.num_words * C * int(np.log2(d.modulation_order)) * d.num_tx
 
 
 def cpu_pool():
@@ -112,13 +140,15 @@ def time_cpu(pool, cores, spec: Spec, rounds: int, seed: int = 11) -> tuple[floa
     if spec.name != "massive":
         pool.map(oracle_drop, work[:par])  # warm the workers (imports, first drop)
     t0 = time.perf_counter()
-    pool.map(oracle_drop, work, chunksize=1)
+    res = pool.map(oracle_drop, work, chunksize=1)
     dt = time.perf_counter() - t0
-    return drops * spec.bits_per_drop / dt, drops, dt
+    bits = sum(res) if spec.name == "uneven" else drops * spec.bits_per_drop
+    return bits / dt, drops, dt
 
 
 def cpu_sample_text(spec, drops, secs):
-    est = {"estimators": "tap-domain LMMSE estimation", "link4x4": "ideal CSI", "massive": "ideal CSI"}[spec.name]
+    est = {"estimators": "tap-domain LMMSE estimation", "link4x4": "ideal CSI", "massive": "ideal CSI",
+           "uneven": "random shapes of the uneven distribution, ideal CSI"}[spec.name]
     return (f"{drops} drops of the workload ({est}, LMMSE detection) in {secs:.1f} s: float64 numpy restatement "
             f"of the reference's drop, one process per core")
 
@@ -131,13 +161,14 @@ def run_reference(args, spec: Spec) -> None:
     rounds = 1 if spec.name != "massive" else 1
     for _ in range(args.warmup):
         time_cpu(pool, cores, spec, rounds)
-    drops, secs = 0, 0.0
+    drops, secs, bits = 0, 0.0, 0.0
     for k in range(args.steps):
-        _, d, s = time_cpu(pool, cores, spec, rounds, seed=100 + k)
+        v, d, s = time_cpu(pool, cores, spec, rounds, seed=100 + k)
         drops += d
         secs += s
+        bits += v * s
     pool.close()
-    value = drops * spec.bits_per_drop / secs
+    value = bits / secs
     line = {
         "impl": "reference",
         "metric": METRIC, "value": value, "unit": "bits/s", "n_gpus": args.gpus, "steps": args.steps,
@@ -524,6 +555,59 @@ def bench_massive(ctx, spec, args):
             "e2e_s": e2e_s, "h2d": 4 * drops, "d2h": 4 * drops, "launches": 5, "extra": extra}
 
 
+def bench_uneven(ctx, spec, args):
+    torch, _lib = ctx["torch"], ctx["lib"]
+    from hermespy_gb300.uneven import UnevenBatch, random_drops
+
+    drops = spec.drops if args.drops is None else args.drops
+    dev, stream = ctx["dev"], ctx["stream"]
+    cfgs = random_drops(drops, SEED + (ctx["drop_base"] >> 44))
+    batch = UnevenBatch(cfgs, 30e3, 50e-9, 20)
+    best = batch.tune(SEED, ctx["drop_base"], repeats=1)
+    batch.capture(SEED, ctx["drop_base"])
+    total_bits = float(batch.bits.sum())
+    for _ in range(args.warmup):
+        batch.replay(stream)
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        batch.replay(stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    total_ms = t0.elapsed_time(t1)
+    ber = float(batch.errors.sum().item()) / total_bits
+    # algorithmic HBM bytes per drop: transmit write, propagation read + write, receive
+    # read + grid write, detection grid read
+    byts = 0.0
+    for d in cfgs:
+        N = d.fft_size
+        C, cp = int(np.floor(0.586 * N)), N * 72 // 1024
+        T = d.num_words * (N + cp)
+        D = int(round((d.num_taps - 1) * 50e-9 * N * 30e3))
+        byts += 8 * (d.num_tx * T + d.num_tx * T + d.num_rx * (T + D) + d.num_rx * d.num_words * (N + C)
+                     + d.num_rx * d.num_words * C)
+    work = {"uneven_persistent": (byts / drops, "hbm")}
+    stage_ms = {"uneven_persistent": total_ms}
+    # e2e: host noise powers in, host errors out, around the graph replay
+    p_host = batch.noise_power.cpu().numpy()
+    p_pin = torch.from_numpy(p_host).pin_memory()
+    out_pin = torch.empty(drops, dtype=torch.int32).pin_memory()
+    n_e2e = max(3, args.steps // 2)
+    s0 = time.perf_counter()
+    for _ in range(n_e2e):
+        batch.noise_power.copy_(p_pin, non_blocking=True)
+        batch.replay(stream)
+        out_pin.copy_(batch.errors, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    e2e_s = (time.perf_counter() - s0) / n_e2e
+    spec.bits_per_drop = total_bits / drops
+    extra = {"autotuner": {"chosen": best, "candidates": batch.tuning}, "launch": "one persistent kernel per step "
+             "(CUDA graph replay of counter reset + kernel)", "total_bits_per_step": total_bits}
+    return {"drops": drops, "total_ms": total_ms, "stage_ms": stage_ms, "work": work, "ber": ber, "e2e_s": e2e_s,
+            "h2d": 4 * drops, "d2h": 4 * drops, "launches": 1, "extra": extra}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -566,8 +650,8 @@ def main() -> None:
     if world > 1:
         torch.distributed.barrier()
     with Clocks(local) as clk:
-        res = {"estimators": bench_estimators, "link4x4": bench_link4x4, "massive": bench_massive}[spec.name](
-            ctx, spec, args)
+        res = {"estimators": bench_estimators, "link4x4": bench_link4x4, "massive": bench_massive,
+               "uneven": bench_uneven}[spec.name](ctx, spec, args)
     total_ms, e2e_s = res["total_ms"], res["e2e_s"]
     if world > 1:
         import torch.distributed as dist
@@ -585,6 +669,8 @@ def main() -> None:
         info = stage_report(res["stage_ms"], args.steps, res["work"], drops, pk)
         roof = roofline_of(info, pk)
         cpu_value, cpu_drops, cpu_s = time_cpu(pool, cores, spec, args.cpu_rounds if spec.name != "massive" else 1)
+        if spec.name == "uneven":
+            spec.config = dict(spec.config, bits_per_drop_mean=spec.bits_per_drop)
         pool.close()
         line = {
             "metric": METRIC, "value": value, "unit": "bits/s", "n_gpus": world, "steps": args.steps,

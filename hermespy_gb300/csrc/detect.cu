@@ -2,6 +2,7 @@
 // receivers that end in bit-error counts.
 #include "fading_dev.cuh"
 #include "lmmse_dev.cuh"
+#include "equalize_dev.cuh"
 
 struct hpx_ls {
   const hpx_frame* frame;
@@ -16,120 +17,6 @@ struct hpx_ls {
 };
 
 namespace {
-
-// --------------------------------------------------------------- solvers
-
-// Cholesky solve of the Hermitian positive definite A x = b (lower triangle of A
-// used and overwritten). Returns false if a pivot is not positive.
-template <int n>
-__device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], float2 (&x)[n]) {
-  bool ok = true;
-  float inv[n];  // reciprocal pivots 1 / L[j][j]
-#pragma unroll
-  for (int j = 0; j < n; ++j) {
-    float d = A[j][j].x;
-#pragma unroll
-    for (int k = 0; k < j; ++k) d -= A[j][k].x * A[j][k].x + A[j][k].y * A[j][k].y;
-    ok = ok && (d > 0.0f);
-    inv[j] = rsqrtf(d);
-#pragma unroll
-    for (int i = j + 1; i < n; ++i) {
-      float2 s = A[i][j];
-#pragma unroll
-      for (int k = 0; k < j; ++k) {
-        // s -= A[i][k] * conj(A[j][k])
-        s.x -= A[i][k].x * A[j][k].x + A[i][k].y * A[j][k].y;
-        s.y -= A[i][k].y * A[j][k].x - A[i][k].x * A[j][k].y;
-      }
-      A[i][j] = cscale(s, inv[j]);
-    }
-  }
-  float2 z[n];
-#pragma unroll
-  for (int i = 0; i < n; ++i) {
-    float2 s = b[i];
-#pragma unroll
-    for (int k = 0; k < i; ++k) s = csub(s, cmul(A[i][k], z[k]));
-    z[i] = cscale(s, inv[i]);
-  }
-#pragma unroll
-  for (int i = n - 1; i >= 0; --i) {
-    float2 s = z[i];
-#pragma unroll
-    for (int k = i + 1; k < n; ++k) s = csub(s, cmulc(A[k][i], x[k]));
-    x[i] = cscale(s, inv[i]);
-  }
-  return ok;
-}
-
-// Equalize one resource element. Returns the number of output streams
-// (1 for ZF with a single receive antenna, which divides by sum_tx h like the
-// reference, NTX otherwise).
-template <int NRX, int NTX>
-__device__ __forceinline__ void equalize_one(int mode, const float2 (&H)[NRX][NTX], const float2 (&y)[NRX], float s2,
-                                             float2 (&x)[NTX]) {
-  if (mode == HPX_EQ_ZF && NRX == 1) {
-    float2 hs = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int t = 0; t < NTX; ++t) hs = cadd(hs, H[0][t]);
-    // complex division y / hs (numpy semantics: inf/nan for hs == 0)
-    const float den = hs.x * hs.x + hs.y * hs.y;
-    x[0] = make_float2((y[0].x * hs.x + y[0].y * hs.y) / den, (y[0].y * hs.x - y[0].x * hs.y) / den);
-#pragma unroll
-    for (int t = 1; t < NTX; ++t) x[t] = make_float2(0.f, 0.f);
-    return;
-  }
-  const float reg = mode == HPX_EQ_LMMSE ? s2 : 0.0f;
-  if (mode == HPX_EQ_ZF && NRX < NTX) {
-    // minimum-norm pseudo-inverse: x = H^H (H H^H)^-1 y
-    float2 A[NRX][NRX], yy[NRX], w[NRX];
-#pragma unroll
-    for (int i = 0; i < NRX; ++i) {
-      yy[i] = y[i];
-#pragma unroll
-      for (int j = 0; j <= i; ++j) {
-        float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int t = 0; t < NTX; ++t) cfma(acc, H[i][t], cconj(H[j][t]));
-        A[i][j] = acc;
-      }
-    }
-    if (!chol_solve<NRX>(A, yy, w)) {
-#pragma unroll
-      for (int t = 0; t < NTX; ++t) x[t] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
-      return;
-    }
-#pragma unroll
-    for (int t = 0; t < NTX; ++t) {
-      float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int i = 0; i < NRX; ++i) cfmac(acc, H[i][t], w[i]);
-      x[t] = acc;
-    }
-    return;
-  }
-  float2 A[NTX][NTX], b[NTX];
-#pragma unroll
-  for (int i = 0; i < NTX; ++i) {
-    float2 mf = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int r = 0; r < NRX; ++r) cfmac(mf, H[r][i], y[r]);
-    b[i] = mf;
-#pragma unroll
-    for (int j = 0; j <= i; ++j) {
-      float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int r = 0; r < NRX; ++r) cfmac(acc, H[r][i], H[r][j]);  // (H^H H)[i][j] = sum_r conj(H[r][i]) H[r][j]
-      A[i][j] = acc;
-    }
-    A[i][i].x += reg;
-    A[i][i].y = 0.0f;
-  }
-  if (!chol_solve<NTX>(A, b, x)) {
-#pragma unroll
-    for (int t = 0; t < NTX; ++t) x[t] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
-  }
-}
 
 template <int NRX, int NTX>
 __global__ void k_equalize(int mode, int64_t K, const float2* __restrict__ Hg, const float2* __restrict__ Yg,

@@ -397,6 +397,49 @@ hpx_status hpx_link_run_static(const hpx_frame* frame, const hpx_fading* fading,
                                int32_t equalizer, uint64_t seed, int64_t drop0, int32_t num_drops,
                                const float* noise_power, uint32_t* errors, void* stream);
 
+/* --------------------------------------------------------- uneven batches */
+
+/* One drop of an uneven batch. Frame: fft_size N in [128, 2048], floor(0.586 N)
+ * used data subcarriers, cyclic prefix N*72/1024, DC suppression, num_words data
+ * words, ideal CSI + LMMSE. Channel: num_taps Rayleigh taps k * tap_spacing apart
+ * with power 10^(-tap_decay_db k / 10), sampled at N * subcarrier_spacing. */
+typedef struct {
+  int32_t num_rx, num_tx;    /* 1, 2, 4 or 8 */
+  int32_t fft_size;
+  int32_t num_words;
+  int32_t modulation_order;  /* 4, 16, 64 or 256 */
+  int32_t num_taps;          /* 1 .. 64 */
+  double tap_decay_db;
+  double doppler_frequency;  /* Hz */
+} hpx_uneven_drop;
+
+/* Drops of different antenna counts, FFT sizes, frame lengths, modulation orders,
+ * channels and SNRs in ONE persistent launch: every CTA takes whole drops from an
+ * atomic counter (longest first) and runs realize -> transmit -> propagate + AWGN
+ * -> receive -> ideal CSI + LMMSE -> demap -> count with the homogeneous engine's
+ * arithmetic, so each drop's errors equal those of hpx_link_run for that drop.
+ * max_slots bounds the resident CTAs (one scratch slot each). No counterpart in the
+ * reference (its Monte Carlo actors run drops one by one). */
+typedef struct hpx_uneven hpx_uneven;
+hpx_status hpx_uneven_create(const hpx_uneven_drop* drops, int32_t num_drops, double subcarrier_spacing,
+                             double tap_spacing, int32_t num_sinusoids, int32_t max_slots, hpx_uneven** out);
+hpx_status hpx_uneven_destroy(hpx_uneven* batch);
+/* Data bits of every drop (host array [num_drops]). */
+hpx_status hpx_uneven_bits(const hpx_uneven* batch, int64_t* bits_per_drop);
+/* Launch shape: threads per CTA (128 or 256) and CTAs per SM (tuned by the caller's
+ * autotuner; hpx_uneven_get_config reports how many fit). */
+hpx_status hpx_uneven_config(hpx_uneven* batch, int32_t threads, int32_t blocks_per_sm);
+hpx_status hpx_uneven_get_config(const hpx_uneven* batch, int32_t* threads, int32_t* blocks_per_sm,
+                                 int32_t* max_blocks_per_sm);
+/* noise_power[num_drops], errors[num_drops] (drop d uses Philox drop index drop0 + d). */
+hpx_status hpx_uneven_run(hpx_uneven* batch, uint64_t seed, int64_t drop0, const float* noise_power,
+                          uint32_t* errors, void* stream);
+/* Capture the launch (counter reset + persistent kernel) into a CUDA graph with these
+ * arguments; hpx_uneven_replay launches it on `stream`. */
+hpx_status hpx_uneven_capture(hpx_uneven* batch, uint64_t seed, int64_t drop0, const float* noise_power,
+                              uint32_t* errors);
+hpx_status hpx_uneven_replay(hpx_uneven* batch, void* stream);
+
 /* ------------------------------------------------- Monte Carlo campaign */
 
 /* Device-resident campaign over noise levels with the reference's confidence
