@@ -141,8 +141,8 @@ _SIGNATURES = {
     "hpx_uneven_create": [c_void_p, c_int32, c_double, c_double, c_int32, c_int32, c_void_p],
     "hpx_uneven_destroy": [c_void_p],
     "hpx_uneven_bits": [c_void_p, c_void_p],
-    "hpx_uneven_config": [c_void_p, c_int32, c_int32],
-    "hpx_uneven_get_config": [c_void_p, c_void_p, c_void_p, c_void_p],
+    "hpx_uneven_config": [c_void_p, c_int32, c_int32, c_int32],
+    "hpx_uneven_get_config": [c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p],
     "hpx_uneven_run": [c_void_p, c_uint64, c_int64, c_void_p, c_void_p, c_void_p],
     "hpx_uneven_capture": [c_void_p, c_uint64, c_int64, c_void_p, c_void_p],
     "hpx_uneven_replay": [c_void_p, c_void_p],

@@ -29,8 +29,10 @@ __host__ __device__ inline size_t lmmse_taps_smem(int W, int U, int np, int ntx,
   return (size_t)W * U * NP * 8 + (size_t)NP * np * U * 8 + (size_t)ntx * U * W * np * 4 + (size_t)U * 4 + 16;
 }
 
-// Tap gains of every antenna pair and word of drop b into gt[W][U][NP] (pair =
-// rx * ntx + tx), all threads of the block:
+// Tap gains of every antenna pair and word of drop b into gt (pair = rx * ntx + tx),
+// stored as planes: for word w and tap u, NP real parts then NP imaginary parts
+// (float index (w U + u) 2 NP + {0, NP} + pair), so two pairs share each packed
+// FP32x2 FMA of the response. All threads of the block:
 //   1. weighted LS of the tap gains on each pilot word (one warp per dot product),
 //   2. per stream and tap the LMMSE weights over the words (np x np Cholesky),
 //   3. gt[w][u][pair] = sum_p weight * LS gain.
@@ -95,6 +97,7 @@ __device__ __forceinline__ void lmmse_drop_taps(const LmmseView& e, int b, int n
     }
   }
   __syncthreads();
+  float* gtf = reinterpret_cast<float*>(gt);
   for (int q = threadIdx.x; q < W * U * NP; q += blockDim.x) {
     const int w = q / (U * NP), rem = q - w * U * NP, u = rem / NP, pair = rem - u * NP;
     const int t = pair % ntx;
@@ -105,30 +108,50 @@ __device__ __forceinline__ void lmmse_drop_taps(const LmmseView& e, int b, int n
       acc.x = fmaf(c, g.x, acc.x);
       acc.y = fmaf(c, g.y, acc.y);
     }
-    gt[q] = acc;
+    float* dst = gtf + ((size_t)w * U + u) * 2 * NP;
+    dst[pair] = acc.x;
+    dst[NP + pair] = acc.y;
   }
   __syncthreads();
 }
 
-// Channel of all NP pairs at one element: H[pair] = sum_u gt_w[u][pair] tw[bin d_u],
-// each twiddle gathered once (gt_w: the word's [U][NP] gains in shared memory).
+// Channel of all NP pairs at one element: H[pair] = sum_u g_w[u][pair] tw[bin d_u],
+// each twiddle gathered once; g_w points at the word's planes (see lmmse_drop_taps).
+// Pairs are processed two at a time: re += gx t.x - gy t.y and im += gx t.y + gy t.x
+// as packed FP32x2 FMAs with (gx, gy) of two pairs from 16-byte loads.
 template <int NP>
 __device__ __forceinline__ void lmmse_response(const float2* gt_w, const int* ds, int U, int N, int bin,
                                                const float2* __restrict__ tw, float2 (&acc)[NP]) {
+  const float* g = reinterpret_cast<const float*>(gt_w);
+  if constexpr (NP == 1) {
+    acc[0] = make_float2(0.f, 0.f);
+    for (int u = 0; u < U; ++u) {
+      const float2 t = __ldg(tw + ((bin * ds[u]) & (N - 1)));
+      cfma(acc[0], make_float2(g[2 * u], g[2 * u + 1]), t);
+    }
+  } else {
+  constexpr int H2 = NP / 2;
+  float2 re[H2], im[H2];
 #pragma unroll
-  for (int i = 0; i < NP; ++i) acc[i] = make_float2(0.f, 0.f);
+  for (int i = 0; i < H2; ++i) re[i] = im[i] = make_float2(0.f, 0.f);
   for (int u = 0; u < U; ++u) {
     const float2 t = __ldg(tw + ((bin * ds[u]) & (N - 1)));
-    if (NP == 1) {
-      cfma(acc[0], gt_w[u], t);
-    } else {
-      const float4* g4 = reinterpret_cast<const float4*>(gt_w + u * NP);
+    const float2 tx = make_float2(t.x, t.x), ty = make_float2(t.y, t.y), nty = make_float2(-t.y, -t.y);
+    const float* gu = g + (size_t)u * 2 * NP;
 #pragma unroll
-      for (int i = 0; i < NP / 2; ++i) {
-        const float4 v = g4[i];
-        cfma(acc[2 * i], make_float2(v.x, v.y), t);
-        cfma(acc[2 * i + 1], make_float2(v.z, v.w), t);
-      }
+    for (int i = 0; i < H2; ++i) {
+      const float2 gx = *reinterpret_cast<const float2*>(gu + 2 * i);
+      const float2 gy = *reinterpret_cast<const float2*>(gu + NP + 2 * i);
+      re[i] = __ffma2_rn(gx, tx, re[i]);
+      re[i] = __ffma2_rn(gy, nty, re[i]);
+      im[i] = __ffma2_rn(gx, ty, im[i]);
+      im[i] = __ffma2_rn(gy, tx, im[i]);
     }
+  }
+#pragma unroll
+  for (int i = 0; i < H2; ++i) {
+    acc[2 * i] = make_float2(re[i].x, im[i].x);
+    acc[2 * i + 1] = make_float2(re[i].y, im[i].y);
+  }
   }
 }

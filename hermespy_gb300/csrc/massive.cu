@@ -150,7 +150,8 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
   unsigned char* wbase = base;  // per-warp areas first (16-byte aligned)
   float2* hb = reinterpret_cast<float2*>(base + MWARPS * SM::WARP_BYTES);
   float2* scratch = hb + fc.L;
-  float2* Sm = scratch + fc.L * fc.S1;  // [NRX][16]
+  // [NRX][16], 16-byte aligned for the float4 loads of the fill
+  float2* Sm = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(scratch + fc.L * fc.S1) + 15) & ~uintptr_t(15));
   int* ds = reinterpret_cast<int*>(Sm + NRX * MT);
   uint32_t* bitsm = reinterpret_cast<uint32_t*>(ds + fc.L + 4);
 
@@ -247,7 +248,8 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
       // P tiles: rows r (Re H) and NRX + r (Im H), two columns per lane and step
       for (int e = lane; e < NRX * MT / 2; e += 32) {
         const int r = e >> 3, t = (e & 7) * 2;
-        const float2 h0 = cmul(Sm[r * MT + t], g), h1 = cmul(Sm[r * MT + t + 1], g);
+        const float4 sp = *reinterpret_cast<const float4*>(Sm + r * MT + t);  // one 16-byte load, no bank conflicts
+        const float2 h0 = cmul(make_float2(sp.x, sp.y), g), h1 = cmul(make_float2(sp.z, sp.w), g);
         __nv_bfloat16 a0, a1, b0, b1, c0, c1, d0, d1;
         split_bf16(h0.x, a0, a1);
         split_bf16(h1.x, b0, b1);
@@ -463,7 +465,7 @@ hpx_status launch_massive(const hpx_fading* f, const void* state, const hpx_fram
   const FadingConst fc = fading_const(f);
   const int C = fr->info.num_columns, m = fr->info.bits_per_symbol;
   const size_t smem = (size_t)MWARPS * MassiveSmem<NRX>::WARP_BYTES + (size_t)fc.L * sizeof(float2) * (1 + fc.S1) +
-                      (size_t)NRX * MT * sizeof(float2) + (fc.L + 4) * sizeof(int) +
+                      (size_t)NRX * MT * sizeof(float2) + 16 + (fc.L + 4) * sizeof(int) +
                       (size_t)MT * staged_bit_words(C, m) * 4 + 16;
   if (smem > 220 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_massive: frame needs %zu bytes of shared memory", smem);
   auto kern = k_detect_massive<NRX>;

@@ -411,7 +411,10 @@ __device__ unsigned int u_detect(const UDrop& d, const UFrame& fr, const FadingC
 }
 
 // ---------------------------------------------------------- persistent kernel
-__global__ void __launch_bounds__(UMAX_THREADS) k_uneven(UArgs a, const __grid_constant__ QamTables qts) {
+// MINB = 1: registers as the largest stage needs; MINB = 2: capped so that two CTAs of
+// 256 threads share an SM (the autotuner measures both).
+template <int MINB>
+__global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __grid_constant__ QamTables qts) {
   extern __shared__ float4 smem4[];
   __shared__ int s_drop;
   __shared__ unsigned int s_sum[32];
@@ -512,7 +515,7 @@ struct hpx_uneven {
   unsigned char* d_scratch = nullptr;
   size_t slot_bytes = 0, off_x = 0, off_y = 0, off_grid = 0, smem = 0;
   int max_slots = 0;
-  int threads = 256, blocks_per_sm = 1, num_sms = 1;
+  int threads = 256, blocks_per_sm = 1, num_sms = 1, variant = 0;
   QamTables qts;
   cudaGraphExec_t graph = nullptr;
   cudaGraph_t graph_def = nullptr;
@@ -552,10 +555,11 @@ hpx_status uneven_launch(hpx_uneven* u, uint64_t seed, int64_t drop0, const floa
   a.drop0 = drop0;
   a.errors = errors;
   const int grid = std::min(u->num_sms * u->blocks_per_sm, u->max_slots);
+  auto kern = u->variant ? k_uneven<2> : k_uneven<1>;
   if (u->smem > 48 * 1024)  // the attribute is per kernel: set it for this batch's size
-    HPX_CUDA(cudaFuncSetAttribute(k_uneven, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem));
+    HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem));
   HPX_CUDA(cudaMemsetAsync(u->d_counter, 0, sizeof(unsigned int), s));
-  k_uneven<<<grid, u->threads, u->smem, s>>>(a, u->qts);
+  kern<<<grid, u->threads, u->smem, s>>>(a, u->qts);
   HPX_LAUNCHED("uneven");
   return HPX_OK;
 }
@@ -721,14 +725,16 @@ hpx_status hpx_uneven_create(const hpx_uneven_drop* drops, int32_t num_drops, do
     return hpx_cuda_status(e, "uneven tables");
   }
   if (u->smem > 48 * 1024) {
-    if ((e = cudaFuncSetAttribute(k_uneven, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem)) !=
-        cudaSuccess) {
+    if ((e = cudaFuncSetAttribute(k_uneven<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem)) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(k_uneven<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem)) !=
+            cudaSuccess) {
       uneven_release(u);
       return hpx_cuda_status(e, "uneven shared memory");
     }
   }
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_uneven, u->threads, u->smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_uneven<1>, u->threads, u->smem);
   u->blocks_per_sm = std::max(1, occ);
   *out = u;
   return HPX_OK;
@@ -745,16 +751,18 @@ hpx_status hpx_uneven_bits(const hpx_uneven* u, int64_t* bits_per_drop) {
   return HPX_OK;
 }
 
-hpx_status hpx_uneven_config(hpx_uneven* u, int32_t threads, int32_t blocks_per_sm) {
+hpx_status hpx_uneven_config(hpx_uneven* u, int32_t threads, int32_t blocks_per_sm, int32_t variant) {
   if (!u) return hpx_fail(HPX_ERR_ARG, "uneven_config: null argument");
   if (threads != 128 && threads != 256) return hpx_fail(HPX_ERR_ARG, "uneven_config: 128 or 256 threads");
+  if (variant != 0 && variant != 1) return hpx_fail(HPX_ERR_ARG, "uneven_config: variant 0 or 1");
   int occ = 0;
-  HPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_uneven, threads, u->smem));
+  HPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, variant ? k_uneven<2> : k_uneven<1>, threads, u->smem));
   if (occ < 1) return hpx_fail(HPX_ERR_UNSUPPORTED, "uneven_config: %d threads do not fit one SM", threads);
   if (blocks_per_sm < 1 || blocks_per_sm > occ)
     return hpx_fail(HPX_ERR_ARG, "uneven_config: %d CTAs per SM (1..%d fit)", blocks_per_sm, occ);
   u->threads = threads;
   u->blocks_per_sm = blocks_per_sm;
+  u->variant = variant;
   if (u->graph) {  // a captured graph holds the old launch shape
     cudaGraphExecDestroy(u->graph);
     cudaGraphDestroy(u->graph_def);
@@ -764,13 +772,17 @@ hpx_status hpx_uneven_config(hpx_uneven* u, int32_t threads, int32_t blocks_per_
   return HPX_OK;
 }
 
-hpx_status hpx_uneven_get_config(const hpx_uneven* u, int32_t* threads, int32_t* blocks_per_sm, int32_t* max_fit) {
+hpx_status hpx_uneven_get_config(const hpx_uneven* u, int32_t threads, int32_t variant, int32_t* cur_threads,
+                                 int32_t* cur_blocks_per_sm, int32_t* cur_variant, int32_t* max_fit) {
   if (!u) return hpx_fail(HPX_ERR_ARG, "uneven_get_config: null argument");
-  if (threads) *threads = u->threads;
-  if (blocks_per_sm) *blocks_per_sm = u->blocks_per_sm;
+  if (cur_threads) *cur_threads = u->threads;
+  if (cur_blocks_per_sm) *cur_blocks_per_sm = u->blocks_per_sm;
+  if (cur_variant) *cur_variant = u->variant;
   if (max_fit) {
     int occ = 0;
-    HPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_uneven, u->threads, u->smem));
+    if (threads == 128 || threads == 256)
+      HPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, variant ? k_uneven<2> : k_uneven<1>, threads,
+                                                             u->smem));
     *max_fit = occ;
   }
   return HPX_OK;

@@ -6,7 +6,7 @@ different antenna counts, FFT sizes, frame lengths, modulation orders, channels 
 SNRs to ``hpx_uneven_*``: one persistent kernel in which every CTA takes whole drops
 from an atomic counter (longest first) and runs each drop end to end with the
 homogeneous engine's arithmetic. ``tune`` times the launch shapes that fit (threads
-per CTA x CTAs per SM) and keeps the fastest; ``capture`` records the launch as a
+per CTA x CTAs per SM x register variant) and keeps the fastest; ``capture`` records the launch as a
 CUDA graph that ``replay`` re-launches.
 """
 
@@ -99,41 +99,46 @@ class UnevenBatch:
             pass
 
     # ------------------------------------------------------------- launch shape
-    def config(self) -> tuple[int, int, int]:
-        t, b, fit = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
-        _lib.call("hpx_uneven_get_config", self.handle, ctypes.byref(t), ctypes.byref(b), ctypes.byref(fit))
-        return t.value, b.value, fit.value
+    def config(self) -> dict:
+        t, b, v = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _lib.call("hpx_uneven_get_config", self.handle, 0, 0, ctypes.byref(t), ctypes.byref(b), ctypes.byref(v), None)
+        return {"threads": t.value, "blocks_per_sm": b.value, "variant": v.value}
 
-    def set_config(self, threads: int, blocks_per_sm: int) -> None:
-        _lib.call("hpx_uneven_config", self.handle, int(threads), int(blocks_per_sm))
+    def fit(self, threads: int, variant: int) -> int:
+        """CTAs of this shape that fit one SM."""
+
+        f = ctypes.c_int32()
+        _lib.call("hpx_uneven_get_config", self.handle, int(threads), int(variant), None, None, None, ctypes.byref(f))
+        return f.value
+
+    def set_config(self, threads: int, blocks_per_sm: int, variant: int = 0) -> None:
+        _lib.call("hpx_uneven_config", self.handle, int(threads), int(blocks_per_sm), int(variant))
 
     def tune(self, seed: int = 0, drop0: int = 0, repeats: int = 2) -> dict:
-        """Time every launch shape that fits (threads in {128, 256} x CTAs per SM up to
-        the occupancy limit) on this batch and keep the fastest."""
+        """Time every launch shape that fits (kernel variant x threads in {128, 256} x
+        CTAs per SM up to the occupancy and slot limits) on this batch; keep the fastest."""
 
+        sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         best = None
         self.tuning = []
-        for threads in (128, 256):
-            try:
-                self.set_config(threads, 1)
-            except (ValueError, NotImplementedError):
-                continue
-            fit = min(self.config()[2], max(1, self.max_slots // torch.cuda.get_device_properties(
-                self.device).multi_processor_count))
-            for bps in range(1, fit + 1):
-                self.set_config(threads, bps)
-                self.run(seed, drop0)  # warm
-                start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                start.record()
-                for _ in range(repeats):
-                    self.run(seed, drop0)
-                end.record()
-                torch.cuda.synchronize()
-                ms = start.elapsed_time(end) / repeats
-                self.tuning.append({"threads": threads, "blocks_per_sm": bps, "ms": ms})
-                if best is None or ms < best["ms"]:
-                    best = {"threads": threads, "blocks_per_sm": bps, "ms": ms}
-        self.set_config(best["threads"], best["blocks_per_sm"])
+        for variant in (0, 1):
+            for threads in (128, 256):
+                fit = min(self.fit(threads, variant), max(1, self.max_slots // sms))
+                for bps in range(1, fit + 1):
+                    self.set_config(threads, bps, variant)
+                    self.run(seed, drop0)  # warm
+                    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    start.record()
+                    for _ in range(repeats):
+                        self.run(seed, drop0)
+                    end.record()
+                    torch.cuda.synchronize()
+                    ms = start.elapsed_time(end) / repeats
+                    cand = {"variant": variant, "threads": threads, "blocks_per_sm": bps, "ms": ms}
+                    self.tuning.append(cand)
+                    if best is None or ms < best["ms"]:
+                        best = cand
+        self.set_config(best["threads"], best["blocks_per_sm"], best["variant"])
         return best
 
     # ------------------------------------------------------------------ running

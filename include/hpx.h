@@ -426,11 +426,13 @@ hpx_status hpx_uneven_create(const hpx_uneven_drop* drops, int32_t num_drops, do
 hpx_status hpx_uneven_destroy(hpx_uneven* batch);
 /* Data bits of every drop (host array [num_drops]). */
 hpx_status hpx_uneven_bits(const hpx_uneven* batch, int64_t* bits_per_drop);
-/* Launch shape: threads per CTA (128 or 256) and CTAs per SM (tuned by the caller's
- * autotuner; hpx_uneven_get_config reports how many fit). */
-hpx_status hpx_uneven_config(hpx_uneven* batch, int32_t threads, int32_t blocks_per_sm);
-hpx_status hpx_uneven_get_config(const hpx_uneven* batch, int32_t* threads, int32_t* blocks_per_sm,
-                                 int32_t* max_blocks_per_sm);
+/* Launch shape: threads per CTA (128 or 256), CTAs per SM and kernel variant (0:
+ * registers as needed, 1: capped for two 256-thread CTAs per SM), picked by the
+ * caller's autotuner. hpx_uneven_get_config reports the current shape and how many
+ * CTAs of (threads, variant) fit one SM. */
+hpx_status hpx_uneven_config(hpx_uneven* batch, int32_t threads, int32_t blocks_per_sm, int32_t variant);
+hpx_status hpx_uneven_get_config(const hpx_uneven* batch, int32_t threads, int32_t variant, int32_t* cur_threads,
+                                 int32_t* cur_blocks_per_sm, int32_t* cur_variant, int32_t* max_blocks_per_sm);
 /* noise_power[num_drops], errors[num_drops] (drop d uses Philox drop index drop0 + d). */
 hpx_status hpx_uneven_run(hpx_uneven* batch, uint64_t seed, int64_t drop0, const float* noise_power,
                           uint32_t* errors, void* stream);

@@ -59,5 +59,6 @@ def test_uneven_tune_graph_and_bits():
     batch.errors.zero_()
     batch.replay()
     assert torch.equal(batch.errors, first)
+    assert batch.config()["variant"] in (0, 1)
     with pytest.raises(ValueError):
         batch.set_config(96, 1)
