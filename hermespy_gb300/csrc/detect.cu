@@ -187,8 +187,9 @@ __global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_csi(
 // (lmmse_drop_taps) and every data element forms its channel from them, so the CSI
 // grid never reaches HBM. Same estimate, equalizer, demap and count as
 // hpx_lmmse_estimate + hpx_detect_csi.
+constexpr int LMMSE_THREADS = 512;
 template <int NRX, int NTX>
-__global__ void __launch_bounds__(256) k_detect_lmmse(LmmseView e, int C, int m, int num_data,
+__global__ void __launch_bounds__(LMMSE_THREADS, 2) k_detect_lmmse(LmmseView e, int C, int m, int num_data,
                                                       const int32_t* __restrict__ data_column,
                                                       const int32_t* __restrict__ data_word,
                                                       const int32_t* __restrict__ bins, const float2* __restrict__ tw,
@@ -599,7 +600,7 @@ hpx_status hpx_detect_lmmse(const hpx_lmmse* lm, int32_t nrx, int32_t mode, cons
   const LmmseView v = lmmse_view(lm);
   auto launch = [&](auto kern) -> hpx_status {
     HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<B, 256, smem, s>>>(v, fr->info.num_columns, m, nd, fr->d_data_column, fr->d_data_word, fr->d_bins,
+    kern<<<B, LMMSE_THREADS, smem, s>>>(v, fr->info.num_columns, m, nd, fr->d_data_column, fr->d_data_word, fr->d_bins,
                               fr->d_twiddle, qt, mode, reinterpret_cast<const float2*>(grid), gcols, nv, seed, drop0,
                               errors);
     HPX_LAUNCHED("detect_lmmse");

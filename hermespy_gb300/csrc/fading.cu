@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
   float* xp = reinterpret_cast<float*>(smem4);                        // [NTX][4][XW]
   float2* terms = reinterpret_cast<float2*>(smem4);                   // [L*S1][K+1], before the tile load
   const int region = DIRECT ? 2 * NTX * XW : max(2 * NTX * XW, L * S1 * (K + 1));  // in float2
-  float2* coef = reinterpret_cast<float2*>(smem4) + region;           // [L][K+1]
+  float4* coef = reinterpret_cast<float4*>(reinterpret_cast<float2*>(smem4) + region);  // [L][K+1] (x, x, y, y)
   int64_t* wp = reinterpret_cast<int64_t*>(coef + L * (K + 1));       // [2][L*S1] (direct)
   float2* Sm = reinterpret_cast<float2*>(wp + (DIRECT ? 2 * L * S1 : 0));  // [nrx*NTX]
   int* dl = reinterpret_cast<int*>(Sm + nrx * NTX);                   // [L]
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
       const int l = q / (K + 1), k = q - l * (K + 1);
       float2 acc = make_float2(0.f, 0.f);
       for (int n = 0; n < S1; ++n) acc = cadd(acc, terms[(l * S1 + n) * (K + 1) + k]);
-      coef[q] = acc;
+      coef[q] = make_float4(acc.x, acc.x, acc.y, acc.y);  // broadcast pairs for the packed FMAs
     }
   }
   __syncthreads();  // terms consumed: the tile may overwrite them
@@ -303,17 +303,17 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
         hy[pr] = make_float2(h0.y, h1.y);
       }
     } else {
-      const float2* cl = coef + l * (K + 1);
-      float2 ck[K + 1];
+      const float4* cl = coef + l * (K + 1);
+      float4 ck[K + 1];
 #pragma unroll
       for (int k = 0; k <= K; ++k) ck[k] = cl[k];
 #pragma unroll
       for (int pr = 0; pr < 2; ++pr) {
-        float2 ax = make_float2(ck[0].x, ck[0].x), ay = make_float2(ck[0].y, ck[0].y);
+        float2 ax = make_float2(ck[0].x, ck[0].y), ay = make_float2(ck[0].z, ck[0].w);
 #pragma unroll
         for (int k = 1; k <= K; ++k) {
-          ax = __ffma2_rn(make_float2(ck[k].x, ck[k].x), up[pr][k], ax);
-          ay = __ffma2_rn(make_float2(ck[k].y, ck[k].y), up[pr][k], ay);
+          ax = __ffma2_rn(make_float2(ck[k].x, ck[k].y), up[pr][k], ax);
+          ay = __ffma2_rn(make_float2(ck[k].z, ck[k].w), up[pr][k], ay);
         }
         hx[pr] = ax;
         hy[pr] = ay;
@@ -427,7 +427,7 @@ hpx_status launch_propagate(const hpx_fading* f, const void* state, int B, const
   constexpr int BT = tile_len<NTX>();
   const size_t tile = 2 * (size_t)NTX * tile_width(BT, fc.D) * sizeof(float2);
   const size_t terms = DIRECT ? 0 : (size_t)fc.L * fc.S1 * (K + 1) * sizeof(float2);
-  const size_t smem = (tile > terms ? tile : terms) + (size_t)fc.L * (K + 1) * sizeof(float2) +
+  const size_t smem = (tile > terms ? tile : terms) + (size_t)fc.L * (K + 1) * sizeof(float4) +
                       (DIRECT ? 2 * (size_t)fc.L * fc.S1 * sizeof(int64_t) : 0) +
                       (size_t)fc.nrx * NTX * sizeof(float2) + (size_t)fc.L * sizeof(int) + 16;
   if (smem > 200 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "propagate: channel too long for one tile");

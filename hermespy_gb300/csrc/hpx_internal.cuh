@@ -104,10 +104,13 @@ __device__ __forceinline__ float u01_f32(uint32_t w) { return ((float)(w >> 8) +
 // Box-Muller pair of unit normals from two words: r (cos 2 pi u2, sin 2 pi u2),
 // evaluated as -r (cos a, sin a) with a = 2 pi (u2 - 1/2) in (-pi, pi), where the
 // fast hardware sine and cosine are accurate to a few 1e-7.
+// The radius uses the hardware logarithm and reciprocal square root (a few 1e-7
+// relative, about 1e-6 RMS over the normal distribution).
 __device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b) {
   const float u1 = u01_f32(a);
   const float u2 = u01_f32(b);
-  const float r = sqrtf(-2.0f * logf(u1));
+  const float x = -2.0f * __logf(u1);
+  const float r = x * rsqrtf(fmaxf(x, 1e-30f));
   float s, c;
   __sincosf(6.283185307179586f * (u2 - 0.5f), &s, &c);
   return make_float2(-r * c, -r * s);

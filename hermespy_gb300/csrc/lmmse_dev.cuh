@@ -138,14 +138,32 @@ __device__ __forceinline__ void lmmse_response(const float2* gt_w, const int* ds
     const float2 t = __ldg(tw + ((bin * ds[u]) & (N - 1)));
     const float2 tx = make_float2(t.x, t.x), ty = make_float2(t.y, t.y), nty = make_float2(-t.y, -t.y);
     const float* gu = g + (size_t)u * 2 * NP;
+    if constexpr (NP % 4 == 0) {  // 16-byte loads: the gains of four pairs at once
 #pragma unroll
-    for (int i = 0; i < H2; ++i) {
-      const float2 gx = *reinterpret_cast<const float2*>(gu + 2 * i);
-      const float2 gy = *reinterpret_cast<const float2*>(gu + NP + 2 * i);
-      re[i] = __ffma2_rn(gx, tx, re[i]);
-      re[i] = __ffma2_rn(gy, nty, re[i]);
-      im[i] = __ffma2_rn(gx, ty, im[i]);
-      im[i] = __ffma2_rn(gy, tx, im[i]);
+      for (int i = 0; i < NP / 4; ++i) {
+        const float4 gx = *reinterpret_cast<const float4*>(gu + 4 * i);
+        const float4 gy = *reinterpret_cast<const float4*>(gu + NP + 4 * i);
+        const float2 gx0 = make_float2(gx.x, gx.y), gx1 = make_float2(gx.z, gx.w);
+        const float2 gy0 = make_float2(gy.x, gy.y), gy1 = make_float2(gy.z, gy.w);
+        re[2 * i] = __ffma2_rn(gx0, tx, re[2 * i]);
+        re[2 * i] = __ffma2_rn(gy0, nty, re[2 * i]);
+        im[2 * i] = __ffma2_rn(gx0, ty, im[2 * i]);
+        im[2 * i] = __ffma2_rn(gy0, tx, im[2 * i]);
+        re[2 * i + 1] = __ffma2_rn(gx1, tx, re[2 * i + 1]);
+        re[2 * i + 1] = __ffma2_rn(gy1, nty, re[2 * i + 1]);
+        im[2 * i + 1] = __ffma2_rn(gx1, ty, im[2 * i + 1]);
+        im[2 * i + 1] = __ffma2_rn(gy1, tx, im[2 * i + 1]);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < H2; ++i) {
+        const float2 gx = *reinterpret_cast<const float2*>(gu + 2 * i);
+        const float2 gy = *reinterpret_cast<const float2*>(gu + NP + 2 * i);
+        re[i] = __ffma2_rn(gx, tx, re[i]);
+        re[i] = __ffma2_rn(gy, nty, re[i]);
+        im[i] = __ffma2_rn(gx, ty, im[i]);
+        im[i] = __ffma2_rn(gy, tx, im[i]);
+      }
     }
   }
 #pragma unroll
