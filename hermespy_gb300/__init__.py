@@ -19,7 +19,7 @@ from .channel import (
     MultipathFadingRealization,
     MultipathFadingSample,
 )
-from .containers import Signal, StatedSymbols, Symbols
+from .containers import DenseSignal, Signal, SignalBlock, SparseSignal, StatedSymbols, Symbols
 from .engine import BerPoint, LinkEngine, clopper_pearson
 from .estimation import (
     ChannelEqualization,
@@ -34,6 +34,7 @@ from .estimation import (
 )
 from .mapping import PskQamMapping
 from .noise import AWGN, EBN0, ESN0, SNR, AWGNRealization
+from .presets import TDL, CorrelationType, Cost259, Cost259Type, DeviceType, StandardAntennaCorrelation, TDLType
 from .simulation import (
     BitErrorEvaluator,
     RandomBitsSource,

@@ -25,7 +25,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .containers import Signal, to_device, to_numpy
+from .containers import DenseSignal, Signal, SignalBlock, to_device, to_numpy
 
 
 class AntennaCorrelation:
@@ -236,10 +236,29 @@ class MultipathFadingSample:
         return y
 
     def propagate(self, signal, interpolation_mode=None) -> Signal:
-        if isinstance(signal, Signal):
+        """Propagate every block of ``signal`` (channel.py:306-379, fading.py:371-406).
+
+        As in the reference, each block is convolved with the taps from time zero
+        of the realization and keeps its offset; several blocks give a sparse
+        signal. A channel with zero expected energy returns an empty signal.
+        """
+
+        if not isinstance(signal, Signal):
+            return Signal(self.propagate_device(signal), self.sampling_rate)
+        if self.expected_energy_scale <= 0.0:
+            return Signal.Empty(signal.sampling_rate, self.num_receive_antennas, 0,
+                                carrier_frequency=signal.carrier_frequency, noise_power=signal.noise_power,
+                                delay=signal.delay)
+        if signal.num_streams != self.num_transmit_antennas:
+            raise ValueError(f"Number of signal streams to be propagated does not match the number of transmitter "
+                             f"antennas ({signal.num_streams} != {self.num_transmit_antennas}))")
+        if signal.num_blocks == 1 and isinstance(signal, DenseSignal):
             y = self.propagate_device(signal.device_samples)
-            return Signal(y, signal.sampling_rate, signal.carrier_frequency, 0.0, signal.offset)
-        return Signal(self.propagate_device(signal), self.sampling_rate)
+            return DenseSignal(y, signal.sampling_rate, signal.carrier_frequency, signal.noise_power, signal.offset,
+                               signal.delay)
+        blocks = [SignalBlock(self.propagate_device(b.device_samples), b.offset) for b in signal.blocks]
+        return Signal.Create(blocks, self.sampling_rate, signal.carrier_frequency, signal.noise_power, signal.delay,
+                             offsets=[b.offset for b in blocks])
 
     def state_device(self, num_samples: int, max_num_taps: int) -> torch.Tensor:
         ntaps = min(1 + self._handle.max_delay, int(max_num_taps))

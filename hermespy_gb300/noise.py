@@ -24,13 +24,21 @@ class AWGNRealization:
         self.drop = int(drop)
 
     def add_to(self, signal: Signal) -> Signal:
+        """Noise of the signal's whole (streams, samples) extent, added to every
+        block at its offset (model.py:143-160)."""
+
         if self.power == 0.0:
             return signal
         out = signal.copy()
-        x = out.device_samples
+        dense = out.num_blocks == 1 and out.blocks[0].offset == 0 and out.blocks[0].num_samples == out.num_samples
+        x = out.blocks[0].device_samples if dense else torch.zeros(out.shape, dtype=torch.complex64,
+                                                                    device=_lib.require_cuda())
         p = torch.tensor([self.power], dtype=torch.float32, device=x.device)
         _lib.call("hpx_awgn_add", _lib.ptr(x), 1, x.shape[0], x.shape[1], _lib.ptr(p), self.seed, self.drop,
                   _lib.stream_ptr())
+        if not dense:
+            for b in out.blocks:
+                b.device_samples.add_(x[:, b.offset:b.end])
         out.noise_power = self.power
         return out
 

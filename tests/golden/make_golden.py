@@ -1,6 +1,9 @@
 """Generate the golden fixtures of the HermesPy reference (run where its source is available).
 
-Usage:  python tests/golden/make_golden.py [path-to-hermespy-checkout]
+Usage:  python tests/golden/make_golden.py [path-to-hermespy-checkout] [fixture ...]
+
+With fixture names (``qam``, ``ofdm``, ``fading``, ``ls``, ``ideal``, ``zf``, ``ber``,
+``drops``, ``presets``) only those are regenerated.
 
 Every fixture is an output of the reference's own code, fed inputs that the
 oracle can reproduce (seeded numpy draws or the engine's Philox streams):
@@ -16,6 +19,10 @@ ls.npz       ``OrthogonalLeastSquaresChannelEstimation.estimate_channel`` on the
 ideal.npz    ``OFDMIdealChannelEstimation.estimate_channel`` for a 2x2 sample.
 zf.npz       ``ZeroForcingChannelEqualization.equalize_channel``, SISO and 4x4.
 ber.npz      ``BitErrorEvaluator.evaluate`` including unequal-length padding.
+presets.npz  Tap delays, power profiles, Rice factors and line-of-sight Doppler of
+             the ``TDL`` (A-E), ``Cost259`` (urban, rural, hilly) and
+             ``Exponential`` presets, and ``StandardAntennaCorrelation``
+             covariances for 1, 2 and 4 antennas per correlation type and side.
 drops.npz    Whole ``SimulationScenario.drop()`` runs (SISO LS+ZF at three Eb/N0,
              2x2 ideal CSI + ZF) with bits, fading draws and noise injected from
              the engine's Philox streams.
@@ -38,6 +45,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 import refimport  # noqa: E402
 
 REF = sys.argv[1] if len(sys.argv) > 1 else refimport.DEFAULT_REFERENCE
+ONLY = set(sys.argv[2:])
 refimport.import_reference(REF)
 
 from scipy.stats import norm  # noqa: E402
@@ -382,12 +390,45 @@ def make_drops() -> None:
     save("drops.npz", **out)
 
 
+def make_presets() -> None:
+    from hermespy.channel import TDL, Cost259, Cost259Type, Exponential, TDLType
+    from hermespy.channel.fading.correlation import CorrelationType, StandardAntennaCorrelation
+    from hermespy.core import AntennaMode
+
+    out = {}
+    for t in TDLType:
+        for tag, rms in (("0", 0.0), ("300ns", 300e-9)):
+            ch = TDL(model_type=t, rms_delay=rms, doppler_frequency=10.0, seed=1)
+            key = f"tdl_{t.name}_{tag}"
+            out[key + "_delays"] = np.asarray(ch.delays, dtype=np.float64)
+            out[key + "_power"] = np.asarray(ch.power_profile, dtype=np.float64)
+            out[key + "_rice"] = np.asarray(ch.rice_factors, dtype=np.float64)
+            out[key + "_los_doppler"] = np.float64(ch.los_doppler_frequency)
+    for t in Cost259Type:
+        ch = Cost259(model_type=t, doppler_frequency=10.0, seed=1)
+        key = f"cost259_{t.name}"
+        out[key + "_delays"] = np.asarray(ch.delays, dtype=np.float64)
+        out[key + "_power"] = np.asarray(ch.power_profile, dtype=np.float64)
+        out[key + "_rice"] = np.asarray(ch.rice_factors, dtype=np.float64)
+        out[key + "_los_doppler"] = np.float64(ch.los_doppler_frequency)
+    for interval, rms in ((1e-7, 3e-7), (5e-8, 1e-6)):
+        ch = Exponential(interval, rms, seed=1)
+        key = f"exponential_{interval:g}_{rms:g}"
+        out[key + "_delays"] = np.asarray(ch.delays, dtype=np.float64)
+        out[key + "_power"] = np.asarray(ch.power_profile, dtype=np.float64)
+    for c in CorrelationType:
+        model = StandardAntennaCorrelation(c)
+        for n in (1, 2, 4):
+            arr = SimpleNamespace(num_receive_antennas=n, num_transmit_antennas=n)
+            out[f"corr_{c.name}_{n}_rx"] = model.sample_covariance(arr, AntennaMode.RX)
+            out[f"corr_{c.name}_{n}_tx"] = model.sample_covariance(arr, AntennaMode.TX)
+    save("presets.npz", **out)
+
+
+MAKERS = {"qam": make_qam, "ofdm": make_ofdm, "fading": make_fading, "ls": make_ls, "ideal": make_ideal,
+          "zf": make_zf, "ber": make_ber, "drops": make_drops, "presets": make_presets}
+
 if __name__ == "__main__":
-    make_qam()
-    make_ofdm()
-    make_fading()
-    make_ls()
-    make_ideal()
-    make_zf()
-    make_ber()
-    make_drops()
+    for name, maker in MAKERS.items():
+        if not ONLY or name in ONLY:
+            maker()
