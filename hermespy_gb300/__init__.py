@@ -42,6 +42,22 @@ from .simulation import (
     SimulatedDevice,
     SimulationScenario,
 )
-from .waveform import ElementType, GridElement, GridResource, OFDMWaveform, PrefixType, SymbolSection
+from .synchronization import (
+    CorrelationSynchronization,
+    OFDMCorrelationSynchronization,
+    OFDMSynchronization,
+    SchmidlCoxSynchronization,
+    Synchronization,
+)
+from .waveform import (
+    ElementType,
+    GridElement,
+    GridResource,
+    OFDMWaveform,
+    PilotSection,
+    PrefixType,
+    SchmidlCoxPilotSection,
+    SymbolSection,
+)
 
 __version__ = "1.0.0"

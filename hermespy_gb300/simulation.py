@@ -88,7 +88,22 @@ class SimplexLink:
     def receive(self, signal: Signal, device: SimulatedDevice) -> torch.Tensor:
         wf = self.waveform
         T = wf.samples_per_frame()
-        frame = signal.device_samples[:, :T].contiguous()
+        # frame start from the waveform's synchronization (modem.py:1085-1146); the
+        # default routine puts frames back to back from sample 0
+        start = None
+        for block in signal.blocks:
+            found = wf.synchronization.synchronize(block.device_samples, device.bandwidth, 1)
+            if found:
+                start = (block, int(found[0]))
+                break
+        if start is None:
+            self.reception = {"bits": torch.zeros(0, dtype=torch.uint8, device=signal.device_samples.device)}
+            return self.reception["bits"]
+        block, s0 = start
+        frame = block.device_samples[:, s0:s0 + T]
+        if frame.shape[1] < T:
+            frame = torch.nn.functional.pad(frame, (0, T - frame.shape[1]))
+        frame = frame.contiguous()
         grids = wf.demodulate_device(frame)  # (Nrx, W, N)
         stated = wf.estimate_channel(Symbols(grids), device.bandwidth, 1)
         stated.noise_variance = signal.noise_power

@@ -7,8 +7,12 @@ Mirrors the reference's grid description and ``OFDMWaveform``
 keeps ``map / unmap / place / pick / modulate / demodulate``,
 ``estimate_channel / equalize_symbols`` and the frame bookkeeping properties.
 The frame's tables live on the GPU (one ``hpx_frame`` handle per layout).
-Oversampling factors other than 1, pilot (preamble) sections and symbol
-sections with a sample offset are not part of the engine and raise
+A ``PilotSection`` / ``SchmidlCoxPilotSection`` preamble (waveform.py:719-903,
+ofdm.py:184-205) is modulated once by the transmit kernel and prepended to every
+frame; ``demodulate`` skips it, and ``synchronization`` (``Synchronization``,
+``SchmidlCoxSynchronization``, ``OFDMCorrelationSynchronization``) finds frame
+starts with the metric kernels of ``hpx_sync_*``. Oversampling factors other than 1
+and symbol sections with a sample offset are not part of the engine and raise
 ``NotImplementedError``.
 """
 
@@ -100,6 +104,127 @@ class SymbolSection:
         return self.num_repetitions * len(self.pattern)
 
 
+class PilotSection:
+    """Static preamble of one OFDM symbol without prefix (waveform.py:719-903).
+
+    Its N subcarriers carry ``pilot_elements`` (tiled), or by default the frame
+    mapping's symbols of ``numpy.random.default_rng(50)`` bits, as in the reference.
+    """
+
+    def __init__(self, pilot_elements: Symbols | None = None, wave=None) -> None:
+        self.pilot_elements = pilot_elements
+        self.wave = wave
+        self._cache = None
+
+    @property
+    def pilot_elements(self) -> Symbols | None:
+        return self._pilot_elements
+
+    @pilot_elements.setter
+    def pilot_elements(self, value: Symbols | None) -> None:
+        if value is not None:
+            if value.num_streams != 1:
+                raise ValueError("Subsymbol pilot configuration may only contain a single stream")
+            if value.num_symbols < 1:
+                raise ValueError("Subsymbol pilot configuration must contain at least one symbol")
+        self._pilot_elements = value
+        self._cache = None
+
+    @property
+    def num_repetitions(self) -> int:
+        return 1
+
+    @num_repetitions.setter
+    def num_repetitions(self, value: int) -> None:
+        if value != 1:
+            raise ValueError("Pilot sections may not be repeated")
+
+    @property
+    def sample_offset(self) -> int:
+        return 0
+
+    @sample_offset.setter
+    def sample_offset(self, value: int) -> None:
+        if value != 0:
+            raise ValueError("Pilot sections may not have a sample offset")
+
+    def num_samples(self, bandwidth: float = 1.0, oversampling_factor: int = 1) -> int:
+        return self.wave.num_subcarriers * oversampling_factor
+
+    @property
+    def num_words(self) -> int:
+        return 1
+
+    @property
+    def num_symbols(self) -> int:
+        return 0
+
+    @property
+    def num_references(self) -> int:
+        if self._pilot_elements is not None or self.wave is None:
+            return 0
+        return self.wave.num_subcarriers
+
+    def _pilot_sequence(self, num_symbols: int | None = None) -> np.ndarray:
+        n = self.wave.num_subcarriers if num_symbols is None else int(num_symbols)
+        if self._pilot_elements is None:
+            rng = np.random.default_rng(50)
+            bits = rng.integers(0, 2, n * self.wave.mapping.bits_per_symbol, np.uint8).flatten()
+            symbols = self.wave.mapping.get_symbols(bits)
+        else:
+            flat = self._pilot_elements.raw.reshape(-1)
+            symbols = np.tile(flat, int(np.ceil(n / flat.size)))
+        return np.asarray(symbols, dtype=np.complex128)[:n]
+
+    def generate_device(self) -> torch.Tensor:
+        """The preamble's N time-domain samples (the transmit kernel on a one-word,
+        N-column, prefix-free frame), cached per subcarrier count."""
+
+        n = self.wave.num_subcarriers
+        key = (n, self.wave.dc_suppression, self.wave.modulation_order)
+        if self._cache is None or self._cache[0] != key:
+            grid = to_device(self._pilot_sequence(n)).reshape(1, 1, n)
+            kind = np.full((1, n), ElementType.REFERENCE.value, dtype=np.int8)
+            prefix = np.zeros(1, dtype=np.int32)
+            desc = _lib.FrameDesc(n, 1, n, self.wave.modulation_order, int(self.wave.dc_suppression),
+                                  prefix.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                  prefix.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                  kind.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), 0)
+            h = ctypes.c_void_p()
+            _lib.check(_lib.load().hpx_frame_create(ctypes.byref(desc), ctypes.byref(h)))
+            try:
+                out = torch.empty((1, n), dtype=torch.complex64, device=grid.device)
+                _lib.call("hpx_ofdm_modulate_grid", h, _lib.ptr(grid), n, 1, _lib.ptr(out), _lib.stream_ptr())
+                torch.cuda.current_stream().synchronize()
+            finally:
+                _lib.call("hpx_frame_destroy", h)
+            self._cache = (key, out[0])
+        return self._cache[1]
+
+    def generate(self, oversampling_factor: int = 1) -> np.ndarray:
+        if self.wave is None:
+            raise RuntimeError("Pilot section must be associated with a waveform")
+        if oversampling_factor != 1:
+            raise NotImplementedError("the engine runs OFDM frames without oversampling")
+        return to_numpy(self.generate_device())
+
+
+class SchmidlCoxPilotSection(PilotSection):
+    """Schmidl-Cox preamble: pilots on every second subcarrier, so the symbol's two
+    halves repeat in time (ofdm.py:184-205)."""
+
+    def _pilot_sequence(self, num_symbols: int | None = None) -> np.ndarray:
+        if self.wave is None:
+            raise RuntimeError("Waveform not set for pilot section")
+        n = self.wave.num_subcarriers
+        stuffed = np.zeros(n, dtype=np.complex128)
+        stuffed[::2] = PilotSection._pilot_sequence(self, int(np.ceil(0.5 * n)))
+        if self.wave.dc_suppression:
+            dc = int(0.5 * n)
+            stuffed[:dc] = np.roll(stuffed[:dc], 1)
+        return stuffed
+
+
 class OFDMWaveform:
     """Orthogonal frequency-division multiplexing waveform (ofdm.py:33-181)."""
 
@@ -109,8 +234,8 @@ class OFDMWaveform:
                  oversampling_factor: int = 1, pilot_comb: int = 0, **kwargs) -> None:
         if num_subcarriers < 1:
             raise ValueError("Number of subcarriers must be greater or equal to one")
-        if pilot_section is not None or pilot_sequence is not None:
-            raise NotImplementedError("pilot sections and custom pilot sequences are not part of the engine")
+        if pilot_sequence is not None:
+            raise NotImplementedError("custom pilot symbol sequences are not part of the engine")
         self.num_subcarriers = int(num_subcarriers)
         self.grid_resources = list(grid_resources)
         self.grid_structure = list(grid_structure)
@@ -123,6 +248,8 @@ class OFDMWaveform:
         # reference): with pilot_comb = P > 1 stream s sends the reference element
         # of grid column c only if c % P == s % P.
         self.pilot_comb = int(pilot_comb)
+        self.pilot_section = pilot_section
+        self._synchronization = None
         self._channel_estimation = None
         self._channel_equalization = None
         self._handle = None
@@ -228,9 +355,50 @@ class OFDMWaveform:
     def symbols_per_frame(self) -> int:
         return self.num_data_symbols + self.references_per_frame
 
+    @property
+    def pilot_section(self) -> PilotSection | None:
+        return self._pilot_section
+
+    @pilot_section.setter
+    def pilot_section(self, value: PilotSection | None) -> None:
+        self._pilot_section = value
+        if value is not None and value.wave is not self:
+            value.wave = self
+
+    def _preamble_length(self) -> int:
+        return self.num_subcarriers if self._pilot_section is not None else 0
+
+    def pilot_signal(self, bandwidth: float = 1.0, oversampling_factor: int = 1):
+        """The preamble as a signal (empty without a pilot section)."""
+
+        from .containers import Signal
+
+        self._check_osf(oversampling_factor)
+        if self._pilot_section is None:
+            return Signal.Empty(bandwidth * oversampling_factor)
+        return Signal.Create(self._pilot_section.generate_device()[None], bandwidth * oversampling_factor)
+
+    @property
+    def synchronization(self):
+        if self._synchronization is None:
+            from .synchronization import Synchronization
+
+            self._synchronization = Synchronization(self)
+        return self._synchronization
+
+    @synchronization.setter
+    def synchronization(self, value) -> None:
+        self._synchronization = value
+        if value is not None and value.waveform is not self:
+            value.waveform = self
+
     def samples_per_frame(self, bandwidth: float = 1.0, oversampling_factor: int = 1) -> int:
         t = self._layout()
-        return int(t["num_words"] * self.num_subcarriers * oversampling_factor + t["prefix"].sum())
+        return int(t["num_words"] * self.num_subcarriers * oversampling_factor + t["prefix"].sum()) + \
+            self._preamble_length() * oversampling_factor
+
+    def _grid_samples(self) -> int:
+        return self.samples_per_frame() - self._preamble_length()
 
     def frame_duration(self, bandwidth: float) -> float:
         return self.samples_per_frame(bandwidth, 1) / bandwidth
@@ -288,18 +456,24 @@ class OFDMWaveform:
         """(batch, words, G) placed grids -> (batch, T) samples."""
 
         grid = grid.contiguous()
-        out = torch.empty((grid.shape[0], self.samples_per_frame()), dtype=torch.complex64, device=grid.device)
+        out = torch.empty((grid.shape[0], self._grid_samples()), dtype=torch.complex64, device=grid.device)
         _lib.call("hpx_ofdm_modulate_grid", self._frame(), _lib.ptr(grid), grid.shape[-1], grid.shape[0],
                   _lib.ptr(out), _lib.stream_ptr())
-        return out
+        return self._with_preamble(out)
+
+    def _with_preamble(self, frames: torch.Tensor) -> torch.Tensor:
+        if self._pilot_section is None:
+            return frames
+        pre = self._pilot_section.generate_device()
+        return torch.cat([pre[None].expand(frames.shape[0], -1), frames], dim=1)
 
     def modulate_data_device(self, data: torch.Tensor) -> torch.Tensor:
         """(batch, num_data) data symbols -> (batch, T) samples (place + modulate fused)."""
 
         data = to_device(data).reshape(-1, self.num_data_symbols).contiguous()
-        out = torch.empty((data.shape[0], self.samples_per_frame()), dtype=torch.complex64, device=data.device)
+        out = torch.empty((data.shape[0], self._grid_samples()), dtype=torch.complex64, device=data.device)
         _lib.call("hpx_ofdm_modulate", self._frame(), _lib.ptr(data), data.shape[0], _lib.ptr(out), _lib.stream_ptr())
-        return out
+        return self._with_preamble(out)
 
     def modulate(self, data_symbols: Symbols, bandwidth: float = 1.0, oversampling_factor: int = 1) -> np.ndarray:
         self._check_osf(oversampling_factor)
@@ -311,6 +485,9 @@ class OFDMWaveform:
     def demodulate_device(self, samples: torch.Tensor, num_columns: int | None = None) -> torch.Tensor:
         """(batch, >= T) samples -> (batch, words, num_columns) grid."""
 
+        pre = self._preamble_length()
+        if pre:  # skip the preamble (waveform.py:1328-1330)
+            samples = samples[:, pre:]
         samples = samples.contiguous()
         cols = self.num_subcarriers if num_columns is None else num_columns
         out = torch.empty((samples.shape[0], self.words_per_frame, cols), dtype=torch.complex64, device=samples.device)

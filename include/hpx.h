@@ -359,6 +359,23 @@ hpx_status hpx_detect_massive(const hpx_fading* fading, const void* state, const
 hpx_status hpx_awgn_add(hpx_cf32* samples, int32_t batch, int32_t num_streams, int64_t num_samples,
                         const float* noise_power, uint64_t seed, int64_t drop0, void* stream);
 
+/* ----------------------------------------------------------- synchronization */
+
+/* Schmidl-Cox delay metric of `batch` received signals [batch][num_streams][num_samples]:
+ * metric[b][0] = 0 and metric[b][1 + d] = sum_s |sum_{k<L/2} conj(x[d+k]) x[d+k+L/2]| for
+ * d = 0 .. num_samples - L (L = symbol_length), i.e. num_samples - L + 2 doubles per
+ * signal, the layout of SchmidlCoxSynchronization.synchronize's delay_powers
+ * (modem/waveforms/orthogonal/ofdm.py:236-248). The caller's find_peaks and the -1
+ * index correction (:250-255) follow on the host. Signals shorter than L write nothing. */
+hpx_status hpx_sync_schmidl_cox(const hpx_cf32* signal, int32_t batch, int32_t num_streams, int64_t num_samples,
+                                int32_t symbol_length, double* metric, void* stream);
+/* Pilot correlation profile correlation[b][k] = sum_s |sum_j x[k - (P-1) + j] conj(pilot[j])|,
+ * k = 0 .. num_samples + P - 2 (scipy.signal.correlate(x, pilot, "full") magnitudes summed
+ * over streams), before the normalization and peak search of
+ * CorrelationSynchronization.synchronize (modem/waveform_correlation_synchronization.py:119-170). */
+hpx_status hpx_sync_correlation(const hpx_cf32* signal, int32_t batch, int32_t num_streams, int64_t num_samples,
+                                const hpx_cf32* pilot, int32_t pilot_length, double* correlation, void* stream);
+
 /* ------------------------------------------------------- batched drop loop */
 
 enum { HPX_EST_IDEAL = 0, HPX_EST_LS = 1 };

@@ -19,6 +19,10 @@ ls.npz       ``OrthogonalLeastSquaresChannelEstimation.estimate_channel`` on the
 ideal.npz    ``OFDMIdealChannelEstimation.estimate_channel`` for a 2x2 sample.
 zf.npz       ``ZeroForcingChannelEqualization.equalize_channel``, SISO and 4x4.
 ber.npz      ``BitErrorEvaluator.evaluate`` including unequal-length padding.
+sync.npz     ``PilotSection`` / ``SchmidlCoxPilotSection`` preambles (128 subcarriers,
+             with and without DC suppression) and the frame starts that
+             ``SchmidlCoxSynchronization`` and ``OFDMCorrelationSynchronization``
+             find in noisy two-stream signals holding two or three frames.
 presets.npz  Tap delays, power profiles, Rice factors and line-of-sight Doppler of
              the ``TDL`` (A-E), ``Cost259`` (urban, rural, hilly) and
              ``Exponential`` presets, and ``StandardAntennaCorrelation``
@@ -425,8 +429,56 @@ def make_presets() -> None:
     save("presets.npz", **out)
 
 
+def sync_waveform(dc: bool, pilot):
+    """128-point frame with a preamble: 100 used data subcarriers, CP 10, 4 words."""
+
+    N, U, CP = 128, 100, 10
+    res = [GridResource(1, prefix_ratio=CP / N, elements=[GridElement(ElementType.DATA, U)])]
+    struct = [SymbolSection(4, [0])]
+    return OFDMWaveform(grid_resources=res, grid_structure=struct, num_subcarriers=N, modulation_order=16,
+                        dc_suppression=dc, pilot_section=pilot)
+
+
+def make_sync() -> None:
+    from hermespy.modem.waveforms.orthogonal.ofdm import (
+        OFDMCorrelationSynchronization,
+        SchmidlCoxPilotSection,
+        SchmidlCoxSynchronization,
+    )
+    from hermespy.modem.waveforms.orthogonal.waveform import PilotSection
+
+    out = {}
+    for dc in (True, False):
+        out[f"schmidl_cox_pilot_dc{int(dc)}"] = sync_waveform(dc, SchmidlCoxPilotSection()).pilot_section.generate(1)
+        out[f"plain_pilot_dc{int(dc)}"] = sync_waveform(dc, PilotSection()).pilot_section.generate(1)
+    rng = np.random.default_rng(11)
+    cases = (("sc", SchmidlCoxPilotSection, SchmidlCoxSynchronization, (37, 700), 0.05),
+             ("sc3", SchmidlCoxPilotSection, SchmidlCoxSynchronization, (0, 650, 1400), 0.2),
+             ("corr", PilotSection, OFDMCorrelationSynchronization, (53, 760), 0.05),
+             ("corr3", PilotSection, OFDMCorrelationSynchronization, (5, 640, 1290), 0.2))
+    for name, section, routine, starts, noise in cases:
+        wf = sync_waveform(True, section())
+        spf = wf.samples_per_frame(1.0, 1)
+        n = starts[-1] + spf + 80
+        signal = np.zeros((2, n), dtype=np.complex128)
+        for s0 in starts:
+            bits = rng.integers(0, 2, wf.bits_per_frame(), dtype=np.uint8)
+            frame = wf.modulate(wf.place(wf.map(bits)), 1.0, 1)
+            signal[0, s0:s0 + spf] += frame
+            signal[1, s0:s0 + spf] += 0.6j * frame
+        signal += noise * (rng.standard_normal(signal.shape) + 1j * rng.standard_normal(signal.shape))
+        signal = signal.astype(np.complex64).astype(np.complex128)  # representable in the engine's complex64
+        sync = routine()
+        sync.waveform = wf
+        out[f"{name}_signal"] = signal
+        out[f"{name}_starts"] = np.asarray(starts)
+        out[f"{name}_indices"] = np.asarray(sync.synchronize(signal, 1.0, 1), dtype=np.int64)
+    save("sync.npz", **out)
+
+
 MAKERS = {"qam": make_qam, "ofdm": make_ofdm, "fading": make_fading, "ls": make_ls, "ideal": make_ideal,
-          "zf": make_zf, "ber": make_ber, "drops": make_drops, "presets": make_presets}
+          "zf": make_zf, "ber": make_ber, "drops": make_drops, "presets": make_presets,
+          "sync": make_sync}
 
 if __name__ == "__main__":
     for name, maker in MAKERS.items():
