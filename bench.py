@@ -457,11 +457,61 @@ def bench_estimators(ctx, spec, args):
                             "ber": r["ber"], "nmse_db": nm[name]}
     sel = results[selected]
     launches = {"learned": 4 + 1 + 8 * ((drops + chunk - 1) // chunk) + 1, "lmmse": 5, "ls": 6}[selected]
-    extra = {"comparison": comparison, "estimator_policy": {
+    extra = {"synchronization": sync_report(ctx, args), "comparison": comparison, "estimator_policy": {
         "selected": selected, "rule": "learned if its validation NMSE <= LMMSE NMSE + 0.5 dB, else LMMSE",
         "validation_drops": nval}, "weights": os.path.relpath(wpath, ROOT)}
     return {"drops": drops, "total_ms": sel["total_ms"], "stage_ms": sel["stage_ms"], "work": work,
             "ber": sel["ber"], "e2e_s": e2e_s, "h2d": hb, "d2h": db, "launches": launches, "extra": extra}
+
+
+def sync_report(ctx, args, signals: int = 2048, slack: int = 256) -> dict:
+    """Schmidl-Cox frame synchronization of the workload frame with a preamble:
+    `signals` received 4-antenna signals (random frame start in [0, slack), AWGN at
+    10 dB SNR) per step through the delay-metric and peak-search kernels."""
+
+    torch, hg, _lib = ctx["torch"], ctx["hg"], ctx["lib"]
+    from hermespy_gb300.train_estimator import pilot_waveform
+
+    dev, sp = ctx["dev"], ctx["sp"]
+    wf = pilot_waveform()
+    wf.pilot_section = hg.SchmidlCoxPilotSection()
+    sc = hg.SchmidlCoxSynchronization(wf)
+    spf, L, S = wf.samples_per_frame(), wf.num_subcarriers, 4
+    n = spf + slack
+    g = torch.Generator(device=dev).manual_seed(SEED)
+    data = torch.randn((signals * S, wf.num_data_symbols), dtype=torch.complex64, device=dev, generator=g)
+    frames = wf.modulate_data_device(data).reshape(signals, S, spf)
+    offsets = ctx["rng"].integers(0, slack, size=signals)
+    x = torch.zeros((signals, S, n), dtype=torch.complex64, device=dev)
+    for b in range(signals):
+        x[b, :, offsets[b]:offsets[b] + spf] = frames[b]
+    p = torch.full((signals,), 0.1, dtype=torch.float32, device=dev)
+    _lib.call("hpx_awgn_add", _lib.ptr(x), signals, S, n, _lib.ptr(p), SEED, 1 << 40, sp)
+    nm = n - L + 2
+    metric = torch.empty((signals, nm), dtype=torch.float64, device=dev)
+    starts = torch.empty((signals, 64), dtype=torch.int64, device=dev)
+    counts = torch.empty(signals, dtype=torch.int32, device=dev)
+    calls = [("sync_metric", lambda: _lib.call("hpx_sync_schmidl_cox", _lib.ptr(x), signals, S, n, L, _lib.ptr(metric),
+                                               sp)),
+             ("sync_peaks", lambda: _lib.call("hpx_sync_peaks", _lib.ptr(metric), signals, nm, 0, 0.75,
+                                              int(0.9 * spf), -1, 0, 0, 0, 64, _lib.ptr(starts), _lib.ptr(counts), sp))]
+    total_ms, stage_ms = ctx["timer"].run(lambda d0, ev: staged(calls, ev, ctx["stream"]),
+                                          [c for c, _ in calls], args.steps, args.warmup, 0, 0)
+    c = counts.cpu().numpy()
+    found = starts[:, 0].cpu().numpy()
+    exact = float(np.mean((c == 1) & (np.abs(found - offsets) <= 3)))
+    single = sc.synchronize_batch(x[:4])  # the public API on a few signals (same kernels)
+    pk = peaks()
+    ms = total_ms / args.steps
+    mbytes = signals * (S * n * 8 + nm * 8)
+    mms = stage_ms["sync_metric"] / args.steps
+    return {"signals_per_step": signals, "streams": S, "samples_per_signal": n, "ms_per_step": round(ms, 4),
+            "frames_per_s": signals / (ms / 1e3),
+            "stages_ms": {k: round(v / args.steps, 4) for k, v in stage_ms.items()},
+            "metric_kernel": {"bound": "hbm", "algorithmic_bytes": mbytes, "achieved_gbs": round(mbytes / mms / 1e6, 1),
+                              "frac": round(mbytes / mms / 1e6 / pk["hbm_gbs"], 4)},
+            "detected_within_3_samples": exact, "api_check": [v[:1] for v in single],
+            "true_starts_of_api_check": offsets[:4].tolist()}
 
 
 def bench_massive(ctx, spec, args):

@@ -110,6 +110,8 @@ _SIGNATURES = {
     "hpx_awgn_add": [c_void_p, c_int32, c_int32, c_int64, c_void_p, c_uint64, c_int64, c_void_p],
     "hpx_sync_schmidl_cox": [c_void_p, c_int32, c_int32, c_int64, c_int32, c_void_p, c_void_p],
     "hpx_sync_correlation": [c_void_p, c_int32, c_int32, c_int64, c_void_p, c_int32, c_void_p, c_void_p],
+    "hpx_sync_peaks": [c_void_p, c_int32, c_int64, c_int32, ctypes.c_double, c_int64, c_int64, c_int32, c_int64,
+                       c_int64, c_int32, c_void_p, c_void_p, c_void_p],
     "hpx_link_workspace_bytes": [c_void_p, c_void_p, c_int32, ctypes.POINTER(c_int64)],
     "hpx_link_create": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, ctypes.POINTER(c_void_p)],
     "hpx_link_destroy": [c_void_p],

@@ -3,20 +3,52 @@
 Mirrors ``Synchronization`` (modem/waveform.py:30-108), the OFDM Schmidl-Cox
 routine (modem/waveforms/orthogonal/ofdm.py:208-257) and the pilot-correlation
 routine (modem/waveform_correlation_synchronization.py:27-186). The metric over
-every candidate delay — the part whose cost grows with the signal length times the
-symbol (or pilot) length — runs in the ``hpx_sync_*`` kernels; the peak search on
-the FP64 metric is the reference's own ``scipy.signal.find_peaks`` call with the
-same height and distance rules, on the host.
+every candidate delay and the ``scipy.signal.find_peaks`` search the reference
+runs on it (same height and distance rules, plateau midpoints, index offsets and
+clipping) both run on the GPU (``hpx_sync_schmidl_cox`` / ``hpx_sync_correlation``
+then ``hpx_sync_peaks``); only the frame start indices come back to the host. The
+``*_batch`` methods synchronize many received signals in one launch each.
 """
 
 from __future__ import annotations
 
 import numpy as np
 import torch
-from scipy.signal import find_peaks
 
 from . import _lib
 from .containers import Signal, to_device
+
+MAX_FRAMES = 64  # frame starts returned per signal
+
+
+def _peaks(metric: torch.Tensor, normalize: bool, height: float, distance: int, offset: int, clip: bool = False,
+           clip_max: int = 0, clip_value: int = 0, max_frames: int = MAX_FRAMES) -> list[list[int]]:
+    """Device find_peaks over each row of ``metric`` (batch, length)."""
+
+    metric = metric.contiguous()
+    batch, length = metric.shape
+    starts = torch.empty((batch, max_frames), dtype=torch.int64, device=metric.device)
+    counts = torch.empty(batch, dtype=torch.int32, device=metric.device)
+    _lib.call("hpx_sync_peaks", _lib.ptr(metric), batch, length, int(normalize), float(height), int(distance),
+              int(offset), int(clip), int(clip_max), int(clip_value), max_frames, _lib.ptr(starts), _lib.ptr(counts),
+              _lib.stream_ptr())
+    c = counts.cpu().numpy()
+    if np.any(c < 0):
+        raise RuntimeError("synchronization: more than 512 candidate peaks above the detection height")
+    if np.any(c > max_frames):
+        raise RuntimeError(f"synchronization: more than {max_frames} frames in one signal")
+    st = starts.cpu().numpy()
+    return [st[b, : c[b]].tolist() for b in range(batch)]
+
+
+def _batch_tensor(signals) -> torch.Tensor:
+    t = signals if isinstance(signals, torch.Tensor) else to_device(signals)
+    t = t.to(torch.complex64)
+    if t.ndim == 2:
+        t = t[:, None, :]
+    if t.ndim != 3:
+        raise ValueError("batched synchronization expects (signals, streams, samples)")
+    return t.contiguous()
 
 
 def _signal_tensor(signal) -> torch.Tensor:
@@ -68,26 +100,33 @@ class SchmidlCoxSynchronization(OFDMSynchronization):
     Needs a ``SchmidlCoxPilotSection`` on the waveform (ofdm.py:214-257).
     """
 
-    def metric_device(self, signal, bandwidth: float = 1.0, oversampling_factor: int = 1) -> torch.Tensor:
-        """The reference's ``delay_powers`` vector (leading zero included) on the GPU."""
+    def metric_batch(self, signals, bandwidth: float = 1.0, oversampling_factor: int = 1) -> torch.Tensor:
+        """``delay_powers`` (leading zero included) of (signals, streams, samples) on the GPU."""
 
         wf = self._require_waveform()
-        x = _signal_tensor(signal)
+        x = _batch_tensor(signals)
         L = oversampling_factor * wf.num_subcarriers
-        n = x.shape[1]
-        out = torch.empty(max(n - L + 2, 0), dtype=torch.float64, device=x.device)
+        B, S, n = x.shape
+        out = torch.empty((B, max(n - L + 2, 0)), dtype=torch.float64, device=x.device)
         if n >= L:
-            _lib.call("hpx_sync_schmidl_cox", _lib.ptr(x), 1, x.shape[0], n, L, _lib.ptr(out), _lib.stream_ptr())
+            _lib.call("hpx_sync_schmidl_cox", _lib.ptr(x), B, S, n, L, _lib.ptr(out), _lib.stream_ptr())
         return out
 
-    def synchronize(self, signal, bandwidth: float = 1.0, oversampling_factor: int = 1) -> list[int]:
+    def metric_device(self, signal, bandwidth: float = 1.0, oversampling_factor: int = 1) -> torch.Tensor:
+        """The reference's ``delay_powers`` vector of one signal on the GPU."""
+
+        return self.metric_batch(_signal_tensor(signal)[None], bandwidth, oversampling_factor)[0]
+
+    def synchronize_batch(self, signals, bandwidth: float = 1.0, oversampling_factor: int = 1) -> list[list[int]]:
         wf = self._require_waveform()
-        if _signal_tensor(signal).shape[1] < oversampling_factor * wf.num_subcarriers:
-            return []
-        powers = self.metric_device(signal, bandwidth, oversampling_factor).cpu().numpy()
+        x = _batch_tensor(signals)
+        if x.shape[2] < oversampling_factor * wf.num_subcarriers:
+            return [[] for _ in range(x.shape[0])]
         spf = wf.samples_per_frame(bandwidth, oversampling_factor)
-        peaks, _ = find_peaks(powers, distance=int(0.9 * spf), height=0.75 * np.max(powers))
-        return (peaks - 1).tolist()
+        return _peaks(self.metric_batch(x, bandwidth, oversampling_factor), False, 0.75, int(0.9 * spf), -1)
+
+    def synchronize(self, signal, bandwidth: float = 1.0, oversampling_factor: int = 1) -> list[int]:
+        return self.synchronize_batch(_signal_tensor(signal)[None], bandwidth, oversampling_factor)[0]
 
 
 class CorrelationSynchronization(Synchronization):
@@ -125,37 +164,40 @@ class CorrelationSynchronization(Synchronization):
             raise ValueError("Synchronization guard ratio must be between zero and one.")
         self._guard_ratio = float(value)
 
-    def correlation_device(self, signal, bandwidth: float = 1.0, oversampling_factor: int = 1) -> torch.Tensor:
-        """Un-normalized correlation profile (length samples + pilot - 1) on the GPU."""
-
+    def _pilot(self, bandwidth: float, oversampling_factor: int) -> torch.Tensor:
         wf = self._require_waveform()
-        x = _signal_tensor(signal)
         pilot = wf.pilot_signal(bandwidth, oversampling_factor).device_samples.reshape(-1).contiguous()
         if pilot.numel() < 1:
             raise RuntimeError("No pilot sequence configured, time-domain correlation synchronization impossible")
-        n = x.shape[1]
-        out = torch.empty(n + pilot.numel() - 1, dtype=torch.float64, device=x.device)
-        _lib.call("hpx_sync_correlation", _lib.ptr(x), 1, x.shape[0], n, _lib.ptr(pilot), pilot.numel(),
-                  _lib.ptr(out), _lib.stream_ptr())
+        return pilot
+
+    def correlation_batch(self, signals, bandwidth: float = 1.0, oversampling_factor: int = 1) -> torch.Tensor:
+        """Un-normalized correlation profiles (signals, samples + pilot - 1) on the GPU."""
+
+        x = _batch_tensor(signals)
+        pilot = self._pilot(bandwidth, oversampling_factor)
+        B, S, n = x.shape
+        out = torch.empty((B, n + pilot.numel() - 1), dtype=torch.float64, device=x.device)
+        _lib.call("hpx_sync_correlation", _lib.ptr(x), B, S, n, _lib.ptr(pilot), pilot.numel(), _lib.ptr(out),
+                  _lib.stream_ptr())
         return out
 
-    def synchronize(self, signal, bandwidth: float = 1.0, oversampling_factor: int = 1) -> list[int]:
+    def correlation_device(self, signal, bandwidth: float = 1.0, oversampling_factor: int = 1) -> torch.Tensor:
+        return self.correlation_batch(_signal_tensor(signal)[None], bandwidth, oversampling_factor)[0]
+
+    def synchronize_batch(self, signals, bandwidth: float = 1.0, oversampling_factor: int = 1) -> list[list[int]]:
         wf = self._require_waveform()
-        x = _signal_tensor(signal)
+        x = _batch_tensor(signals)
         if x.numel() < 1:
-            return []
-        correlation = self.correlation_device(x, bandwidth, oversampling_factor).cpu().numpy()
-        correlation /= correlation.max()
+            return [[] for _ in range(x.shape[0])]
         frame_length = wf.samples_per_frame(bandwidth, oversampling_factor)
-        indices, _ = find_peaks(np.abs(correlation), height=0.9, distance=int(0.8 * frame_length))
-        if len(indices) < 1:
-            return []
-        pilot_length = wf.pilot_signal(bandwidth, oversampling_factor).num_samples
-        indices = indices - (pilot_length - 1)
-        indices = np.where(indices < 0, 0, indices)
-        n = x.shape[1]
-        indices = np.where(indices > (n - frame_length), abs(n - frame_length), indices)
-        return indices.tolist()
+        pilot_length = self._pilot(bandwidth, oversampling_factor).numel()
+        n = x.shape[2]
+        return _peaks(self.correlation_batch(x, bandwidth, oversampling_factor), True, 0.9, int(0.8 * frame_length),
+                      1 - pilot_length, True, n - frame_length, abs(n - frame_length))
+
+    def synchronize(self, signal, bandwidth: float = 1.0, oversampling_factor: int = 1) -> list[int]:
+        return self.synchronize_batch(_signal_tensor(signal)[None], bandwidth, oversampling_factor)[0]
 
 
 class OFDMCorrelationSynchronization(CorrelationSynchronization):

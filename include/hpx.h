@@ -376,6 +376,18 @@ hpx_status hpx_sync_schmidl_cox(const hpx_cf32* signal, int32_t batch, int32_t n
 hpx_status hpx_sync_correlation(const hpx_cf32* signal, int32_t batch, int32_t num_streams, int64_t num_samples,
                                 const hpx_cf32* pilot, int32_t pilot_length, double* correlation, void* stream);
 
+/* Frame starts from `batch` metrics of `length` doubles (either output above), the
+ * peak search of scipy.signal.find_peaks(x, height, distance) as the two routines
+ * call it: local maxima (plateau midpoints), height >= height * max(x) (or, with
+ * normalize, x / max(x) >= height), then distance suppression by decreasing height.
+ * Kept peaks in index order, plus `offset` (Schmidl-Cox: -1; correlation: 1 - P),
+ * optionally clipped (negative -> 0, above clip_max -> clip_value) go to
+ * starts[b][0 .. max_frames); counts[b] = number kept, -1 if more than 512 peaks
+ * passed the height test. */
+hpx_status hpx_sync_peaks(const double* metric, int32_t batch, int64_t length, int32_t normalize, double height,
+                          int64_t distance, int64_t offset, int32_t clip, int64_t clip_max, int64_t clip_value,
+                          int32_t max_frames, int64_t* starts, int32_t* counts, void* stream);
+
 /* ------------------------------------------------------- batched drop loop */
 
 enum { HPX_EST_IDEAL = 0, HPX_EST_LS = 1 };

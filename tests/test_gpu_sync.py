@@ -115,3 +115,43 @@ def test_default_and_floating_synchronization():
         OFDMCorrelationSynchronization(waveform=wf).synchronize(np.ones((1, 300), np.complex64))
     with pytest.raises(ValueError):
         OFDMCorrelationSynchronization(threshold=1.5)
+
+
+@pytest.mark.parametrize("normalize", [False, True])
+def test_device_peaks_match_find_peaks(normalize):
+    """hpx_sync_peaks against scipy.signal.find_peaks on metrics with plateaus
+    (runs of equal samples) and several frames. Distinct peaks have distinct
+    heights: for exact ties numpy's argsort order is platform dependent."""
+
+    from scipy.signal import find_peaks
+
+    rng = np.random.default_rng(21)
+    height = 0.9 if normalize else 0.75
+    rows = []
+    t = np.arange(3000)
+    for _ in range(6):
+        x = np.zeros(3000)
+        for c in rng.choice(np.arange(200, 2800), 3, replace=False):
+            x += np.maximum(0.0, 1.0 - np.abs(t - c) / 200.0) * rng.uniform(0.8, 1.0)
+        x = x + 0.05 * rng.standard_normal(3000)
+        for i in rng.choice(np.arange(1, 2990), 60, replace=False):  # plateaus of 2-5 equal samples
+            x[i:i + rng.integers(2, 6)] = x[i]
+        x[1500:1504] = x.max() * 1.01  # a flat top
+        rows.append(x)
+    metric = torch.from_numpy(np.stack(rows)).cuda()
+    from hermespy_gb300.synchronization import _peaks
+
+    for distance in (1, 7, 400):
+        got = _peaks(metric, normalize, height, distance, -1, max_frames=512)
+        for b, x in enumerate(rows):
+            h = x / x.max() if normalize else x
+            ref, _ = find_peaks(h, height=height if normalize else height * x.max(), distance=distance)
+            assert got[b] == (ref - 1).tolist(), (b, distance)
+
+
+def test_batched_synchronize_matches_single(golden):
+    g = golden("sync.npz")
+    wf = _waveform(True, SchmidlCoxPilotSection())
+    sc = SchmidlCoxSynchronization(wf)
+    a, b = g["sc_signal"], g["sc3_signal"][:, : g["sc_signal"].shape[1]]
+    assert sc.synchronize_batch(np.stack([a, b])) == [sc.synchronize(a), sc.synchronize(b)]
