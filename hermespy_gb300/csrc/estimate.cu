@@ -250,6 +250,7 @@ void release(hpx_lmmse* e) {
   void* p[] = {e->d_delay, e->d_pw_word, e->d_pw_count, e->d_pw_off, e->d_pcol, e->d_G, e->d_E, e->d_R, e->d_r, e->d_np};
   for (void* q : p)
     if (q) cudaFree(q);
+  lmmse_tc_release(e);
   delete e;
 }
 
@@ -390,6 +391,13 @@ hpx_status hpx_lmmse_create(const hpx_frame* frame, const hpx_fading* fading, in
       (err = upload(&e->d_r, rw)) != cudaSuccess || (err = upload(&e->d_np, np_stream)) != cudaSuccess) {
     release(e);
     return hpx_cuda_status(err, "lmmse tables");
+  }
+  if (ntx == 4 && 2 * U <= 128) {  // the 4 x 4 receiver's tensor-core path
+    const hpx_status st = lmmse_tc_prepare(e, delays);
+    if (st != HPX_OK) {
+      release(e);
+      return st;
+    }
   }
   *out = e;
   return HPX_OK;

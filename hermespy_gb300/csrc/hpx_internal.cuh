@@ -201,7 +201,20 @@ struct hpx_lmmse {
   float* d_R = nullptr;           // [U][P][P]
   float* d_r = nullptr;           // [U][W][P]
   int32_t* d_np = nullptr;        // [ntx] pilot words per stream
+  // tensor-core receiver of the 4 x 4 link (lmmse_tc.cu)
+  int tc_KP = 0, tc_mtiles = 0, tc_nwl = 0, tc_ws_drops = 0;
+  uint16_t* d_tc_ftab = nullptr;   // [mtiles][2][128 x KP] FP16 twiddle operand (hi, lo)
+  int32_t* d_tc_wlist = nullptr;   // [nwl] data words, -1 padding
+  int32_t* d_tc_kfirst = nullptr;  // [W][mtiles] first data element of row w in the tile
+  uint16_t* d_tc_bop = nullptr;    // [tc_ws_drops][passes][2][128 x KP] FP16 gains operand
+  float* d_tc_scale = nullptr;     // [tc_ws_drops]
+  int* d_tc_fail = nullptr;        // set if a tensor-core wait timed out (later CTAs skip)
 };
+constexpr int kLmmseTcChunk = 2048;  // drops per gains/GEMM launch pair
+hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays);
+void lmmse_tc_release(hpx_lmmse* e);
+hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int gcols, const float* nv,
+                           uint64_t seed, int64_t drop0, int B, uint32_t* errors, cudaStream_t s);
 
 // Per-drop realization state, read by the kernels.
 struct FadingView {

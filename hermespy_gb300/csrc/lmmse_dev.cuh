@@ -44,20 +44,42 @@ __device__ __forceinline__ void lmmse_drop_taps(const LmmseView& e, int b, int n
   const int np = e.np;  // every stream has the same pilot words (checked at create time)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int u = threadIdx.x; u < U; u += blockDim.x) ds[u] = e.delay[u];
-  for (int q = warp; q < NP * np * U; q += nwarps) {
-    const int pair = q / (np * U), rem = q - pair * np * U, p = rem / U, u = rem - p * U;
+  // One warp per (pair, pilot word): the word's received pilots stay in registers
+  // (lane holds pilots lane + 32 j, up to 256 per pass over the row) while the
+  // warp walks the U rows of the weighted-LS matrix.
+  constexpr int YR = 8;
+  for (int q = warp; q < NP * np; q += nwarps) {
+    const int pair = q / np, p = q - pair * np;
     const int t = pair % ntx, r = pair / ntx;
     const int word = e.pw_word[t * P + p], cnt = e.pw_count[t * P + p], off = e.pw_off[t * P + p];
-    const float2* grow = e.G + (int64_t)off * U + (int64_t)u * cnt;
     const float2* yw = grid + (((int64_t)b * nrx + r) * W + word) * gcols;
-    float2 acc = make_float2(0.f, 0.f);
-    for (int k = lane; k < cnt; k += 32) cfma(acc, grow[k], yw[e.pcol[off + k]]);
+    const float2* Gp = e.G + (int64_t)off * U;
+    for (int k0 = 0; k0 < cnt; k0 += 32 * YR) {
+      float2 yv[YR];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
-      acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+      for (int j = 0; j < YR; ++j) {
+        const int k = k0 + lane + 32 * j;
+        yv[j] = k < cnt ? yw[e.pcol[off + k]] : make_float2(0.f, 0.f);
+      }
+      for (int u = 0; u < U; ++u) {
+        const float2* grow = Gp + (int64_t)u * cnt;
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < YR; ++j) {
+          const int k = k0 + lane + 32 * j;
+          if (k < cnt) cfma(acc, grow[k], yv[j]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+          acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+        }
+        if (lane == 0) {
+          float2* dst = gls + (pair * np + p) * U + u;
+          *dst = k0 == 0 ? acc : cadd(*dst, acc);
+        }
+      }
     }
-    if (lane == 0) gls[(pair * np + p) * U + u] = acc;
   }
   for (int q = threadIdx.x; q < ntx * U; q += blockDim.x) {
     const int t = q / U, u = q - t * U;

@@ -1,0 +1,380 @@
+// Fused tap-domain LMMSE receiver of the 4 x 4 pilot-comb link on the tcgen05
+// tensor cores.
+//
+// The per-element channel of every antenna pair is a tap DFT,
+//   H[w][c][pair] = sum_u g[w][u][pair] exp(-2 pi i bin(c) d_u / N),
+// i.e. for one drop a GEMM of (subcarriers x 2U) twiddles by (2U x words*pairs*{re,im})
+// gains: [Re H | Im H] = [F_re | F_im] [[G_re, G_im], [-G_im, G_re]]. It runs in two
+// kernels per chunk of drops:
+//   k_lmmse_gains  (one CTA per drop): pilot LS, per-tap LMMSE over the words and
+//                  the gains of every word and pair (lmmse_drop_taps), written to a
+//                  workspace as the GEMM's FP16 (hi, lo) operand in its shared-memory
+//                  layout, scaled by a power of two bounding them by 1;
+//   k_lmmse_tc     (one CTA per drop and 128 subcarriers): the GEMM as FP16 MMAs
+//                  with FP32 accumulation in tensor memory, operands split
+//                  x = hi + lo and multiplied hi*hi + hi*lo + lo*hi (~2^-22 of the
+//                  largest term), four words (128 accumulator columns) per pass;
+//                  then every thread owns one subcarrier (its TMEM lane), reads a
+//                  word's 16 complex gains with one tcgen05.ld, equalizes (LMMSE /
+//                  ZF, Cholesky), demaps and counts bit errors against the
+//                  regenerated Philox bits.
+// The twiddle operand (hi, lo) of each 128-subcarrier tile is built once at
+// handle creation. Other antenna configurations use the FP32 kernel in detect.cu.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "equalize_dev.cuh"
+#include "lmmse_dev.cuh"
+#include "tcgen05.cuh"
+
+namespace {
+
+constexpr int TC_THREADS = 256;   // 8 warps: 4 lane quarters x 2 word slots
+constexpr int TC_M = 128;         // subcarriers per CTA (TMEM lanes)
+constexpr int TC_WORDS = 4;       // words per pass: 4 x 16 pairs x {re, im} = 128 columns
+constexpr int TC_N = TC_WORDS * 32;
+constexpr int TC_BITBLK = 10;     // Philox blocks staged per (word slot, stream)
+constexpr int TC_NP = 16;         // antenna pairs (4 x 4)
+constexpr long long TC_WAIT = 40ll * 1000 * 1000;  // cycles (~20 ms) before a wait gives up
+
+struct TcView {
+  int W, FC, U, KP, mtiles, nwl, m;
+  const int32_t* wlist;   // [nwl] data words, -1 padding
+  const int32_t* kfirst;  // [W][mtiles] first data element of row w in tile, -1: none
+  const int8_t* kind;     // [W][FC]
+  const int32_t* index;   // [W][FC]
+  const uint16_t* ftab;   // [mtiles][2][TC_M x KP] K-major FP16 (hi, lo)
+  const uint16_t* bop;    // [drops][passes][2][TC_M x KP] FP16 gains operand (hi, lo)
+  const float* scale;     // [drops]
+};
+
+// ------------------------------------------------------------ kernel 1: gains
+// Writes, per pass of four data words, the FP16 (hi, lo) gains operand of the
+// GEMM in its K-major shared-memory layout: row n = slot * 32 + q (q < 16: Re H of
+// pair q, else Im H of pair q - 16), k < U: the coefficient of Re F (G_re or G_im),
+// U <= k < 2U: of Im F (-G_im or G_re), scaled by a power of two bounding the
+// drop's gains by 1.
+__global__ void __launch_bounds__(512, 2) k_lmmse_gains(LmmseView e, const float2* __restrict__ grid, int gcols,
+                                                         const float* __restrict__ nv, const int32_t* __restrict__ wlist,
+                                                         int nwl, int KP, uint16_t* __restrict__ bop,
+                                                         float* __restrict__ scale_ws) {
+  extern __shared__ float4 smem4[];
+  __shared__ float red[16];
+  __shared__ float sscale;
+  const int b = blockIdx.x;
+  const int W = e.W, U = e.U;
+  float2* gt = reinterpret_cast<float2*>(smem4);
+  float2* gls = gt + (size_t)W * U * TC_NP;
+  float* cw = reinterpret_cast<float*>(gls + TC_NP * e.np * U);
+  int* ds = reinterpret_cast<int*>(cw + (size_t)e.ntx * U * W * e.np);
+  const float s2 = nv ? nv[b] : 0.0f;
+  lmmse_drop_taps<TC_NP>(e, b, 4, grid, gcols, s2, gt, gls, cw, ds);  // ends with __syncthreads
+  const float* g = reinterpret_cast<const float*>(gt);  // [W][U][32]
+  float mx = 0.0f;
+  for (int i = threadIdx.x; i < W * U * 2 * TC_NP; i += blockDim.x) mx = fmaxf(mx, fabsf(g[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+    int ex = 0;
+    frexpf(m, &ex);  // m < 2^ex
+    sscale = (m > 0.0f && isfinite(m)) ? ldexpf(1.0f, ex) : 1.0f;
+    scale_ws[b] = sscale;
+  }
+  __syncthreads();
+  const float inv = 1.0f / sscale;
+  const int kg = KP / 8;
+  const size_t opel = (size_t)TC_M * KP;  // halves per operand
+  uint16_t* dst = bop + (size_t)b * (nwl / TC_WORDS) * 2 * opel;
+  for (int it = threadIdx.x; it < nwl * 32 * kg; it += blockDim.x) {
+    const int row = it / kg, gk = it - row * kg;  // row over all words: pass = row / 128
+    const int pass = row / TC_N, n = row - pass * TC_N;
+    const int s = n >> 5, q = n & 31;
+    const int w = wlist[pass * TC_WORDS + s];
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int k = gk * 8 + j;
+      float val = 0.0f;
+      if (w >= 0) {
+        if (k < U) {
+          val = g[((size_t)w * U + k) * 32 + q];
+        } else if (k < 2 * U) {
+          const float* rw = g + ((size_t)w * U + (k - U)) * 32;
+          val = q < 16 ? -rw[q + 16] : rw[q - 16];
+        }
+      }
+      val *= inv;
+      const __half h = __float2half_rn(val);
+      const __half l = __float2half_rn(val - __half2float(h));
+      const uint32_t hb = __half_as_ushort(h), lb = __half_as_ushort(l);
+      if (j & 1) {
+        hw[j >> 1] |= hb << 16;
+        lw[j >> 1] |= lb << 16;
+      } else {
+        hw[j >> 1] = hb;
+        lw[j >> 1] = lb;
+      }
+    }
+    uint16_t* base = dst + (size_t)pass * 2 * opel;
+    const uint32_t off = tc::kmajor_offset(n, gk * 8, KP) / 2;
+    *reinterpret_cast<uint4*>(base + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4*>(base + opel + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+  }
+}
+
+// ------------------------------------------------------- kernel 2: GEMM + detect
+__global__ void __launch_bounds__(TC_THREADS, 2) k_lmmse_tc(TcView v, int W, const float2* __restrict__ grid,
+                                                             int gcols, const float* __restrict__ nv,
+                                                             const __grid_constant__ QamDemapTable qt, int mode,
+                                                             uint64_t seed, int64_t drop0,
+                                                             uint32_t* __restrict__ errors, int* fail) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  const int mt = blockIdx.x, b = blockIdx.y;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int KP = v.KP, m = v.m;
+  const uint32_t opbytes = (uint32_t)TC_M * KP * 2;  // one 128-row FP16 operand
+  unsigned char* a_hi = sm;
+  unsigned char* a_lo = sm + opbytes;
+  unsigned char* b_hi = sm + 2 * opbytes;
+  unsigned char* b_lo = sm + 3 * opbytes;
+  uint32_t* bits = reinterpret_cast<uint32_t*>(sm + 4 * opbytes);  // [4 slots][4 streams][TC_BITBLK * 4]
+
+  __shared__ int skip;
+  if (tid == 0) skip = *(volatile int*)fail;
+  __syncthreads();
+  if (skip) {  // an earlier CTA timed out on the tensor core: flag and leave
+    if (tid == 0) atomicOr(errors + b, 0x80000000u);
+    return;
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_slot, TC_N);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) tc::mbar_init(&mbar, 1);
+  // twiddle operand of this tile
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(v.ftab + (size_t)mt * 2 * TC_M * KP);
+    uint4* dst = reinterpret_cast<uint4*>(a_hi);
+    for (int i = tid; i < (int)(2 * opbytes / 16); i += TC_THREADS) dst[i] = src[i];
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  const float scl = v.scale[b];
+  const float s2 = nv ? nv[b] : 0.0f;
+  const int c0 = mt * TC_M;
+  const unsigned char* bop = reinterpret_cast<const unsigned char*>(v.bop) + (size_t)b * (v.nwl / TC_WORDS) * 2 * opbytes;
+  bool ok = true;
+  unsigned int local = 0;
+  const uint32_t idesc = tc::idesc_f16_f32(TC_M, TC_N);
+  const int npass = v.nwl / TC_WORDS;
+  for (int p = 0; p < npass; ++p) {
+    if (p > 0) __syncthreads();  // every thread is done with the previous pass's bits
+    // ---- the pass's gains operand (hi, lo), prepared by k_lmmse_gains
+    {
+      const uint4* src = reinterpret_cast<const uint4*>(bop + (size_t)p * 2 * opbytes);
+      uint4* dst = reinterpret_cast<uint4*>(b_hi);
+      for (int i = tid; i < (int)(2 * opbytes / 16); i += TC_THREADS) dst[i] = src[i];
+    }
+    // ---- Philox bits of the elements of the pass's rows in this tile
+    for (int it = tid; it < TC_WORDS * 4 * TC_BITBLK; it += TC_THREADS) {
+      const int s = it / (4 * TC_BITBLK), r = it - s * 4 * TC_BITBLK;
+      const int t = r / TC_BITBLK, j = r - t * TC_BITBLK;
+      const int w = v.wlist[p * TC_WORDS + s];
+      const int kf = w >= 0 ? v.kfirst[w * v.mtiles + mt] : -1;
+      uint4 blk = make_uint4(0u, 0u, 0u, 0u);
+      if (kf >= 0) {
+        const int64_t blk0 = ((int64_t)kf * m) >> 7;
+        blk = hpx_random_block(seed, drop0 + b, (uint32_t)t, HPX_DOMAIN_BITS, (uint32_t)(blk0 + j));
+      }
+      *reinterpret_cast<uint4*>(bits + (size_t)(s * 4 + t) * TC_BITBLK * 4 + j * 4) = blk;
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();  // operands written; previous pass's TMEM reads done
+    tc::fence_after_sync();
+    if (tid == 0) {
+      for (int ks = 0; ks < KP / 16; ++ks) {
+        const uint32_t koff = (uint32_t)ks * 256;  // two core matrices along K
+        const uint64_t ah = tc::smem_desc(a_hi + koff, 128, KP * 16), al = tc::smem_desc(a_lo + koff, 128, KP * 16);
+        const uint64_t bh = tc::smem_desc(b_hi + koff, 128, KP * 16), bl = tc::smem_desc(b_lo + koff, 128, KP * 16);
+        tc::mma_f16(tmem, ah, bh, idesc, ks > 0);
+        tc::mma_f16(tmem, ah, bl, idesc, true);
+        tc::mma_f16(tmem, al, bh, idesc, true);
+      }
+      tc::mma_commit(&mbar);
+    }
+    ok = ok && tc::mbar_wait(&mbar, (uint32_t)(p & 1), TC_WAIT);
+    tc::fence_after_sync();
+    // ---- epilogue: thread = subcarrier (TMEM lane), two word slots per warp
+    const int qtr = warp & 3;
+    const int c = c0 + qtr * 32 + lane;
+#pragma unroll 1
+    for (int s = warp >> 2; s < TC_WORDS; s += 2) {
+      float acc[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(qtr * 32) << 16) + (uint32_t)(s * 32), acc);
+      const int w = v.wlist[p * TC_WORDS + s];
+      if (!ok || w < 0 || c >= v.FC) continue;
+      if (v.kind[w * v.FC + c] != HPX_RE_DATA) continue;
+      const int k = v.index[w * v.FC + c];
+      float2 H[4][4], y[4], x[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        y[r] = grid[(((int64_t)b * 4 + r) * W + w) * gcols + c];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) H[r][t] = make_float2(acc[r * 4 + t] * scl, acc[16 + r * 4 + t] * scl);
+      }
+      equalize_one<4, 4>(mode, H, y, s2, x);
+      const int kf = v.kfirst[w * v.mtiles + mt];
+      const int64_t pos = (int64_t)k * m - ((((int64_t)kf * m) >> 7) << 7);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const uint32_t rx_v = qam_decide(qt, x[t]);
+        const uint32_t tx_v = extract_bits_msb(bits + (size_t)(s * 4 + t) * TC_BITBLK * 4, pos, m);
+        local += __popc(rx_v ^ tx_v);
+      }
+    }
+    tc::fence_before_sync();
+  }
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, TC_N);
+  // block error count
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+  __shared__ unsigned int wsum[TC_THREADS / 32];
+  __shared__ int okall;
+  if (tid == 0) okall = 1;
+  __syncthreads();
+  if (!ok) okall = 0;
+  if (lane == 0) wsum[warp] = local;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned int tot = 0;
+    for (int i = 0; i < TC_THREADS / 32; ++i) tot += wsum[i];
+    if (!okall) {  // the tensor core never signalled completion
+      atomicOr(errors + b, 0x80000000u);
+      atomicExch(fail, 1);
+    }
+    else if (tot) atomicAdd(errors + b, tot);
+  }
+}
+
+void upload_raw(void** dst, const void* src, size_t bytes, cudaError_t* err) {
+  if (*err != cudaSuccess) return;
+  *err = cudaMalloc(dst, bytes);
+  if (*err == cudaSuccess && src) *err = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+}
+
+}  // namespace
+
+// Host tables of the tensor-core receiver (called by hpx_lmmse_create for 4 x 4).
+hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays) {
+  const hpx_frame* fr = e->frame;
+  const int N = e->N, W = e->W, FC = fr->info.num_columns, U = e->U;
+  const int KP = ((2 * U + 15) / 16) * 16;
+  const int mtiles = (e->C + TC_M - 1) / TC_M;
+  // twiddle operand per tile: row c (subcarrier), k < U: Re F, U <= k < 2U: Im F
+  std::vector<float2> tw(N);
+  for (int t = 0; t < N; ++t) {
+    const double a = -2.0 * M_PI * (double)t / (double)N;
+    tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  std::vector<uint16_t> ftab((size_t)mtiles * 2 * TC_M * KP, 0);
+  for (int mt = 0; mt < mtiles; ++mt)
+    for (int r = 0; r < TC_M; ++r) {
+      const int c = mt * TC_M + r;
+      if (c >= e->C) continue;
+      for (int k = 0; k < 2 * U; ++k) {
+        const int u = k < U ? k : k - U;
+        const float2 f = tw[((int64_t)fr->h_bins[c] * delays[u]) & (N - 1)];
+        const float val = k < U ? f.x : f.y;
+        const __half hi = __float2half_rn(val);
+        const __half lo = __float2half_rn(val - __half2float(hi));
+        const size_t base = ((size_t)mt * 2) * TC_M * KP;
+        const uint32_t off = tc::kmajor_offset(r, k, KP) / 2;
+        ftab[base + off] = static_cast<__half_raw>(hi).x;
+        ftab[base + (size_t)TC_M * KP + off] = static_cast<__half_raw>(lo).x;
+      }
+    }
+  // words holding data, padded to whole passes
+  std::vector<int32_t> wl;
+  for (int w = 0; w < W; ++w) {
+    bool any = false;
+    for (int c = 0; c < FC && !any; ++c) any = fr->h_kind[(size_t)w * FC + c] == HPX_RE_DATA;
+    if (any) wl.push_back(w);
+  }
+  while (wl.empty() || wl.size() % TC_WORDS) wl.push_back(-1);
+  std::vector<int32_t> kfirst((size_t)W * mtiles, -1);
+  for (int w = 0; w < W; ++w)
+    for (int c = 0; c < FC; ++c)
+      if (fr->h_kind[(size_t)w * FC + c] == HPX_RE_DATA) {
+        int32_t& kf = kfirst[(size_t)w * mtiles + c / TC_M];
+        if (kf < 0) kf = fr->h_index[(size_t)w * FC + c];
+      }
+  e->tc_KP = KP;
+  e->tc_mtiles = mtiles;
+  e->tc_nwl = (int)wl.size();
+  e->tc_ws_drops = kLmmseTcChunk;
+  cudaError_t err = cudaSuccess;
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_ftab), ftab.data(), ftab.size() * 2, &err);
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_wlist), wl.data(), wl.size() * 4, &err);
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_kfirst), kfirst.data(), kfirst.size() * 4, &err);
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_bop), nullptr,
+             (size_t)kLmmseTcChunk * (wl.size() / TC_WORDS) * 2 * TC_M * KP * 2, &err);
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_scale), nullptr, (size_t)kLmmseTcChunk * 4, &err);
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_fail), nullptr, sizeof(int), &err);
+  if (err == cudaSuccess) err = cudaMemset(e->d_tc_fail, 0, sizeof(int));
+  if (err != cudaSuccess) return hpx_cuda_status(err, "lmmse tensor-core tables");
+  return HPX_OK;
+}
+
+void lmmse_tc_release(hpx_lmmse* e) {
+  void* p[] = {e->d_tc_ftab, e->d_tc_wlist, e->d_tc_kfirst, e->d_tc_bop, e->d_tc_scale, e->d_tc_fail};
+  for (void* q : p)
+    if (q) cudaFree(q);
+}
+
+// At least 48 KB, so that at most four CTAs (4 x 128 TMEM columns) share an SM.
+size_t lmmse_tc_smem(const hpx_lmmse* e) {
+  const size_t need = (size_t)4 * TC_M * e->tc_KP * 2 + (size_t)TC_WORDS * 4 * TC_BITBLK * 16 + 128;
+  return std::max(need, (size_t)48 * 1024);
+}
+
+// The 4 x 4 receiver over B drops in chunks of the workspace size.
+hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int gcols, const float* nv,
+                           uint64_t seed, int64_t drop0, int B, uint32_t* errors, cudaStream_t s) {
+  const hpx_frame* fr = e->frame;
+  QamDemapTable qt;
+  HPX_TRY(qam_demap_table(fr->info.modulation_order, &qt));
+  const size_t smem_g = lmmse_taps_smem(e->W, e->U, e->np, e->ntx, TC_NP);
+  const size_t smem_t = lmmse_tc_smem(e);
+  if (smem_g > 220 * 1024 || smem_t > 220 * 1024)
+    return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_lmmse: frame needs too much shared memory");
+  HPX_CUDA(cudaFuncSetAttribute(k_lmmse_gains, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g));
+  HPX_CUDA(cudaFuncSetAttribute(k_lmmse_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
+  const LmmseView lv = lmmse_view(e);
+  TcView tv{e->W, fr->info.num_columns, e->U, e->tc_KP, e->tc_mtiles, e->tc_nwl, fr->info.bits_per_symbol,
+            e->d_tc_wlist, e->d_tc_kfirst, fr->d_kind, fr->d_index, e->d_tc_ftab, e->d_tc_bop, e->d_tc_scale};
+  const int64_t per_drop = (int64_t)4 * e->W * gcols;  // grid samples per drop
+  for (int d = 0; d < B; d += e->tc_ws_drops) {
+    const int nb = std::min(e->tc_ws_drops, B - d);
+    const float2* g = grid + (int64_t)d * per_drop;
+    const float* n = nv ? nv + d : nullptr;
+    k_lmmse_gains<<<nb, 512, smem_g, s>>>(lv, g, gcols, n, e->d_tc_wlist, e->tc_nwl, e->tc_KP, e->d_tc_bop,
+                                          e->d_tc_scale);
+    HPX_LAUNCHED("lmmse_gains");
+    k_lmmse_tc<<<dim3(e->tc_mtiles, nb), TC_THREADS, smem_t, s>>>(tv, e->W, g, gcols, n, qt, mode, seed, drop0 + d,
+                                                                  errors + d, e->d_tc_fail);
+    HPX_LAUNCHED("lmmse_tc");
+  }
+  return HPX_OK;
+}
