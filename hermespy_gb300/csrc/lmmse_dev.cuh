@@ -29,6 +29,68 @@ __host__ __device__ inline size_t lmmse_taps_smem(int W, int U, int np, int ntx,
   return (size_t)W * U * NP * 8 + (size_t)NP * np * U * 8 + (size_t)ntx * U * W * np * 4 + (size_t)U * 4 + 16;
 }
 
+// Per stream t and tap u the LMMSE weights of the np pilot words for every word w:
+// solve (R_u + s2 diag(E_t,u)) z = r_u(w) by Cholesky, cw[t][u][w][.] = z. A tap
+// without signal power (non-positive pivot) gets zero weights. NPW >= np is the
+// compile-time bound of the system (exact size when np == NPW).
+template <int NPW>
+__device__ __forceinline__ void lmmse_word_weights(const LmmseView& e, float s2, float* cw, int np = NPW) {
+  const int W = e.W, U = e.U, P = e.P, ntx = e.ntx;
+  for (int q = threadIdx.x; q < ntx * U; q += blockDim.x) {
+    const int t = q / U, u = q - t * U;
+    float m[NPW][NPW];
+#pragma unroll
+    for (int i = 0; i < NPW; ++i)
+#pragma unroll
+      for (int j = 0; j < NPW; ++j)
+        m[i][j] = (i < np && j < np)
+                      ? e.R[((size_t)u * P + i) * P + j] + (i == j ? s2 * e.E[(t * P + i) * U + u] : 0.f)
+                      : 0.f;
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < NPW; ++j) {
+      if (j >= np) break;
+      float d = m[j][j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) d -= m[j][k] * m[j][k];
+      if (!(d > 0.f)) ok = false;  // no signal power on this tap: its gains stay zero
+      const float inv = ok ? rsqrtf(d) : 0.f;
+      m[j][j] = inv;
+#pragma unroll
+      for (int i = j + 1; i < NPW; ++i) {
+        if (i >= np) break;
+        float sm = m[i][j];
+#pragma unroll
+        for (int k = 0; k < j; ++k) sm -= m[i][k] * m[j][k];
+        m[i][j] = sm * inv;
+      }
+    }
+    for (int w = 0; w < W; ++w) {
+      float z[NPW];
+#pragma unroll
+      for (int i = 0; i < NPW; ++i) {
+        if (i >= np) break;
+        float sm = ok ? e.rw[((size_t)u * W + w) * P + i] : 0.f;
+#pragma unroll
+        for (int k = 0; k < i; ++k) sm -= m[i][k] * z[k];
+        z[i] = ok ? sm * m[i][i] : 0.f;
+      }
+#pragma unroll
+      for (int i = NPW - 1; i >= 0; --i) {
+        if (i >= np) continue;
+        float sm = z[i];
+#pragma unroll
+        for (int k = i + 1; k < NPW; ++k)
+          if (k < np) sm -= m[k][i] * z[k];
+        z[i] = ok ? sm * m[i][i] : 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < NPW; ++i)
+        if (i < np) cw[(((size_t)t * U + u) * W + w) * np + i] = z[i];
+    }
+  }
+}
+
 // Tap gains of every antenna pair and word of drop b into gt (pair = rx * ntx + tx),
 // stored as planes: for word w and tap u, NP real parts then NP imaginary parts
 // (float index (w U + u) 2 NP + {0, NP} + pair), so two pairs share each packed
@@ -81,42 +143,12 @@ __device__ __forceinline__ void lmmse_drop_taps(const LmmseView& e, int b, int n
       }
     }
   }
-  for (int q = threadIdx.x; q < ntx * U; q += blockDim.x) {
-    const int t = q / U, u = q - t * U;
-    float m[kMaxPilotWords][kMaxPilotWords];
-    for (int i = 0; i < np; ++i)
-      for (int j = 0; j < np; ++j)
-        m[i][j] = e.R[((size_t)u * P + i) * P + j] + (i == j ? s2 * e.E[(t * P + i) * U + u] : 0.f);
-    bool ok = true;
-    for (int j = 0; j < np && ok; ++j) {
-      float d = m[j][j];
-      for (int k = 0; k < j; ++k) d -= m[j][k] * m[j][k];
-      if (!(d > 0.f)) {  // no signal power on this tap: its gains stay zero
-        ok = false;
-        break;
-      }
-      const float inv = rsqrtf(d);
-      m[j][j] = inv;
-      for (int i = j + 1; i < np; ++i) {
-        float sm = m[i][j];
-        for (int k = 0; k < j; ++k) sm -= m[i][k] * m[j][k];
-        m[i][j] = sm * inv;
-      }
-    }
-    for (int w = 0; w < W; ++w) {
-      float z[kMaxPilotWords];
-      for (int i = 0; i < np; ++i) {
-        float sm = ok ? e.rw[((size_t)u * W + w) * P + i] : 0.f;
-        for (int k = 0; k < i; ++k) sm -= m[i][k] * z[k];
-        z[i] = ok ? sm * m[i][i] : 0.f;
-      }
-      for (int i = np - 1; i >= 0; --i) {
-        float sm = z[i];
-        for (int k = i + 1; k < np; ++k) sm -= m[k][i] * z[k];
-        z[i] = ok ? sm * m[i][i] : 0.f;
-      }
-      for (int i = 0; i < np; ++i) cw[(((size_t)t * U + u) * W + w) * np + i] = z[i];
-    }
+  switch (np) {  // register-resident systems for the usual pilot-word counts
+    case 1: lmmse_word_weights<1>(e, s2, cw); break;
+    case 2: lmmse_word_weights<2>(e, s2, cw); break;
+    case 3: lmmse_word_weights<3>(e, s2, cw); break;
+    case 4: lmmse_word_weights<4>(e, s2, cw); break;
+    default: lmmse_word_weights<kMaxPilotWords>(e, s2, cw, np); break;
   }
   __syncthreads();
   float* gtf = reinterpret_cast<float*>(gt);

@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(512, 2) k_lmmse_gains(LmmseView e, const float
 }
 
 // ------------------------------------------------------- kernel 2: GEMM + detect
-__global__ void __launch_bounds__(TC_THREADS, 2) k_lmmse_tc(TcView v, int W, const float2* __restrict__ grid,
+__global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, const float2* __restrict__ grid,
                                                              int gcols, const float* __restrict__ nv,
                                                              const __grid_constant__ QamDemapTable qt, int mode,
                                                              uint64_t seed, int64_t drop0,
