@@ -48,10 +48,12 @@ __device__ __forceinline__ float2 twiddle32(float2 v, int t) {
   return make_float2(v.x * c - v.y * s, v.x * s + v.y * c);
 }
 
+// Complex sum and difference as packed FP32x2 adds (round to nearest, the same
+// results as two scalar adds each).
 __device__ __forceinline__ void dft2(float2& a, float2& b) {
   const float2 t = a;
-  a = make_float2(t.x + b.x, t.y + b.y);
-  b = make_float2(t.x - b.x, t.y - b.y);
+  a = __fadd2_rn(t, b);
+  b = __fadd2_rn(t, make_float2(-b.x, -b.y));
 }
 
 // In-register DFT of length R in {2, 4, 8, 16, 32}, natural order in and out.
