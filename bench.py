@@ -300,14 +300,18 @@ def stage_report(stage_ms, steps, work, drops, pk):
     return info
 
 
-def roofline_of(info, pk, traffic_key_map=None):
+def roofline_of(info, pk, drops):
+    """Roofline of the stage with the largest share; traffic = ncu DRAM bytes per drop
+    (profiles/traffic.json) times the drops of one launch."""
+
     dom = max(info, key=lambda s: info[s]["ms"])
     d = info[dom]
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
-            traffic = json.load(f).get(dom)
+            per_drop = json.load(f).get(dom)
+        traffic = None if per_drop is None else int(per_drop * drops)
     if d["bound"] == "tensor":
         return {"kernel": dom, "bound": "tensor", "achieved": d["achieved_tflops"], "peak": pk["bf16_tflops"],
                 "unit": "TFLOP/s", "frac": d["frac"], "traffic": traffic, "peak_source": pk["src"]}
@@ -456,7 +460,10 @@ def bench_estimators(ctx, spec, args):
         comparison[name] = {"bits_per_s": drops * spec.bits_per_drop / (ms / 1e3), "ms_per_step": round(ms, 4),
                             "ber": r["ber"], "nmse_db": nm[name]}
     sel = results[selected]
-    launches = {"learned": 4 + 1 + 8 * ((drops + chunk - 1) // chunk) + 1, "lmmse": 5, "ls": 6}[selected]
+    # lmmse: realize, transmit, propagate, receive, then gains + tensor-core receiver per
+    # chunk of 2 048 drops
+    launches = {"learned": 4 + 1 + 8 * ((drops + chunk - 1) // chunk) + 1,
+                "lmmse": 4 + 2 * ((drops + 2047) // 2048), "ls": 6}[selected]
     extra = {"synchronization": sync_report(ctx, args), "comparison": comparison, "estimator_policy": {
         "selected": selected, "rule": "learned if its validation NMSE <= LMMSE NMSE + 0.5 dB, else LMMSE",
         "validation_drops": nval}, "weights": os.path.relpath(wpath, ROOT)}
@@ -717,7 +724,7 @@ def main() -> None:
     if rank == 0:
         pk = peaks()
         info = stage_report(res["stage_ms"], args.steps, res["work"], drops, pk)
-        roof = roofline_of(info, pk)
+        roof = roofline_of(info, pk, drops)
         cpu_value, cpu_drops, cpu_s = time_cpu(pool, cores, spec, args.cpu_rounds if spec.name != "massive" else 1)
         if spec.name == "uneven":
             spec.config = dict(spec.config, bits_per_drop_mean=spec.bits_per_drop)
