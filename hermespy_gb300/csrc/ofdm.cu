@@ -76,10 +76,10 @@ constexpr int groups_per_block() {
 // MODE 0: data symbols `data` [items][num_data]; MODE 1: Philox bits of drop
 // item / num_streams, stream item % num_streams; MODE 2: a placed grid `data`
 // [items][W][G] with G = num_streams columns.
-// Five CTAs per SM: the transmit FFT with its staged Philox bits is latency bound,
-// and the register cap (about 100) costs a few bytes of spill but gains occupancy.
+// Seven CTAs per SM: the transmit FFT with its staged Philox bits is latency bound,
+// and the register cap (72) costs a few bytes of spill but gains occupancy.
 template <int N, int MODE>
-__global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), 5)
+__global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), 7)
     k_ofdm_tx(FrameDev fr, int num_pairs, const float2* __restrict__ data, uint64_t seed, int64_t drop0,
               int num_streams, float2* __restrict__ out) {
   constexpr int TP = fft::Plan<N>::TP;
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), 5)
 }
 
 template <int N>
-__global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>())
+__global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), 6)
     k_ofdm_rx(FrameDev fr, int num_pairs, const float2* __restrict__ in, int64_t stride, int ncols,
               float2* __restrict__ grid) {
   constexpr int TP = fft::Plan<N>::TP;
