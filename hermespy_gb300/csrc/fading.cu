@@ -192,8 +192,8 @@ __host__ __device__ constexpr int tile_len() { return NTX <= 4 ? 1024 : (NTX <= 
 
 __host__ __device__ constexpr int tile_width(int BT, int D) { return (BT + D + 2) & ~1; }
 
-template <int NTX, int K, bool DIRECT, int BT = tile_len<NTX>(), int PTHREADS = tile_len<NTX>() / 4>
-__global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingView v, int T, const float2* __restrict__ x,
+template <int NTX, int K, bool DIRECT, int PPT = 2, int BT = tile_len<NTX>(), int PTHREADS = tile_len<NTX>() / (2 * PPT)>
+__global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 1) k_propagate(FadingConst fc, FadingView v, int T, const float2* __restrict__ x,
                                                         float2* __restrict__ y, const float* __restrict__ noise_power,
                                                         uint64_t seed, int64_t drop0) {
   extern __shared__ float4 smem4[];
@@ -274,15 +274,17 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
 
   // ---- convolution: z_tx[m] = sum_l h_l[m - d_l] x_tx[m - d_l], two samples per
   // packed FP32x2 FMA: zr/zi hold the real/imaginary parts of a pair of samples.
-  const int jp[2] = {2 * tid, 2 * tid + BT / 2};  // tile index of each pair's first sample
-  float2 zr[2][NTX], zi[2][NTX];
+  int jp[PPT];  // tile index of each pair's first sample
 #pragma unroll
-  for (int pr = 0; pr < 2; ++pr)
+  for (int pr = 0; pr < PPT; ++pr) jp[pr] = 2 * tid + pr * (BT / PPT);
+  float2 zr[PPT][NTX], zi[PPT][NTX];
+#pragma unroll
+  for (int pr = 0; pr < PPT; ++pr)
 #pragma unroll
     for (int tx = 0; tx < NTX; ++tx) zr[pr][tx] = zi[pr][tx] = make_float2(0.f, 0.f);
-  float2 up[2][K + 1];  // powers of u for both samples of a pair
+  float2 up[PPT][K + 1];  // powers of u for both samples of a pair
 #pragma unroll
-  for (int pr = 0; pr < 2; ++pr) {
+  for (int pr = 0; pr < PPT; ++pr) {
     const float u0 = ((float)jp[pr] - 0.5f * BT) / (0.5f * BT);
     const float u1 = ((float)(jp[pr] + 1) - 0.5f * BT) / (0.5f * BT);
     up[pr][0] = make_float2(1.0f, 1.0f);
@@ -292,11 +294,11 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
 #pragma unroll 1
   for (int l = 0; l < L; ++l) {
     const int d = dl[l];
-    float2 hx[2], hy[2];
+    float2 hx[PPT], hy[PPT];
     if (DIRECT) {
       const float an = fc.amp[2 * l], al = fc.amp[2 * l + 1];
 #pragma unroll
-      for (int pr = 0; pr < 2; ++pr) {
+      for (int pr = 0; pr < PPT; ++pr) {
         const float2 h0 = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al, (int64_t)m0 + jp[pr] - d);
         const float2 h1 = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al, (int64_t)m0 + jp[pr] + 1 - d);
         hx[pr] = make_float2(h0.x, h1.x);
@@ -308,7 +310,7 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
 #pragma unroll
       for (int k = 0; k <= K; ++k) ck[k] = cl[k];
 #pragma unroll
-      for (int pr = 0; pr < 2; ++pr) {
+      for (int pr = 0; pr < PPT; ++pr) {
         float2 ax = make_float2(ck[0].x, ck[0].y), ay = make_float2(ck[0].z, ck[0].w);
 #pragma unroll
         for (int k = 1; k <= K; ++k) {
@@ -323,7 +325,7 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
     const int odd = (D - d) & 1;
     const float* src = xp + 2 * odd * XW - odd;  // plane offset of the even/odd copy, index shifted by one
 #pragma unroll
-    for (int pr = 0; pr < 2; ++pr) {
+    for (int pr = 0; pr < PPT; ++pr) {
       const int s0 = jp[pr] - d + D;
       const float2 nhy = make_float2(-hy[pr].x, -hy[pr].y);
 #pragma unroll
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(PTHREADS) k_propagate(FadingConst fc, FadingVi
   for (int rx = 0; rx < nrx; ++rx) {
     float2* yr = y + ((int64_t)b * nrx + rx) * TD;
 #pragma unroll
-    for (int pr = 0; pr < 2; ++pr) {
+    for (int pr = 0; pr < PPT; ++pr) {
       float2 ore = make_float2(0.f, 0.f), oim = make_float2(0.f, 0.f);
 #pragma unroll
       for (int tx = 0; tx < NTX; ++tx) {
@@ -431,12 +433,15 @@ hpx_status launch_propagate(const hpx_fading* f, const void* state, int B, const
                       (DIRECT ? 2 * (size_t)fc.L * fc.S1 * sizeof(int64_t) : 0) +
                       (size_t)fc.nrx * NTX * sizeof(float2) + (size_t)fc.L * sizeof(int) + 16;
   if (smem > 200 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "propagate: channel too long for one tile");
-  auto kern = k_propagate<NTX, K, DIRECT>;
+  // Two pairs per thread: one pair (512 threads, 62 registers, 2 CTAs/SM) took 7.4 ms and
+  // four pairs (152 registers) 6.2 ms for 8 192 drops of the 4 x 4 link, against 5.5 ms.
+  constexpr int PPT = 2;
+  auto kern = k_propagate<NTX, K, DIRECT, PPT>;
   if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int TD = T + fc.D;
   dim3 grid((TD + BT - 1) / BT, B);
-  kern<<<grid, BT / 4, smem, s>>>(fc, v, T, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(y), np,
-                                    seed, drop0);
+  kern<<<grid, BT / (2 * PPT), smem, s>>>(fc, v, T, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(y),
+                                          np, seed, drop0);
   HPX_LAUNCHED("propagate");
   return HPX_OK;
 }
