@@ -193,7 +193,7 @@ __host__ __device__ constexpr int tile_len() { return NTX <= 4 ? 1024 : (NTX <= 
 __host__ __device__ constexpr int tile_width(int BT, int D) { return (BT + D + 2) & ~1; }
 
 template <int NTX, int K, bool DIRECT, int PPT = 2, int BT = tile_len<NTX>(), int PTHREADS = tile_len<NTX>() / (2 * PPT)>
-__global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 1) k_propagate(FadingConst fc, FadingView v, int T, const float2* __restrict__ x,
+__global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(FadingConst fc, FadingView v, int T, const float2* __restrict__ x,
                                                         float2* __restrict__ y, const float* __restrict__ noise_power,
                                                         uint64_t seed, int64_t drop0) {
   extern __shared__ float4 smem4[];
