@@ -76,10 +76,16 @@ constexpr int groups_per_block() {
 // MODE 0: data symbols `data` [items][num_data]; MODE 1: Philox bits of drop
 // item / num_streams, stream item % num_streams; MODE 2: a placed grid `data`
 // [items][W][G] with G = num_streams columns.
-// Seven CTAs per SM: the transmit FFT with its staged Philox bits is latency bound,
-// and the register cap (72) costs a few bytes of spill but gains occupancy.
+// Resident CTAs per SM the FFT kernels are compiled for: the transforms are latency
+// bound, so the 128-thread CTAs of N <= 2048 take a register cap (72 transmit / 80
+// receive) at a few bytes of spill; the 256-thread CTAs of N = 4096 keep 85 registers.
+template <int N>
+constexpr int tx_min_blocks() { return fft::Plan<N>::TP * groups_per_block<N>() >= 256 ? 3 : 7; }
+template <int N>
+constexpr int rx_min_blocks() { return fft::Plan<N>::TP * groups_per_block<N>() >= 256 ? 3 : 6; }
+
 template <int N, int MODE>
-__global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), 7)
+__global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), tx_min_blocks<N>())
     k_ofdm_tx(FrameDev fr, int num_pairs, const float2* __restrict__ data, uint64_t seed, int64_t drop0,
               int num_streams, float2* __restrict__ out) {
   constexpr int TP = fft::Plan<N>::TP;
@@ -151,7 +157,7 @@ __global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), 7)
 }
 
 template <int N>
-__global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), 6)
+__global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), rx_min_blocks<N>())
     k_ofdm_rx(FrameDev fr, int num_pairs, const float2* __restrict__ in, int64_t stride, int ncols,
               float2* __restrict__ grid) {
   constexpr int TP = fft::Plan<N>::TP;
