@@ -32,6 +32,7 @@ from .estimation import (
     ZeroForcingChannelEqualization,
     ls_interpolation_table,
 )
+from .fec import Encoder, EncoderManager, LDPCCoding
 from .mapping import PskQamMapping
 from .noise import AWGN, EBN0, ESN0, SNR, AWGNRealization
 from .presets import TDL, CorrelationType, Cost259, Cost259Type, DeviceType, StandardAntennaCorrelation, TDLType

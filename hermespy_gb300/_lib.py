@@ -110,6 +110,11 @@ _SIGNATURES = {
     "hpx_awgn_add": [c_void_p, c_int32, c_int32, c_int64, c_void_p, c_uint64, c_int64, c_void_p],
     "hpx_sync_schmidl_cox": [c_void_p, c_int32, c_int32, c_int64, c_int32, c_void_p, c_void_p],
     "hpx_sync_correlation": [c_void_p, c_int32, c_int32, c_int64, c_void_p, c_int32, c_void_p, c_void_p],
+    "hpx_ldpc_create": [c_int32, c_int32, c_int32, c_void_p, c_void_p, ctypes.POINTER(c_void_p)],
+    "hpx_ldpc_destroy": [c_void_p],
+    "hpx_ldpc_info": [c_void_p, ctypes.POINTER(c_int32), ctypes.POINTER(c_int32), c_void_p],
+    "hpx_ldpc_encode": [c_void_p, c_void_p, c_int32, c_void_p, c_void_p],
+    "hpx_ldpc_decode": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
     "hpx_sync_peaks": [c_void_p, c_int32, c_int64, c_int32, ctypes.c_double, c_int64, c_int64, c_int32, c_int64,
                        c_int64, c_int32, c_void_p, c_void_p, c_void_p],
     "hpx_link_workspace_bytes": [c_void_p, c_void_p, c_int32, ctypes.POINTER(c_int64)],

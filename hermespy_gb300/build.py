@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhpx.so")
-SOURCES = ["frame.cu", "mapping.cu", "ofdm.cu", "fading.cu", "detect.cu", "estimate.cu", "lmmse_tc.cu", "cnn.cu", "massive.cu", "campaign.cu", "sync.cu", "uneven.cu", "link.cu", "link_static.cu"]
+SOURCES = ["frame.cu", "mapping.cu", "ofdm.cu", "fading.cu", "detect.cu", "estimate.cu", "lmmse_tc.cu", "cnn.cu", "massive.cu", "campaign.cu", "sync.cu", "ldpc.cu", "uneven.cu", "link.cu", "link_static.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
 

@@ -388,6 +388,31 @@ hpx_status hpx_sync_peaks(const double* metric, int32_t batch, int64_t length, i
                           int64_t distance, int64_t offset, int32_t clip, int64_t clip_max, int64_t clip_value,
                           int32_t max_frames, int64_t* starts, int32_t* counts, void* stream);
 
+/* --------------------------------------------------------------------- FEC */
+
+/* LDPC block code from the edges of its parity-check matrix H (edge e joins variable
+ * edge_var[e] < N and check edge_chk[e] < M). Replaces the aff3ct LDPC wrapper of the
+ * reference (fec/aff3ct/ldpc.cpp: LDPC::LDPC, encode, decode; fec/aff3ct_wrappers.py
+ * LDPCCoding), whose H comes from an alist file: the encoder is systematic from the
+ * reduced row-echelon form of H (K = N - rank(H) data bits at the non-pivot columns),
+ * the decoder belief propagation with the flooding schedule and the sum-product check
+ * update. */
+typedef struct hpx_ldpc hpx_ldpc;
+hpx_status hpx_ldpc_create(int32_t N, int32_t M, int32_t E, const int32_t* edge_var, const int32_t* edge_chk,
+                           hpx_ldpc** out);
+hpx_status hpx_ldpc_destroy(hpx_ldpc* code);
+/* K, N and (host array of K, may be NULL) the codeword position of each data bit. */
+hpx_status hpx_ldpc_info(const hpx_ldpc* code, int32_t* data_bits, int32_t* code_bits, int32_t* info_positions);
+/* data[B][K] bits (one per byte) -> code[B][N] bits (LDPC::encode). */
+hpx_status hpx_ldpc_encode(const hpx_ldpc* code, const uint8_t* data, int32_t B, uint8_t* out, void* stream);
+/* Hard code bits hard[B][N] (LDPC::decode's hard input: bit b -> channel LLR 4 (1 - 2b)) or,
+ * if hard is NULL, channel LLRs llr[B][N] (log P(0) / P(1)) -> data[B][K]. At most
+ * `iterations` flooding iterations; with syndrome_checking the decoder stops once every
+ * parity check holds and min_iterations have run. iterations_used[B] may be NULL. */
+hpx_status hpx_ldpc_decode(const hpx_ldpc* code, const uint8_t* hard, const float* llr, int32_t B, int32_t iterations,
+                           int32_t syndrome_checking, int32_t min_iterations, uint8_t* data, int32_t* iterations_used,
+                           void* stream);
+
 /* ------------------------------------------------------- batched drop loop */
 
 enum { HPX_EST_IDEAL = 0, HPX_EST_LS = 1 };

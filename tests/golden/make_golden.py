@@ -23,6 +23,9 @@ sync.npz     ``PilotSection`` / ``SchmidlCoxPilotSection`` preambles (128 subcar
              with and without DC suppression) and the frame starts that
              ``SchmidlCoxSynchronization`` and ``OFDMCorrelationSynchronization``
              find in noisy two-stream signals holding two or three frames.
+ldpc.npz     Edges of the parity-check matrix the reference ships for its 5G NR OFDM
+             modem (``modem/resources/ofdm_ldpc.alist``, read as data; the aff3ct
+             decoder that the reference wraps is not part of the checkout).
 presets.npz  Tap delays, power profiles, Rice factors and line-of-sight Doppler of
              the ``TDL`` (A-E), ``Cost259`` (urban, rural, hilly) and
              ``Exponential`` presets, and ``StandardAntennaCorrelation``
@@ -476,9 +479,16 @@ def make_sync() -> None:
     save("sync.npz", **out)
 
 
+def make_ldpc() -> None:
+    from oracle import ldpc as oldpc
+
+    N, M, ev, ec = oldpc.read_alist(os.path.join(REF, "hermespy", "modem", "resources", "ofdm_ldpc.alist"))
+    save("ldpc.npz", N=np.int64(N), M=np.int64(M), edge_var=ev, edge_chk=ec)
+
+
 MAKERS = {"qam": make_qam, "ofdm": make_ofdm, "fading": make_fading, "ls": make_ls, "ideal": make_ideal,
           "zf": make_zf, "ber": make_ber, "drops": make_drops, "presets": make_presets,
-          "sync": make_sync}
+          "sync": make_sync, "ldpc": make_ldpc}
 
 if __name__ == "__main__":
     for name, maker in MAKERS.items():
