@@ -469,7 +469,8 @@ def bench_estimators(ctx, spec, args):
     # chunk of 2 048 drops
     launches = {"learned": 4 + 1 + 8 * ((drops + chunk - 1) // chunk) + 1,
                 "lmmse": 4 + 2 * ((drops + 2047) // 2048), "ls": 6}[selected]
-    extra = {"synchronization": sync_report(ctx, args), "comparison": comparison, "estimator_policy": {
+    extra = {"synchronization": sync_report(ctx, args), "fec": fec_report(ctx, args), "comparison": comparison,
+             "estimator_policy": {
         "selected": selected, "rule": "learned if its validation NMSE <= LMMSE NMSE + 0.5 dB, else LMMSE",
         "validation_drops": nval}, "weights": os.path.relpath(wpath, ROOT)}
     extra["stages_note"] = ("stages: CUDA events around each kernel of a serialised run of the same path "
@@ -526,6 +527,37 @@ def sync_report(ctx, args, signals: int = 2048, slack: int = 256) -> dict:
                               "frac": round(mbytes / mms / 1e6 / pk["hbm_gbs"], 4)},
             "detected_within_3_samples": exact, "api_check": [v[:1] for v in single],
             "true_starts_of_api_check": offsets[:4].tolist()}
+
+
+def fec_report(ctx, args, blocks: int = 65535, snr_db: float = 3.0) -> dict:
+    """LDPC decoding of the (128, 64) code the reference ships for its 5G NR modem:
+    `blocks` BPSK code blocks over AWGN at `snr_db` per step, channel LLRs resident."""
+
+    torch, hg = ctx["torch"], ctx["hg"]
+    g = np.load(os.path.join(ROOT, "tests", "golden", "ldpc.npz"))
+    code = hg.LDPCCoding.from_edges(int(g["N"]), int(g["M"]), g["edge_var"], g["edge_chk"], 100, True, 10)
+    K, N = code.bit_block_size, code.code_block_size
+    gen = torch.Generator(device=ctx["dev"]).manual_seed(SEED)
+    data = torch.randint(0, 2, (blocks, K), dtype=torch.uint8, device=ctx["dev"], generator=gen)
+    cw = code.encode_device(data)
+    sigma2 = 10 ** (-snr_db / 10)
+    y = (1.0 - 2.0 * cw.float()) + sigma2 ** 0.5 * torch.randn(cw.shape, device=ctx["dev"], generator=gen)
+    llr = (2.0 * y / sigma2).contiguous()
+    out = torch.empty((blocks, K), dtype=torch.uint8, device=ctx["dev"])
+    used = torch.empty(blocks, dtype=torch.int32, device=ctx["dev"])
+    lib = ctx["lib"]
+
+    def step(d0, ev):
+        lib.call("hpx_ldpc_decode", code.handle, None, lib.ptr(llr), blocks, 100, 1, 10, lib.ptr(out),
+                 lib.ptr(used), ctx["sp"])
+
+    total_ms, _ = ctx["timer"].run(step, [], args.steps, args.warmup, 0, 0)
+    ms = total_ms / args.steps
+    ber = float((out != data).float().mean().item())
+    return {"code": "(128, 64) LDPC of modem/resources/ofdm_ldpc.alist", "blocks_per_step": blocks,
+            "snr_db": snr_db, "ms_per_step": round(ms, 4), "blocks_per_s": blocks / (ms / 1e3),
+            "info_bits_per_s": blocks * K / (ms / 1e3), "mean_iterations": float(used.float().mean().item()),
+            "post_decoding_ber": ber}
 
 
 def bench_massive(ctx, spec, args):
