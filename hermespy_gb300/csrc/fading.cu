@@ -35,34 +35,35 @@ __global__ void k_fading_params(FadingConst fc, double nlos_rate, double los_rat
     return u01_f64(uint4_get(r, idx & 3));
   };
 
+  // Drawn angles enter as turns: theta = -pi + 2 pi u gives (2 pi (n + 1) + theta) / S
+  // = pi (2 n + 1 + 2 u) / S and phi / (2 pi) = u - 1/2, so the FP64 work per sinusoid
+  // is one cospi and no division.
+  const double inv_s = 1.0 / (double)(S > 0 ? S : 1);
+  constexpr double kInv2Pi = 0.15915494309189535;
   for (int q = threadIdx.x; q < L * S1; q += blockDim.x) {
     const int l = q / S1, n = q - l * S1;
-    double omega, phase;
+    double omega, turns;
     if (n < S) {
-      double theta, phi;
       if (MODE == 0) {
-        theta = -kPi + 2.0 * kPi * uniform(nsp + L + l * S + n);
-        phi = -kPi + 2.0 * kPi * uniform(nsp + 2 * L + L * S + l * S + n);
+        const double ut = uniform(nsp + L + l * S + n);
+        omega = nlos_rate * cospi((2.0 * n + 1.0 + 2.0 * ut) * inv_s);
+        turns = uniform(nsp + 2 * L + L * S + l * S + n) - 0.5;
       } else {
-        theta = na[((int64_t)b * L + l) * S + n];
-        phi = np_[((int64_t)b * L + l) * S + n];
+        const double theta = na[((int64_t)b * L + l) * S + n];
+        omega = nlos_rate * cos((2.0 * kPi * (n + 1) + theta) / (double)S);
+        turns = np_[((int64_t)b * L + l) * S + n] * kInv2Pi;
       }
-      omega = nlos_rate * cos((2.0 * kPi * (n + 1) + theta) / (double)S);
-      phase = phi;
     } else {
-      double alpha, psi;
       if (MODE == 0) {
-        alpha = 2.0 * kPi * uniform(nsp + l);
-        psi = -kPi + 2.0 * kPi * uniform(nsp + L + L * S + l);
+        omega = los_rate * cospi(2.0 * uniform(nsp + l));
+        turns = uniform(nsp + L + L * S + l) - 0.5;
       } else {
-        alpha = la[(int64_t)b * L + l];
-        psi = lp[(int64_t)b * L + l];
+        omega = los_rate * cos(la[(int64_t)b * L + l]);
+        turns = lp[(int64_t)b * L + l] * kInv2Pi;
       }
-      omega = los_rate * cos(alpha);
-      phase = psi;
     }
-    Wout[q] = turns_to_fixed(omega / (2.0 * kPi));
-    Pout[q] = turns_to_fixed(phase / (2.0 * kPi));
+    Wout[q] = turns_to_fixed(omega * kInv2Pi);
+    Pout[q] = turns_to_fixed(turns);
   }
   for (int j = threadIdx.x; j < nsp; j += blockDim.x) {
     if (MODE == 0) {

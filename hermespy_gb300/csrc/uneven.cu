@@ -77,22 +77,21 @@ __device__ void u_realize(const UDrop& d, int S, uint64_t seed, int64_t drop, in
     const uint4 r = hpx_random_block(seed, drop, 0u, HPX_DOMAIN_FADING, (uint32_t)(idx >> 2));
     return u01_f64(uint4_get(r, idx & 3));
   };
-  for (int q = threadIdx.x; q < L * S1; q += blockDim.x) {
+  const double inv_s = 1.0 / (double)(S > 0 ? S : 1);
+  constexpr double kInv2Pi = 0.15915494309189535;
+  for (int q = threadIdx.x; q < L * S1; q += blockDim.x) {  // the same arithmetic as k_fading_params<0>
     const int l = q / S1, n = q - l * S1;
-    double omega, phase;
+    double omega, turns;
     if (n < S) {
-      const double theta = -kPi + 2.0 * kPi * uniform(nsp + L + l * S + n);
-      const double phi = -kPi + 2.0 * kPi * uniform(nsp + 2 * L + L * S + l * S + n);
-      omega = d.nlos_rate * cos((2.0 * kPi * (n + 1) + theta) / (double)S);
-      phase = phi;
+      const double ut = uniform(nsp + L + l * S + n);
+      omega = d.nlos_rate * cospi((2.0 * n + 1.0 + 2.0 * ut) * inv_s);
+      turns = uniform(nsp + 2 * L + L * S + l * S + n) - 0.5;
     } else {
-      const double alpha = 2.0 * kPi * uniform(nsp + l);
-      const double psi = -kPi + 2.0 * kPi * uniform(nsp + L + L * S + l);
-      omega = d.los_rate * cos(alpha);
-      phase = psi;
+      omega = d.los_rate * cospi(2.0 * uniform(nsp + l));
+      turns = uniform(nsp + L + L * S + l) - 0.5;
     }
-    Wp[q] = turns_to_fixed(omega / (2.0 * kPi));
-    P0[q] = turns_to_fixed(phase / (2.0 * kPi));
+    Wp[q] = turns_to_fixed(omega * kInv2Pi);
+    P0[q] = turns_to_fixed(turns);
   }
   for (int j = threadIdx.x; j < nsp; j += blockDim.x) {
     double s, c;
