@@ -651,6 +651,35 @@ def bench_massive(ctx, spec, args):
             "e2e_s": e2e_s, "h2d": 4 * drops, "d2h": 4 * drops, "launches": 5, "extra": extra}
 
 
+def homogeneous_persistent(ctx, args, drops: int = 4096) -> dict:
+    """The persistent path on the plain 4x4 workload (1024/600, CP 72, 14 words, 64-QAM,
+    23 taps 50 ns apart at -0.4 dB/tap, 500 Hz, ideal CSI + LMMSE, SNR U[0, 30] dB):
+    bits/s beside the staged kernels' (`--workload link4x4`) on the same drop shape."""
+
+    torch = ctx["torch"]
+    from hermespy_gb300.uneven import DropConfig, UnevenBatch
+
+    rng = np.random.default_rng(SEED + 7)
+    cfgs = [DropConfig(4, 4, 1024, 14, 64, 23, 0.4, 500.0, float(s)) for s in rng.uniform(0.0, 30.0, drops)]
+    batch = UnevenBatch(cfgs, 30e3, 50e-9, 20)
+    best = batch.tune(SEED, ctx["drop_base"] + (1 << 41), repeats=1)
+    batch.capture(SEED, ctx["drop_base"] + (1 << 41))
+    stream = ctx["stream"]
+    for _ in range(args.warmup):
+        batch.replay(stream)
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        batch.replay(stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    bits = float(batch.bits.sum())
+    return {"drops_per_step": drops, "ms_per_step": round(ms, 4), "bits_per_s": bits / (ms / 1e3),
+            "ber": float(batch.errors.sum().item()) / bits, "launch_shape": best}
+
+
 def bench_uneven(ctx, spec, args):
     torch, _lib = ctx["torch"], ctx["lib"]
     from hermespy_gb300.uneven import UnevenBatch, random_drops
@@ -699,7 +728,8 @@ def bench_uneven(ctx, spec, args):
     e2e_s = (time.perf_counter() - s0) / n_e2e
     spec.bits_per_drop = total_bits / drops
     extra = {"autotuner": {"chosen": best, "candidates": batch.tuning}, "launch": "one persistent kernel per step "
-             "(CUDA graph replay of counter reset + kernel)", "total_bits_per_step": total_bits}
+             "(CUDA graph replay of counter reset + kernel)", "total_bits_per_step": total_bits,
+             "homogeneous_4x4": homogeneous_persistent(ctx, args)}
     return {"drops": drops, "total_ms": total_ms, "stage_ms": stage_ms, "work": work, "ber": ber, "e2e_s": e2e_s,
             "h2d": 4 * drops, "d2h": 4 * drops, "launches": 1, "extra": extra}
 
