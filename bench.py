@@ -771,20 +771,17 @@ def main() -> None:
     build()
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
+    from hermespy_gb300.distributed import max_over_ranks, rank_base
+
     ctx = {"torch": torch, "hg": hg, "lib": _lib, "dev": dev, "stream": stream, "sp": stream.cuda_stream,
-           "rng": np.random.default_rng(SEED + rank), "drop_base": rank * (1 << 44), "timer": Timer(torch, stream)}
+           "rng": np.random.default_rng(SEED + rank), "drop_base": rank_base(rank), "timer": Timer(torch, stream)}
     if world > 1:
         torch.distributed.barrier()
     with Clocks(local) as clk:
         res = {"estimators": bench_estimators, "link4x4": bench_link4x4, "massive": bench_massive,
                "uneven": bench_uneven}[spec.name](ctx, spec, args)
-    total_ms, e2e_s = res["total_ms"], res["e2e_s"]
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms, e2e_s = float(tt[0]), float(tt[1])
+    # the slowest rank's times (drops are sharded by index; no data-path collective)
+    total_ms, e2e_s = max_over_ranks(res["total_ms"]), max_over_ranks(res["e2e_s"])
     drops = res["drops"]
     ms_per_step = total_ms / args.steps
     value = world * drops * spec.bits_per_drop / (ms_per_step / 1e3)
