@@ -92,14 +92,16 @@ __global__ void k_ldpc_decode(int N, int M, int K, int E, const int32_t* __restr
       const int e0 = chk_ptr[c], e1 = chk_ptr[c + 1];
       float sum = 0.0f;
       uint32_t neg = 0;
-      for (int e = e0; e < e1; ++e) {
+      for (int e = e0; e < e1; ++e) {  // phi(|m|) parked in c2v for the second pass
         const float m = v2c[e];
-        sum += bp_phi(fabsf(m));
+        const float p = bp_phi(fabsf(m));
+        c2v[e] = p;
+        sum += p;
         neg ^= m < 0.0f;
       }
       for (int e = e0; e < e1; ++e) {
         const float m = v2c[e];
-        const float mag = bp_phi(fmaxf(sum - bp_phi(fabsf(m)), 0.0f));
+        const float mag = bp_phi(fmaxf(sum - c2v[e], 0.0f));
         c2v[e] = ((neg ^ (m < 0.0f)) ? -mag : mag);
       }
     }
