@@ -6,7 +6,7 @@
 // k = j mod Ns, computes a DFT of length R_s in registers and writes point r to
 // (j - k) R_s + k + r Ns. Each thread of a transform owns N/TP points (one or
 // more butterflies) per stage; points move between stages through shared memory
-// (padded by one complex every 32 to spread banks). The first stage reads its
+// (padded by one complex every 16 to spread banks). The first stage reads its
 // points through a caller functor (device memory or generated symbols) and the
 // last stage hands the natural-order results to another functor, so a transform
 // touches HBM exactly once in each direction.
@@ -97,7 +97,11 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
   }
 }
 
-__device__ __forceinline__ int pad(int i) { return i + (i >> 5); }
+// One padding slot every 16 points: the first stage's stride-R writes of a half-warp
+// (16 lanes x 8 bytes) then fall on distinct banks.
+__device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
+template <int N>
+__host__ __device__ constexpr int padded() { return N + N / 16; }
 
 // Stage plan of an N-point transform: radices (product N), threads per transform.
 template <int N>

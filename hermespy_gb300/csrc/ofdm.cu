@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), tx_m
               int num_streams, float2* __restrict__ out) {
   constexpr int TP = fft::Plan<N>::TP;
   constexpr int F = groups_per_block<N>();
-  constexpr int PN = N + N / 32;
+  constexpr int PN = fft::padded<N>();
   extern __shared__ float4 smem4[];
   const int g = threadIdx.x / TP, t = threadIdx.x - g * TP;
   float2* buf = reinterpret_cast<float2*>(smem4) + g * PN;
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), rx_m
               float2* __restrict__ grid) {
   constexpr int TP = fft::Plan<N>::TP;
   constexpr int F = groups_per_block<N>();
-  constexpr int PN = N + N / 32;
+  constexpr int PN = fft::padded<N>();
   extern __shared__ float4 smem4[];
   const int g = threadIdx.x / TP, t = threadIdx.x - g * TP;
   float2* buf = reinterpret_cast<float2*>(smem4) + g * PN;
@@ -195,7 +195,7 @@ hpx_status launch_tx_n(const FrameDev& d, int pairs, const float2* data, uint64_
                        float2* out, cudaStream_t s) {
   constexpr int F = groups_per_block<N>();
   constexpr int threads = fft::Plan<N>::TP * F;
-  const size_t smem = (size_t)F * (N + N / 32) * sizeof(float2) +
+  const size_t smem = (size_t)F * (N + N / 16) * sizeof(float2) +
                       (MODE == 1 ? (size_t)d.order * sizeof(float2) + (size_t)F * staged_bit_words(d.C, d.m) * 4 : 0);
   auto kern = k_ofdm_tx<N, MODE>;
   if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -225,7 +225,7 @@ hpx_status launch_rx_n(const FrameDev& d, int pairs, const float2* in, int64_t s
                        cudaStream_t s) {
   constexpr int F = groups_per_block<N>();
   constexpr int threads = fft::Plan<N>::TP * F;
-  const size_t smem = (size_t)F * (N + N / 32) * sizeof(float2);
+  const size_t smem = (size_t)F * (N + N / 16) * sizeof(float2);
   auto kern = k_ofdm_rx<N>;
   if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int blocks = (pairs + F - 1) / F;

@@ -104,7 +104,7 @@ __device__ void u_realize(const UDrop& d, int S, uint64_t seed, int64_t drop, in
 template <int N>
 __device__ void u_tx(const UFrame& fr, int ntx, uint64_t seed, int64_t drop, float2* x, unsigned char* sm) {
   constexpr int TP = fft::Plan<N>::TP;
-  constexpr int PN = N + N / 32;
+  constexpr int PN = fft::padded<N>();
   const int F = blockDim.x / TP, g = threadIdx.x / TP, t = threadIdx.x - g * TP;
   const int BW = staged_bit_words(fr.C, fr.m);
   float2* buf = reinterpret_cast<float2*>(sm) + g * PN;
@@ -151,7 +151,7 @@ __device__ void u_tx(const UFrame& fr, int ntx, uint64_t seed, int64_t drop, flo
 template <int N>
 __device__ void u_rx(const UFrame& fr, int nrx, int TD, const float2* y, float2* grid, unsigned char* sm) {
   constexpr int TP = fft::Plan<N>::TP;
-  constexpr int PN = N + N / 32;
+  constexpr int PN = fft::padded<N>();
   const int F = blockDim.x / TP, g = threadIdx.x / TP, t = threadIdx.x - g * TP;
   float2* buf = reinterpret_cast<float2*>(sm) + g * PN;
   const float scale = rsqrtf((float)N);
@@ -682,7 +682,7 @@ hpx_status hpx_uneven_create(const hpx_uneven_drop* drops, int32_t num_drops, do
     // stage shared memory (beyond the 768-byte header), for UMAX_THREADS threads
     const int TP = N == 128 ? 8 : N == 256 ? 16 : N == 512 ? 32 : N == 1024 ? 64 : 128;
     const int F = UMAX_THREADS / TP;
-    const size_t fft_smem = (size_t)F * (N + N / 32) * sizeof(float2) + (size_t)F * staged_bit_words(fr.C, m) * 4;
+    const size_t fft_smem = (size_t)F * (N + N / 16) * sizeof(float2) + (size_t)F * staged_bit_words(fr.C, m) * 4;
     const int KK = d.K < 0 ? 0 : d.K;
     const int XW = (d.BT + d.D + 2) & ~1;
     const size_t region = std::max((size_t)2 * d.ntx * XW, (size_t)d.L * S1 * (KK + 1));
