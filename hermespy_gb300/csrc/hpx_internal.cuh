@@ -210,7 +210,7 @@ struct hpx_lmmse {
   float* d_tc_scale = nullptr;     // [tc_ws_drops]
   int* d_tc_fail = nullptr;        // set if a tensor-core wait timed out (later CTAs skip)
 };
-constexpr int kLmmseTcChunk = 2048;  // drops per gains/GEMM launch pair
+constexpr int kLmmseTcChunk = 8192;  // drops per gains/GEMM launch pair (workspace 72 KB per drop)
 hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays);
 void lmmse_tc_release(hpx_lmmse* e);
 hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int gcols, const float* nv,
