@@ -106,39 +106,54 @@ __device__ __forceinline__ void lmmse_drop_taps(const LmmseView& e, int b, int n
   const int np = e.np;  // every stream has the same pilot words (checked at create time)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int u = threadIdx.x; u < U; u += blockDim.x) ds[u] = e.delay[u];
-  // One warp per (pair, pilot word): the word's received pilots stay in registers
-  // (lane holds pilots lane + 32 j, up to 256 per pass over the row) while the
-  // warp walks the U rows of the weighted-LS matrix.
-  constexpr int YR = 8;
-  for (int q = warp; q < NP * np; q += nwarps) {
-    const int pair = q / np, p = q - pair * np;
-    const int t = pair % ntx, r = pair / ntx;
+  // One warp per (stream, pilot word, pair of receive antennas): the word's received
+  // pilots of both antennas stay in registers (lane holds pilots lane + 32 j, up to 160
+  // per pass over the row) while the warp walks the U rows of the stream's
+  // weighted-LS matrix, each row load serving both antennas. Per (antenna, tap) the
+  // lane sums run over j and the warp sum is the same shuffle tree as for one antenna.
+  constexpr int YR = 5;
+  const int rgroups = (nrx + 1) / 2;
+  for (int q = warp; q < ntx * np * rgroups; q += nwarps) {
+    const int t = q / (np * rgroups), rem = q - t * np * rgroups, p = rem / rgroups;
+    const int r0 = 2 * (rem - p * rgroups), nr = min(2, nrx - r0);
     const int word = e.pw_word[t * P + p], cnt = e.pw_count[t * P + p], off = e.pw_off[t * P + p];
-    const float2* yw = grid + (((int64_t)b * nrx + r) * W + word) * gcols;
     const float2* Gp = e.G + (int64_t)off * U;
     for (int k0 = 0; k0 < cnt; k0 += 32 * YR) {
-      float2 yv[YR];
+      float2 yv[2][YR];
 #pragma unroll
-      for (int j = 0; j < YR; ++j) {
-        const int k = k0 + lane + 32 * j;
-        yv[j] = k < cnt ? yw[e.pcol[off + k]] : make_float2(0.f, 0.f);
-      }
-      for (int u = 0; u < U; ++u) {
-        const float2* grow = Gp + (int64_t)u * cnt;
-        float2 acc = make_float2(0.f, 0.f);
+      for (int rr = 0; rr < 2; ++rr) {
+        const float2* yw = grid + (((int64_t)b * nrx + r0 + min(rr, nr - 1)) * W + word) * gcols;
 #pragma unroll
         for (int j = 0; j < YR; ++j) {
           const int k = k0 + lane + 32 * j;
-          if (k < cnt) cfma(acc, grow[k], yv[j]);
+          yv[rr][j] = k < cnt ? yw[e.pcol[off + k]] : make_float2(0.f, 0.f);
+        }
+      }
+      for (int u = 0; u < U; ++u) {
+        const float2* grow = Gp + (int64_t)u * cnt;
+        float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+        for (int j = 0; j < YR; ++j) {
+          const int k = k0 + lane + 32 * j;
+          if (k < cnt) {
+            const float2 g = grow[k];
+            cfma(acc[0], g, yv[0][j]);
+            cfma(acc[1], g, yv[1][j]);
+          }
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
-          acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+        for (int rr = 0; rr < 2; ++rr) {
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            acc[rr].x += __shfl_down_sync(0xffffffffu, acc[rr].x, o);
+            acc[rr].y += __shfl_down_sync(0xffffffffu, acc[rr].y, o);
+          }
         }
         if (lane == 0) {
-          float2* dst = gls + (pair * np + p) * U + u;
-          *dst = k0 == 0 ? acc : cadd(*dst, acc);
+          for (int rr = 0; rr < nr; ++rr) {
+            float2* dst = gls + (((r0 + rr) * ntx + t) * np + p) * U + u;
+            *dst = k0 == 0 ? acc[rr] : cadd(*dst, acc[rr]);
+          }
         }
       }
     }
