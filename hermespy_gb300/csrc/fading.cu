@@ -183,8 +183,10 @@ __global__ void k_fading_csi(FadingConst fc, FadingView v, int T, int ntaps, flo
 // centre as a degree-K Taylor polynomial in u = (m - m0 - BT/2) / (BT/2):
 //   h_l = sum_k C_lk u^k,  C_lk = (i H)^k / k! sum_n a_n w_n^k exp(i theta_n(t_c)),
 // exact to |w H|^(K+1)/(K+1)! per sinusoid; u depends on the output sample only,
-// so one set of powers serves every tap. DIRECT evaluates every sinusoid at every
-// sample instead (used when the Doppler rate makes the expansion long).
+// so one set of powers serves every tap. Taps that round to one sample delay
+// multiply the same transmit samples, so their coefficients are summed and the
+// convolution runs once per distinct delay. DIRECT evaluates every sinusoid at
+// every sample instead (used when the Doppler rate makes the expansion long).
 // The transmit tile is staged twice, the second copy shifted by one sample, so a
 // pair starting at any tap delay is one aligned 16-byte load.
 // Tile length per transmit-antenna count (shared memory holds 2 NTX tile rows).
@@ -200,25 +202,42 @@ __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(Fading
   extern __shared__ float4 smem4[];
   const int b = blockIdx.y;
   const int m0 = blockIdx.x * BT;
-  const int L = fc.L, S1 = fc.S1, D = fc.D, nrx = fc.nrx;
+  const int L = fc.L, G = fc.G, S1 = fc.S1, D = fc.D, nrx = fc.nrx;
   const int XW = tile_width(BT, D);  // even row width
   // Transmit tile as planes of real and imaginary parts, each stored twice: plane
   // (tx, q) with q = 0 re even, 1 im even, 2 re odd, 3 im odd; even copies hold
   // x[m0 - D + i], odd copies x[m0 - D + i + 1].
   float* xp = reinterpret_cast<float*>(smem4);                        // [NTX][4][XW]
-  float2* terms = reinterpret_cast<float2*>(smem4);                   // [L*S1][K+1], before the tile load
+  float2* terms = reinterpret_cast<float2*>(smem4);                   // [L*S1][K+1], before the tile store
   const int region = DIRECT ? 2 * NTX * XW : max(2 * NTX * XW, L * S1 * (K + 1));  // in float2
-  float4* coef = reinterpret_cast<float4*>(reinterpret_cast<float2*>(smem4) + region);  // [L][K+1] (x, x, y, y)
-  int64_t* wp = reinterpret_cast<int64_t*>(coef + L * (K + 1));       // [2][L*S1] (direct)
+  float4* coef = reinterpret_cast<float4*>(reinterpret_cast<float2*>(smem4) + region);  // [G][K+1] (x, x, y, y)
+  int64_t* wp = reinterpret_cast<int64_t*>(coef + G * (K + 1));       // [2][L*S1] (direct)
   float2* Sm = reinterpret_cast<float2*>(wp + (DIRECT ? 2 * L * S1 : 0));  // [nrx*NTX]
-  int* dl = reinterpret_cast<int*>(Sm + nrx * NTX);                   // [L]
+  int* dl = reinterpret_cast<int*>(Sm + nrx * NTX);                   // [G] group delays
+  int* gf = dl + G;                                                   // [G + 1] first tap of each group
   const int tid = threadIdx.x;
 
   const float2* Sg = v.spatial(b);
   for (int i = tid; i < nrx * NTX; i += PTHREADS) Sm[i] = Sg[i];
-  for (int l = tid; l < L; l += PTHREADS) dl[l] = fc.delay[l];
+  for (int g = tid; g <= G; g += PTHREADS) {
+    gf[g] = fc.gfirst[g];
+    if (g < G) dl[g] = fc.gdelay[g];
+  }
   const int64_t* Wg = v.W(b);
   const int64_t* Pg = v.P0(b);
+  // Transmit samples of the tile, fetched into registers first so that their load
+  // latency overlaps the coefficient set-up (tile samples beyond PF per thread, for
+  // delays above PTHREADS - 3 samples, are fetched afterwards).
+  constexpr int PF = NTX <= 4 ? BT / PTHREADS + 1 : 0;  // register budget: up to 4 transmit antennas
+  const float2* xb = x + (int64_t)b * NTX * T;
+  float2 xpf[NTX][PF > 0 ? PF : 1];
+#pragma unroll
+  for (int tx = 0; tx < NTX; ++tx)
+#pragma unroll
+    for (int i = 0; i < PF; ++i) {
+      const int j = tid + i * PTHREADS, t = m0 - D + j;
+      xpf[tx][i] = (j <= XW && t >= 0 && t < T) ? __ldg(xb + (int64_t)tx * T + t) : make_float2(0.f, 0.f);
+    }
   if (DIRECT) {
     for (int q = tid; q < L * S1; q += PTHREADS) {
       wp[q] = Wg[q];
@@ -230,11 +249,11 @@ __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(Fading
       const int l = q / S1, n = q - l * S1;
       const int64_t tc = (int64_t)m0 - fc.delay[l] + BT / 2;
       const uint64_t p = (uint64_t)Pg[q] + (uint64_t)Wg[q] * (uint64_t)tc;
-      float s, c;
-      __sincosf(fixed_to_angle(p), &s, &c);
+      float sn, cs;
+      __sincosf(fixed_to_angle(p), &sn, &cs);
       const float a = fc.amp[2 * l + (n < fc.S ? 0 : 1)];
       const float wh = fixed_rate(Wg[q]) * H;
-      float2 t = make_float2(a * c, a * s);
+      float2 t = make_float2(a * cs, a * sn);
       float2* dst = terms + q * (K + 1);
       dst[0] = t;
 #pragma unroll
@@ -245,33 +264,45 @@ __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(Fading
       }
     }
     __syncthreads();
-    for (int q = tid; q < L * (K + 1); q += PTHREADS) {
-      const int l = q / (K + 1), k = q - l * (K + 1);
+    for (int q = tid; q < G * (K + 1); q += PTHREADS) {
+      const int g = q / (K + 1), k = q - g * (K + 1);
       float2 acc = make_float2(0.f, 0.f);
-      for (int n = 0; n < S1; ++n) acc = cadd(acc, terms[(l * S1 + n) * (K + 1) + k]);
+      for (int l = gf[g]; l < gf[g + 1]; ++l)
+        for (int n = 0; n < S1; ++n) acc = cadd(acc, terms[(l * S1 + n) * (K + 1) + k]);
       coef[q] = make_float4(acc.x, acc.x, acc.y, acc.y);  // broadcast pairs for the packed FMAs
     }
   }
   __syncthreads();  // terms consumed: the tile may overwrite them
-  const float2* xb = x + (int64_t)b * NTX * T;
-#pragma unroll 1
-  for (int tx = 0; tx < NTX; ++tx) {
-    const float2* xr = xb + (int64_t)tx * T;
+  auto put = [&](int tx, int j, float2 val) {
     float* pl = xp + tx * 4 * XW;
-    for (int j = tid; j <= XW; j += PTHREADS) {
-      const int t = m0 - D + j;
-      const float2 val = (t >= 0 && t < T) ? __ldg(xr + t) : make_float2(0.f, 0.f);
-      if (j < XW) {
-        pl[j] = val.x;
-        pl[XW + j] = val.y;
-      }
-      if (j > 0) {
-        pl[2 * XW + j - 1] = val.x;
-        pl[3 * XW + j - 1] = val.y;
-      }
+    if (j < XW) {
+      pl[j] = val.x;
+      pl[XW + j] = val.y;
     }
+    if (j > 0) {
+      pl[2 * XW + j - 1] = val.x;
+      pl[3 * XW + j - 1] = val.y;
+    }
+  };
+#pragma unroll
+  for (int tx = 0; tx < NTX; ++tx)
+#pragma unroll
+    for (int i = 0; i < PF; ++i) {
+      const int j = tid + i * PTHREADS;
+      if (j <= XW) put(tx, j, xpf[tx][i]);
+    }
+  if (XW >= PF * PTHREADS) {
+#pragma unroll 1
+    for (int tx = 0; tx < NTX; ++tx)
+      for (int j = tid + PF * PTHREADS; j <= XW; j += PTHREADS) {
+        const int t = m0 - D + j;
+        put(tx, j, (t >= 0 && t < T) ? __ldg(xb + (int64_t)tx * T + t) : make_float2(0.f, 0.f));
+      }
   }
   __syncthreads();
+  // warps whose samples all lie past the end of the received signal (last tile)
+  const int TD = T + D;
+  if (m0 + 2 * (tid & ~31) >= TD) return;
 
   // ---- convolution: z_tx[m] = sum_l h_l[m - d_l] x_tx[m - d_l], two samples per
   // packed FP32x2 FMA: zr/zi hold the real/imaginary parts of a pair of samples.
@@ -293,20 +324,24 @@ __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(Fading
     for (int k = 1; k <= K; ++k) up[pr][k] = make_float2(up[pr][k - 1].x * u0, up[pr][k - 1].y * u1);
   }
 #pragma unroll 1
-  for (int l = 0; l < L; ++l) {
-    const int d = dl[l];
+  for (int g = 0; g < G; ++g) {
+    const int d = dl[g];
     float2 hx[PPT], hy[PPT];
     if (DIRECT) {
-      const float an = fc.amp[2 * l], al = fc.amp[2 * l + 1];
 #pragma unroll
-      for (int pr = 0; pr < PPT; ++pr) {
-        const float2 h0 = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al, (int64_t)m0 + jp[pr] - d);
-        const float2 h1 = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al, (int64_t)m0 + jp[pr] + 1 - d);
-        hx[pr] = make_float2(h0.x, h1.x);
-        hy[pr] = make_float2(h0.y, h1.y);
+      for (int pr = 0; pr < PPT; ++pr) hx[pr] = hy[pr] = make_float2(0.f, 0.f);
+      for (int l = gf[g]; l < gf[g + 1]; ++l) {
+        const float an = fc.amp[2 * l], al = fc.amp[2 * l + 1];
+#pragma unroll
+        for (int pr = 0; pr < PPT; ++pr) {
+          const float2 h0 = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al, (int64_t)m0 + jp[pr] - d);
+          const float2 h1 = tap_direct(wp + l * S1, wp + L * S1 + l * S1, fc.S, an, al, (int64_t)m0 + jp[pr] + 1 - d);
+          hx[pr] = make_float2(hx[pr].x + h0.x, hx[pr].y + h1.x);
+          hy[pr] = make_float2(hy[pr].x + h0.y, hy[pr].y + h1.y);
+        }
       }
     } else {
-      const float4* cl = coef + l * (K + 1);
+      const float4* cl = coef + g * (K + 1);
       float4 ck[K + 1];
 #pragma unroll
       for (int k = 0; k <= K; ++k) ck[k] = cl[k];
@@ -343,7 +378,6 @@ __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(Fading
   }
 
   // ---- spatial mixing, AWGN, store
-  const int TD = T + D;
   const float np = noise_power ? noise_power[b] : 0.0f;
   const float sigma = sqrtf(0.5f * np);
 #pragma unroll 1
@@ -399,6 +433,7 @@ __global__ void k_ideal_csi(FadingConst fc, FadingView v, int N, int W, const in
 void release(hpx_fading* f) {
   if (!f) return;
   if (f->d_delay) cudaFree(f->d_delay);
+  if (f->d_group) cudaFree(f->d_group);
   if (f->d_amp) cudaFree(f->d_amp);
   if (f->d_rx_corr) cudaFree(f->d_rx_corr);
   if (f->d_tx_corr) cudaFree(f->d_tx_corr);
@@ -413,7 +448,7 @@ int taylor_degree(const hpx_fading* f, int BT) {
   if (wmax > kPi) wmax = 2.0 * kPi - wmax;
   if (rate > kPi) wmax = kPi;  // cos() spreads the sinusoid rates over [-rate, rate]
   const double theta = wmax * 0.5 * BT;
-  const int degrees[3] = {2, 4, 8};
+  const int degrees[6] = {2, 3, 4, 5, 6, 8};
   for (int K : degrees) {
     double bound = 1.0;
     for (int k = 1; k <= K + 1; ++k) bound *= theta / k;
@@ -430,9 +465,9 @@ hpx_status launch_propagate(const hpx_fading* f, const void* state, int B, const
   constexpr int BT = tile_len<NTX>();
   const size_t tile = 2 * (size_t)NTX * tile_width(BT, fc.D) * sizeof(float2);
   const size_t terms = DIRECT ? 0 : (size_t)fc.L * fc.S1 * (K + 1) * sizeof(float2);
-  const size_t smem = (tile > terms ? tile : terms) + (size_t)fc.L * (K + 1) * sizeof(float4) +
+  const size_t smem = (tile > terms ? tile : terms) + (size_t)fc.G * (K + 1) * sizeof(float4) +
                       (DIRECT ? 2 * (size_t)fc.L * fc.S1 * sizeof(int64_t) : 0) +
-                      (size_t)fc.nrx * NTX * sizeof(float2) + (size_t)fc.L * sizeof(int) + 16;
+                      (size_t)fc.nrx * NTX * sizeof(float2) + (size_t)(2 * fc.G + 1) * sizeof(int) + 16;
   if (smem > 200 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "propagate: channel too long for one tile");
   // Two pairs per thread: one pair (512 threads, 62 registers, 2 CTAs/SM) took 7.4 ms and
   // four pairs (152 registers) 6.2 ms for 8 192 drops of the 4 x 4 link, against 5.5 ms.
@@ -452,7 +487,10 @@ hpx_status dispatch_degree(const hpx_fading* f, const void* state, int B, const 
                            const float* np, uint64_t seed, int64_t drop0, cudaStream_t s) {
   switch (taylor_degree(f, tile_len<NTX>())) {
     case 2: return launch_propagate<NTX, 2, false>(f, state, B, x, T, y, np, seed, drop0, s);
+    case 3: return launch_propagate<NTX, 3, false>(f, state, B, x, T, y, np, seed, drop0, s);
     case 4: return launch_propagate<NTX, 4, false>(f, state, B, x, T, y, np, seed, drop0, s);
+    case 5: return launch_propagate<NTX, 5, false>(f, state, B, x, T, y, np, seed, drop0, s);
+    case 6: return launch_propagate<NTX, 6, false>(f, state, B, x, T, y, np, seed, drop0, s);
     case 8: return launch_propagate<NTX, 8, false>(f, state, B, x, T, y, np, seed, drop0, s);
     default: return launch_propagate<NTX, 0, true>(f, state, B, x, T, y, np, seed, drop0, s);
   }
@@ -530,9 +568,22 @@ hpx_status hpx_fading_create(const hpx_fading_desc* d, hpx_fading** out) {
     amp[2 * l] = f->h_amp_nlos[l];
     amp[2 * l + 1] = f->h_amp_los[l];
   }
+  // Delay groups: taps that round to one sample delay share every transmit sample, so
+  // propagation sums their responses before the convolution.
+  std::vector<int32_t> gfirst, gdelay;
+  for (int l = 0; l < L; ++l)
+    if (l == 0 || f->h_delay[l] != f->h_delay[l - 1]) {
+      gfirst.push_back(l);
+      gdelay.push_back(f->h_delay[l]);
+    }
+  f->G = (int)gdelay.size();
+  gfirst.push_back(L);
+  gfirst.insert(gfirst.end(), gdelay.begin(), gdelay.end());
   cudaError_t e;
   if ((e = cudaMalloc(&f->d_delay, L * sizeof(int32_t))) != cudaSuccess ||
       (e = cudaMemcpy(f->d_delay, f->h_delay.data(), L * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMalloc(&f->d_group, gfirst.size() * sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMemcpy(f->d_group, gfirst.data(), gfirst.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMalloc(&f->d_amp, 2 * L * sizeof(float))) != cudaSuccess ||
       (e = cudaMemcpy(f->d_amp, amp.data(), 2 * L * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess) {
     release(f);

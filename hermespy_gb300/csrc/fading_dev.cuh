@@ -5,7 +5,10 @@
 
 struct FadingConst {
   int L, S, S1, nrx, ntx, D;
+  int G;                 // distinct delays
   const int32_t* delay;  // [L]
+  const int32_t* gfirst; // [G + 1] first tap of each delay group (delays are sorted)
+  const int32_t* gdelay; // [G] delay of each group
   const float* amp;      // [L][2] (nlos, los)
 };
 
@@ -17,7 +20,10 @@ static inline FadingConst fading_const(const hpx_fading* f) {
   c.nrx = f->nrx;
   c.ntx = f->ntx;
   c.D = f->max_delay;
+  c.G = f->G;
   c.delay = f->d_delay;
+  c.gfirst = f->d_group;
+  c.gdelay = f->d_group ? f->d_group + f->G + 1 : nullptr;
   c.amp = f->d_amp;
   return c;
 }

@@ -172,11 +172,13 @@ struct hpx_fading {
   int nrx, ntx;
   double fs, doppler, los_doppler, gain;
   int max_delay;  // D
+  int G;          // distinct tap delays (taps sharing one sample delay form a group)
   std::vector<int32_t> h_delay;
   std::vector<float> h_amp_nlos, h_amp_los;  // sqrt(gain g_l) * gain_{nlos,los}
   std::vector<double> h_rx_corr, h_tx_corr;  // complex interleaved, empty if none
   // device copies
   int32_t* d_delay = nullptr;
+  int32_t* d_group = nullptr;   // [G + 1] first tap of each delay group, then [G] group delays
   float* d_amp = nullptr;       // [L][2] (nlos, los)
   double* d_rx_corr = nullptr;  // [nrx*nrx*2] or null
   double* d_tx_corr = nullptr;
