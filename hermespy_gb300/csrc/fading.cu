@@ -195,7 +195,8 @@ __host__ __device__ constexpr int tile_len() { return NTX <= 4 ? 1024 : (NTX <= 
 
 __host__ __device__ constexpr int tile_width(int BT, int D) { return (BT + D + 2) & ~1; }
 
-template <int NTX, int K, bool DIRECT, int PPT = 2, int BT = tile_len<NTX>(), int PTHREADS = tile_len<NTX>() / (2 * PPT)>
+template <int NTX, int K, bool DIRECT, int XS = 0, int PPT = 2, int BT = tile_len<NTX>(),
+          int PTHREADS = tile_len<NTX>() / (2 * PPT)>
 __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(FadingConst fc, FadingView v, int T, const float2* __restrict__ x,
                                                         float2* __restrict__ y, const float* __restrict__ noise_power,
                                                         uint64_t seed, int64_t drop0) {
@@ -203,13 +204,14 @@ __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(Fading
   const int b = blockIdx.y;
   const int m0 = blockIdx.x * BT;
   const int L = fc.L, G = fc.G, S1 = fc.S1, D = fc.D, nrx = fc.nrx;
-  const int XW = tile_width(BT, D);  // even row width
+  const int XW = tile_width(BT, D);  // samples of a row (even)
+  const int PS = XS ? XS : XW;       // row stride: a compile-time constant for short channels
   // Transmit tile as planes of real and imaginary parts, each stored twice: plane
   // (tx, q) with q = 0 re even, 1 im even, 2 re odd, 3 im odd; even copies hold
   // x[m0 - D + i], odd copies x[m0 - D + i + 1].
-  float* xp = reinterpret_cast<float*>(smem4);                        // [NTX][4][XW]
+  float* xp = reinterpret_cast<float*>(smem4);                        // [NTX][4][PS]
   float2* terms = reinterpret_cast<float2*>(smem4);                   // [L*S1][K+1], before the tile store
-  const int region = DIRECT ? 2 * NTX * XW : max(2 * NTX * XW, L * S1 * (K + 1));  // in float2
+  const int region = DIRECT ? 2 * NTX * PS : max(2 * NTX * PS, L * S1 * (K + 1));  // in float2
   float4* coef = reinterpret_cast<float4*>(reinterpret_cast<float2*>(smem4) + region);  // [G][K+1] (x, x, y, y)
   int64_t* wp = reinterpret_cast<int64_t*>(coef + G * (K + 1));       // [2][L*S1] (direct)
   float2* Sm = reinterpret_cast<float2*>(wp + (DIRECT ? 2 * L * S1 : 0));  // [nrx*NTX]
@@ -274,14 +276,14 @@ __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(Fading
   }
   __syncthreads();  // terms consumed: the tile may overwrite them
   auto put = [&](int tx, int j, float2 val) {
-    float* pl = xp + tx * 4 * XW;
+    float* pl = xp + tx * 4 * PS;
     if (j < XW) {
       pl[j] = val.x;
-      pl[XW + j] = val.y;
+      pl[PS + j] = val.y;
     }
     if (j > 0) {
-      pl[2 * XW + j - 1] = val.x;
-      pl[3 * XW + j - 1] = val.y;
+      pl[2 * PS + j - 1] = val.x;
+      pl[3 * PS + j - 1] = val.y;
     }
   };
 #pragma unroll
@@ -359,16 +361,16 @@ __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(Fading
     }
     // all lanes share the parity of D - d, hence the same copy: conflict-free
     const int odd = (D - d) & 1;
-    const float* src = xp + 2 * odd * XW - odd;  // plane offset of the even/odd copy, index shifted by one
+    const float* src = xp + 2 * odd * PS - odd;  // plane offset of the even/odd copy, index shifted by one
 #pragma unroll
     for (int pr = 0; pr < PPT; ++pr) {
       const int s0 = jp[pr] - d + D;
       const float2 nhy = make_float2(-hy[pr].x, -hy[pr].y);
 #pragma unroll
       for (int tx = 0; tx < NTX; ++tx) {
-        const float* pl = src + tx * 4 * XW + s0;
+        const float* pl = src + tx * 4 * PS + s0;
         const float2 re = *reinterpret_cast<const float2*>(pl);
-        const float2 im = *reinterpret_cast<const float2*>(pl + XW);
+        const float2 im = *reinterpret_cast<const float2*>(pl + PS);
         zr[pr][tx] = __ffma2_rn(hx[pr], re, zr[pr][tx]);
         zr[pr][tx] = __ffma2_rn(nhy, im, zr[pr][tx]);
         zi[pr][tx] = __ffma2_rn(hx[pr], im, zi[pr][tx]);
@@ -457,13 +459,13 @@ int taylor_degree(const hpx_fading* f, int BT) {
   return -1;
 }
 
-template <int NTX, int K, bool DIRECT>
+template <int NTX, int K, bool DIRECT, int XS>
 hpx_status launch_propagate(const hpx_fading* f, const void* state, int B, const hpx_cf32* x, int T, hpx_cf32* y,
                             const float* np, uint64_t seed, int64_t drop0, cudaStream_t s) {
   const FadingConst fc = fading_const(f);
   const FadingView v = fading_view(f, state);
   constexpr int BT = tile_len<NTX>();
-  const size_t tile = 2 * (size_t)NTX * tile_width(BT, fc.D) * sizeof(float2);
+  const size_t tile = 2 * (size_t)NTX * (XS ? XS : tile_width(BT, fc.D)) * sizeof(float2);
   const size_t terms = DIRECT ? 0 : (size_t)fc.L * fc.S1 * (K + 1) * sizeof(float2);
   const size_t smem = (tile > terms ? tile : terms) + (size_t)fc.G * (K + 1) * sizeof(float4) +
                       (DIRECT ? 2 * (size_t)fc.L * fc.S1 * sizeof(int64_t) : 0) +
@@ -472,7 +474,7 @@ hpx_status launch_propagate(const hpx_fading* f, const void* state, int B, const
   // Two pairs per thread: one pair (512 threads, 62 registers, 2 CTAs/SM) took 7.4 ms and
   // four pairs (152 registers) 6.2 ms for 8 192 drops of the 4 x 4 link, against 5.5 ms.
   constexpr int PPT = 2;
-  auto kern = k_propagate<NTX, K, DIRECT, PPT>;
+  auto kern = k_propagate<NTX, K, DIRECT, XS, PPT>;
   if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int TD = T + fc.D;
   dim3 grid((TD + BT - 1) / BT, B);
@@ -482,18 +484,29 @@ hpx_status launch_propagate(const hpx_fading* f, const void* state, int B, const
   return HPX_OK;
 }
 
+// Short channels (D <= 62 samples) with up to four transmit antennas use a fixed row
+// stride, so the per-antenna and per-plane offsets of the tap loop are immediates.
+template <int NTX, int XS>
+hpx_status dispatch_degree_xs(const hpx_fading* f, const void* state, int B, const hpx_cf32* x, int T, hpx_cf32* y,
+                              const float* np, uint64_t seed, int64_t drop0, cudaStream_t s) {
+  switch (taylor_degree(f, tile_len<NTX>())) {
+    case 2: return launch_propagate<NTX, 2, false, XS>(f, state, B, x, T, y, np, seed, drop0, s);
+    case 3: return launch_propagate<NTX, 3, false, XS>(f, state, B, x, T, y, np, seed, drop0, s);
+    case 4: return launch_propagate<NTX, 4, false, XS>(f, state, B, x, T, y, np, seed, drop0, s);
+    case 5: return launch_propagate<NTX, 5, false, XS>(f, state, B, x, T, y, np, seed, drop0, s);
+    case 6: return launch_propagate<NTX, 6, false, XS>(f, state, B, x, T, y, np, seed, drop0, s);
+    case 8: return launch_propagate<NTX, 8, false, XS>(f, state, B, x, T, y, np, seed, drop0, s);
+    default: return launch_propagate<NTX, 0, true, 0>(f, state, B, x, T, y, np, seed, drop0, s);
+  }
+}
+
 template <int NTX>
 hpx_status dispatch_degree(const hpx_fading* f, const void* state, int B, const hpx_cf32* x, int T, hpx_cf32* y,
                            const float* np, uint64_t seed, int64_t drop0, cudaStream_t s) {
-  switch (taylor_degree(f, tile_len<NTX>())) {
-    case 2: return launch_propagate<NTX, 2, false>(f, state, B, x, T, y, np, seed, drop0, s);
-    case 3: return launch_propagate<NTX, 3, false>(f, state, B, x, T, y, np, seed, drop0, s);
-    case 4: return launch_propagate<NTX, 4, false>(f, state, B, x, T, y, np, seed, drop0, s);
-    case 5: return launch_propagate<NTX, 5, false>(f, state, B, x, T, y, np, seed, drop0, s);
-    case 6: return launch_propagate<NTX, 6, false>(f, state, B, x, T, y, np, seed, drop0, s);
-    case 8: return launch_propagate<NTX, 8, false>(f, state, B, x, T, y, np, seed, drop0, s);
-    default: return launch_propagate<NTX, 0, true>(f, state, B, x, T, y, np, seed, drop0, s);
-  }
+  constexpr int XS = tile_len<NTX>() + 64;
+  if (NTX <= 4 && tile_width(tile_len<NTX>(), f->max_delay) <= XS)
+    return dispatch_degree_xs<NTX, NTX <= 4 ? XS : 0>(f, state, B, x, T, y, np, seed, drop0, s);
+  return dispatch_degree_xs<NTX, 0>(f, state, B, x, T, y, np, seed, drop0, s);
 }
 
 }  // namespace
