@@ -57,6 +57,12 @@ FADING_CASES = {
     "fast": (np.array([0, 3, 7, 19]), np.array([1.0, 0.5, 0.3, 0.1]), np.array([0.0, 1.0, 0.0, 2.0]), 5,
              50 * 1e6, 20 * 1e6, 0.987, 2, 3, 700, 1e6),
     "los": (np.array([0, 2]), np.array([1.0, 0.2]), np.array([np.inf, 3.0]), 7, 1e5, 3e4, 1.0, 1, 2, 500, 1e6),
+    # taps rounding to one sample delay (groups at 0, 1 and 3 samples), LOS and NLOS
+    # taps mixed inside a group; slow Doppler (Taylor tiles) and fast (direct sums)
+    "grp": (np.array([0.0, 0.4, 1.2, 1.4, 3.0, 3.3, 3.45]), np.array([1.0, 0.7, 0.5, 0.4, 0.3, 0.2, 0.1]),
+            np.array([np.inf, 0.0, 1.5, 0.0, 0.0, 2.0, np.inf]), 9, 100.0, 50.0, 1.0, 2, 2, 900, 1e6),
+    "grp_fast": (np.array([0.0, 0.4, 1.2, 1.4, 3.0, 3.3, 3.45]), np.array([1.0, 0.7, 0.5, 0.4, 0.3, 0.2, 0.1]),
+                 np.array([np.inf, 0.0, 1.5, 0.0, 0.0, 2.0, np.inf]), 9, 2e4, 1e4, 1.0, 2, 2, 900, 1e6),
 }
 
 

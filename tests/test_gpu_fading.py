@@ -93,7 +93,7 @@ def test_propagate_golden(golden):
         assert rel_rms(csi, st) < TOL
 
 
-@pytest.mark.parametrize("name", ["c1", "c2", "los"])
+@pytest.mark.parametrize("name", ["c1", "c2", "los", "grp"])
 def test_channel_state(name):
     cfg, nrx, ntx, T, fs = fading_case(name)
     h = fading_handle(cfg, nrx, ntx, fs)

@@ -54,7 +54,7 @@ def _with_dc(spec, dc):
     return s
 
 
-@pytest.mark.parametrize("name", ["c1", "c2", "fast", "los"])
+@pytest.mark.parametrize("name", ["c1", "c2", "fast", "los", "grp", "grp_fast"])
 def test_fading_golden(golden, name):
     g = golden("fading.npz")
     cfg, nrx, ntx, T, fs = fading_case(name)
