@@ -463,7 +463,8 @@ def bench_estimators(ctx, spec, args):
     for name, r in results.items():
         ms = r["total_ms"] / args.steps
         comparison[name] = {"bits_per_s": drops * spec.bits_per_drop / (ms / 1e3), "ms_per_step": round(ms, 4),
-                            "ber": r["ber"], "nmse_db": nm[name]}
+                            "ber": r["ber"], "nmse_db": nm[name],
+                            "stages_ms": {k: round(v / args.steps, 4) for k, v in r["stage_ms"].items()}}
     sel = results[selected]
     # lmmse: realize, transmit, propagate, receive, then gains + tensor-core receiver per
     # chunk of 8 192 drops

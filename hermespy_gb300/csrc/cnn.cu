@@ -6,19 +6,24 @@
 //   h_l = relu(conv3x3_l(h_{l-1}) + b_l), l = 1..5;  out = LS + s (conv3x3_6(h_5) + b_6)
 // so the network works at unit scale whatever the channel energy and SNR.
 //
-// Activations are BF16 NHWC ([drop][word][column][32 channels], 64 bytes per grid
-// element); every layer is an implicit GEMM (M = grid elements, N = 32 output
-// channels, K = 9 taps x 32 input channels) on the BF16 tensor cores with FP32
-// accumulation (mma.sync m16n8k16). Training runs the same forward kernel, its
-// transpose for the input gradients (weights flipped and transposed), a
-// weight-gradient kernel and Adam on FP32 master weights.
+// Every layer is an implicit GEMM (M = grid elements, N = 32 output channels,
+// K = 9 taps x 32 input channels) on the BF16 tensor cores with FP32 accumulation.
+// Inference (hpx_cnn_refine) runs on TMA + tcgen05 (k_conv3x3_tc: 128 output
+// elements of one word per MMA tile, accumulators in tensor memory) with planar
+// activations [drop][4 chunks of 8 channels][word][column][8]. Training keeps NHWC
+// activations ([drop][word][column][32 channels]) for its mma.sync m16n8k16 kernels:
+// forward, the input-gradient pass (the forward kernel's transpose, weights flipped
+// and transposed) and the weight gradients; Adam updates FP32 master weights.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <random>
 #include <vector>
 
 #include "hpx_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace {
 
@@ -181,6 +186,215 @@ __global__ void __launch_bounds__(128) k_conv3x3(int H, int W, const __nv_bfloat
     }
 }
 
+// ------------------------------------------------------------ tcgen05 forward
+// One tile = 128 consecutive output columns of one word of one drop (thread i <->
+// TMEM lane i <-> column w0 + i). The input rows h - 1, h, h + 1 over columns
+// w0 - 1 .. w0 + 128 arrive by TMA as four planes of 8 channels: a 4-D tensor map
+// over the planar activation (channel in chunk, column, word, 4 drop + chunk) with
+// box (8, 130, 3, 1) delivers plane j as three contiguous 2 080-byte rows (row r,
+// column p at (r 130 + p) 16 bytes), zero outside the grid. For tap (dy, dx)
+// the A operand (128 elements x 16 channels) is then the K-major, unswizzled
+// operand that starts at element (dy, dx) of planes 2 kc and 2 kc + 1: rows 16
+// bytes apart (core matrices 128 bytes apart along M), the two 8-channel halves a
+// plane apart along K. The weights of tap t and channel half kc form a 32 x 16
+// K-major block. Eighteen MMAs (M = 128, N = 32, K = 16, BF16 in, FP32 out) give
+// the tile. The CTA walks tiles persistently as a pipeline: two input stages
+// (the TMA of tile k + 2 starts as soon as the MMAs of tile k have read their
+// stage) and two accumulator slots in tensor memory (the MMAs of tile k run while
+// the epilogue of tile k - 1 reads the other slot). A tensor-core or TMA wait that
+// times out writes NaN outputs and sets *fail.
+constexpr int TCW = 128;                           // output columns per tile
+constexpr int TC_INW = TCW + 2;                    // input columns with halo
+constexpr int TC_BOX = 3 * TC_INW * 16;            // bytes of one TMA box (one plane)
+constexpr int TC_PLANE = (TC_BOX + 127) / 128 * 128;  // plane stride (TMA destinations 128-byte aligned)
+constexpr int TC_BUF = 4 * TC_PLANE;               // one input stage
+constexpr int TC_STAGES = 2;                       // input stages in flight per CTA
+constexpr int TC_WBLK = CH * 16 * 2;               // one 32 x 16 bf16 weight block
+constexpr int TC_SMEM = TC_STAGES * TC_BUF + 18 * TC_WBLK + 128;  // + alignment slack
+constexpr uint32_t TC_IDESC = tc::idesc_f16_f32(128, CH) | (1u << 7) | (1u << 10);  // A, B: BF16
+constexpr long long TC_CONV_WAIT = 40ll * 1000 * 1000;  // cycles (~20 ms)
+constexpr int TC_CTAS_PER_SM = 3;                  // shared memory: 3 x 67 KB
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(tc::smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(tc::smem_u32(bar))
+      : "memory");
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(128, TC_CTAS_PER_SM) k_conv3x3_tc(const __grid_constant__ CUtensorMap tmap, int B,
+                                                                    int H, int W, const __nv_bfloat16* __restrict__ wt,
+                                                                    const float* __restrict__ bias,
+                                                                    __nv_bfloat16* __restrict__ out,
+                                                                    const float2* resid, float2* out_c, int ccols,
+                                                                    const float* __restrict__ pw, float inv_count,
+                                                                    int* fail) {
+  extern __shared__ unsigned char sm_raw[];
+  unsigned char* sm = sm_raw + ((128u - (tc::smem_u32(sm_raw) & 127u)) & 127u);
+  unsigned char* s_in = sm;                    // [TC_STAGES][4 planes]
+  unsigned char* s_w = sm + TC_STAGES * TC_BUF;  // [9 taps x 2 halves] weight blocks
+  __shared__ uint64_t bar_in[TC_STAGES], bar_mma[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ float s_bias[CH];
+  __shared__ int skip;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // weights: element (n, tap 32 + c) -> block (tap, c / 16), K-major inside
+  for (int q = tid; q < CH * 36; q += 128) {
+    const int n = q / 36, r = q - n * 36, tap = r >> 2, c8 = r & 3;
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(wt + n * KK + tap * CH + c8 * 8));
+    *reinterpret_cast<uint4*>(s_w + (tap * 2 + (c8 >> 1)) * TC_WBLK + tc::kmajor_offset(n, (c8 & 1) * 8, 16)) = v;
+  }
+  if (tid < CH) s_bias[tid] = bias[tid];
+  if (tid == 0) {
+    skip = *(volatile int*)fail;
+    for (int i = 0; i < TC_STAGES; ++i) tc::mbar_init(&bar_in[i], 1);
+    tc::mbar_init(&bar_mma[0], 1);
+    tc::mbar_init(&bar_mma[1], 1);
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_slot, 64);  // two accumulator slots of 32 columns
+    tc::tmem_relinquish();
+  }
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  bool ok = skip == 0;
+  const uint64_t b_desc = tc::smem_desc(s_w, 128, 256);
+  const int tiles_w = (W + TCW - 1) / TCW;
+  const int64_t ntiles = (int64_t)B * H * tiles_w;
+  // tiles of this CTA: blockIdx.x + k gridDim.x, k < K
+  const int K = blockIdx.x < ntiles ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x) + 1 : 0;
+  auto decode = [&](int k, int& b, int& h, int& w0) {
+    const int64_t tile = blockIdx.x + (int64_t)k * gridDim.x;
+    const int64_t bh = tile / tiles_w;
+    w0 = (int)(tile - bh * tiles_w) * TCW;
+    b = (int)(bh / H);
+    h = (int)(bh - (int64_t)b * H);
+  };
+  int issued[TC_STAGES] = {}, landed[TC_STAGES] = {};  // thread 0: TMA phases per stage
+  auto issue = [&](int k) {  // thread 0: the four planes of tile k into stage k % TC_STAGES
+    const int st = k % TC_STAGES;
+    int b, h, w0;
+    decode(k, b, h, w0);
+    ++issued[st];
+    mbar_expect_tx(&bar_in[st], 4 * TC_BOX);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) tma_load_4d(s_in + st * TC_BUF + j * TC_PLANE, &tmap, 0, w0 - 1, h - 1, 4 * b + j, &bar_in[st]);
+  };
+  if (tid == 0 && ok)
+    for (int k = 0; k < TC_STAGES && k < K; ++k) issue(k);
+  // Iteration k issues the MMAs of tile k (accumulator slot k & 1) and then finishes
+  // tile k - 1: its MMAs done, its stage refilled with tile k + 2, its epilogue.
+  for (int k = 0; k <= K; ++k) {
+    if (k < K) {
+      const int st = k % TC_STAGES;
+      if (ok) ok = tc::mbar_wait(&bar_in[st], (uint32_t)((k / TC_STAGES) & 1), TC_CONV_WAIT);
+      if (tid == 0 && ok) {
+        ++landed[st];
+        // every operand is a fixed offset from the two buffers: the descriptors differ
+        // from the buffers' only in the start-address field (address / 16)
+        const uint64_t a_desc = tc::smem_desc(s_in + st * TC_BUF, TC_PLANE, 128);
+        const uint32_t d = tmem + (uint32_t)((k & 1) * 32);
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+          const int dy = tap / 3, dx = tap - dy * 3;
+#pragma unroll
+          for (int kc = 0; kc < 2; ++kc) {
+            const uint64_t ad = a_desc + (uint64_t)((2 * kc * TC_PLANE + (dy * TC_INW + dx) * 16) >> 4);
+            const uint64_t bd = b_desc + (uint64_t)(((tap * 2 + kc) * TC_WBLK) >> 4);
+            tc::mma_f16(d, ad, bd, TC_IDESC, (tap | kc) != 0);
+          }
+        }
+        tc::mma_commit(&bar_mma[k & 1]);
+      }
+    }
+    if (k == 0) continue;
+    const int j = k - 1;
+    if (ok) ok = tc::mbar_wait(&bar_mma[j & 1], (uint32_t)((j >> 1) & 1), TC_CONV_WAIT);
+    tc::fence_after_sync();
+    // the MMAs of tile j have read their stage: refill it
+    if (tid == 0 && ok && j + TC_STAGES < K) issue(j + TC_STAGES);
+    int b, h, w0;
+    decode(j, b, h, w0);
+    float acc[32];
+    tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((j & 1) * 32), acc);
+    const int w = w0 + tid;
+    if (w < W) {
+      const float nan = __int_as_float(0x7fc00000);
+      if (EPI == 0) {
+        uint32_t u[NPAIR];
+#pragma unroll
+        for (int i = 0; i < NPAIR; ++i)
+          u[i] = ok ? bf2_bits(fmaxf(acc[2 * i] + s_bias[2 * i], 0.f), fmaxf(acc[2 * i + 1] + s_bias[2 * i + 1], 0.f))
+                    : bf2_bits(nan, nan);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          *reinterpret_cast<uint4*>(out + ((((int64_t)b * 4 + j) * H + h) * W + w) * 8) =
+              make_uint4(u[4 * j], u[4 * j + 1], u[4 * j + 2], u[4 * j + 3]);
+      } else {
+        // resid may be out_c itself: every residual of this element is read before the
+        // first store, so the 16 loads are in flight together
+        const float scale = sqrtf(pw[b] * inv_count);
+        const int64_t e0 = ((int64_t)b * NPAIR * H + h) * ccols + w, es = (int64_t)H * ccols;
+        float2 x[NPAIR];
+#pragma unroll
+        for (int i = 0; i < NPAIR; ++i) x[i] = resid[e0 + i * es];
+#pragma unroll
+        for (int i = 0; i < NPAIR; ++i)
+          out_c[e0 + i * es] = ok ? make_float2(fmaf(scale, acc[2 * i] + s_bias[2 * i], x[i].x),
+                                                fmaf(scale, acc[2 * i + 1] + s_bias[2 * i + 1], x[i].y))
+                                  : make_float2(nan, nan);
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();  // slot j & 1 read by every warp before the MMAs of tile j + 2
+    tc::fence_after_sync();
+  }
+  if (tid == 0)  // after a timeout: let copies still in flight land (bounded) before leaving
+    for (int st = 0; st < TC_STAGES; ++st)
+      for (; landed[st] < issued[st]; ++landed[st])
+        tc::mbar_wait(&bar_in[st], (uint32_t)(landed[st] & 1), TC_CONV_WAIT);
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (!ok && skip == 0) atomicExch(fail, 1);
+}
+
+// Tensor map of a planar BF16 activation [B][4 chunks][H][W][8] with the conv tile's box:
+// dimensions (channel in chunk, column, word, 4 drop + chunk).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+hpx_status activation_map(const __nv_bfloat16* act, int B, int H, int W, CUtensorMap* map) {
+  static EncodeTiledFn encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    HPX_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !fn)
+      return hpx_fail(HPX_ERR_CUDA, "cnn: cuTensorMapEncodeTiled unavailable");
+    encode = reinterpret_cast<EncodeTiledFn>(fn);
+  }
+  const cuuint64_t dims[4] = {8, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B * 4};
+  const cuuint64_t strides[3] = {16, (cuuint64_t)W * 16, (cuuint64_t)H * W * 16};
+  const cuuint32_t box[4] = {8, (cuuint32_t)TC_INW, 3, 1};
+  const cuuint32_t estride[4] = {1, 1, 1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(act), dims, strides,
+                            box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return hpx_fail(HPX_ERR_CUDA, "cnn: tensor map encoding failed (%d)", (int)r);
+  return HPX_OK;
+}
+
 // Weight and bias gradients of one layer: dW[n][tap*32 + c] += sum_p dY[p][n] X[p + tap][c],
 // db[n] += sum_p dY[p][n] over all grid elements of the batch. Nine warps, warp = tap;
 // each block walks a contiguous range of tiles and adds its partial sums once.
@@ -281,6 +495,9 @@ __global__ void k_cnn_power(int H, int W, int ccols, const float2* __restrict__ 
 }
 
 // complex planes [drop][pair][word][ccols] / s -> bf16 NHWC [drop][word][column][32]
+// PLANAR: the tensor-core forward's layout [drop][4 chunks][word][column][8 channels];
+// else NHWC.
+template <bool PLANAR>
 __global__ void k_cnn_pack(int H, int W, int ccols, int B, const float2* __restrict__ csi, const float* __restrict__ pw,
                            float inv_count, __nv_bfloat16* __restrict__ out) {
   const int64_t total = (int64_t)B * H * W;
@@ -295,7 +512,14 @@ __global__ void k_cnn_pack(int H, int W, int ccols, int B, const float2* __restr
       const float2 z = csi[((b * NPAIR + p) * H + h) * ccols + w];
       v[p] = bf2_bits(z.x * is, z.y * is);
     }
-    store_px(out + q * CH, v);
+    if (PLANAR) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        *reinterpret_cast<uint4*>(out + (((b * 4 + j) * H + h) * W + w) * 8) =
+            make_uint4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+    } else {
+      store_px(out + q * CH, v);
+    }
   }
 }
 
@@ -367,6 +591,8 @@ struct hpx_cnn {
   float2* d_out = nullptr;        // [max_batch][16][H][W] training output
   float* d_pw = nullptr;          // [max_batch] per-drop LS power sums
   double* d_loss = nullptr;
+  int* d_fail = nullptr;          // set when a tensor-core wait of the forward pass timed out
+  int num_sms = 0;
 };
 
 namespace {
@@ -375,7 +601,8 @@ constexpr int NW = LAYERS * CH * KK, NB = LAYERS * CH, NPARAM = NW + NB;
 
 void cnn_release(hpx_cnn* c) {
   if (!c) return;
-  void* p[] = {c->d_param, c->d_m, c->d_v, c->d_grad, c->d_w, c->d_wd, c->d_act, c->d_g, c->d_out, c->d_pw, c->d_loss};
+  void* p[] = {c->d_param, c->d_m, c->d_v, c->d_grad, c->d_w,  c->d_wd,
+               c->d_act,   c->d_g, c->d_out, c->d_pw,  c->d_loss, c->d_fail};
   for (void* q : p)
     if (q) cudaFree(q);
   delete c;
@@ -403,17 +630,22 @@ hpx_status refresh_bf16(hpx_cnn* c) {
 int conv_tiles(int H, int W) { return ((H + TH - 1) / TH) * ((W + TW - 1) / TW); }
 
 // Power sums and the packed, scaled input of B drops of complex planes.
-hpx_status prepare(const hpx_cnn* c, int B, const float2* csi, int ccols, __nv_bfloat16* x0, cudaStream_t s) {
+hpx_status prepare(const hpx_cnn* c, int B, const float2* csi, int ccols, __nv_bfloat16* x0, bool planar,
+                   cudaStream_t s) {
   HPX_CUDA(cudaMemsetAsync(c->d_pw, 0, sizeof(float) * B, s));
   const float inv = 1.f / (float)(NPAIR * c->H * c->W);
   k_cnn_power<<<dim3(16, B), 256, 0, s>>>(c->H, c->W, ccols, csi, c->d_pw);
   HPX_LAUNCHED("cnn power");
   const int64_t px = (int64_t)B * c->H * c->W;
-  k_cnn_pack<<<(int)((px + 255) / 256), 256, 0, s>>>(c->H, c->W, ccols, B, csi, c->d_pw, inv, x0);
+  if (planar)
+    k_cnn_pack<true><<<(int)((px + 255) / 256), 256, 0, s>>>(c->H, c->W, ccols, B, csi, c->d_pw, inv, x0);
+  else
+    k_cnn_pack<false><<<(int)((px + 255) / 256), 256, 0, s>>>(c->H, c->W, ccols, B, csi, c->d_pw, inv, x0);
   HPX_LAUNCHED("cnn pack");
   return HPX_OK;
 }
 
+// Training forward (NHWC activations kept for the backward pass): mma.sync layers.
 hpx_status forward(const hpx_cnn* c, int B, const __nv_bfloat16* x0, __nv_bfloat16* const* act_out,
                    const float2* resid, float2* out_c, int ccols, cudaStream_t s) {
   const float inv = 1.f / (float)(NPAIR * c->H * c->W);
@@ -427,6 +659,36 @@ hpx_status forward(const hpx_cnn* c, int B, const __nv_bfloat16* x0, __nv_bfloat
   k_conv3x3<1><<<g, 128, 0, s>>>(c->H, c->W, in, c->d_w + (size_t)(LAYERS - 1) * CH * KK,
                                  c->d_param + NW + (LAYERS - 1) * CH, nullptr, nullptr, resid, out_c, ccols, c->d_pw,
                                  inv);
+  HPX_LAUNCHED("cnn forward");
+  return HPX_OK;
+}
+
+// Inference forward on the tensor cores (TMA + tcgen05), planar activations.
+hpx_status forward_tc(const hpx_cnn* c, int B, const __nv_bfloat16* x0, __nv_bfloat16* const* act_out,
+                      const float2* resid, float2* out_c, int ccols, cudaStream_t s) {
+  const float inv = 1.f / (float)(NPAIR * c->H * c->W);
+  const int64_t tiles = (int64_t)B * c->H * ((c->W + TCW - 1) / TCW);
+  const int grid = (int)std::min<int64_t>(tiles, (int64_t)c->num_sms * TC_CTAS_PER_SM);
+  static bool attr = false;
+  if (!attr) {
+    HPX_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    HPX_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    attr = true;
+  }
+  const __nv_bfloat16* in = x0;
+  CUtensorMap map;
+  for (int l = 0; l < LAYERS - 1; ++l) {
+    HPX_TRY(activation_map(in, B, c->H, c->W, &map));
+    k_conv3x3_tc<0><<<grid, 128, TC_SMEM, s>>>(map, B, c->H, c->W, c->d_w + (size_t)l * CH * KK,
+                                               c->d_param + NW + l * CH, act_out[l], nullptr, nullptr, 0, nullptr,
+                                               0.f, c->d_fail);
+    HPX_LAUNCHED("cnn forward");
+    in = act_out[l];
+  }
+  HPX_TRY(activation_map(in, B, c->H, c->W, &map));
+  k_conv3x3_tc<1><<<grid, 128, TC_SMEM, s>>>(map, B, c->H, c->W, c->d_w + (size_t)(LAYERS - 1) * CH * KK,
+                                             c->d_param + NW + (LAYERS - 1) * CH, nullptr, resid, out_c, ccols,
+                                             c->d_pw, inv, c->d_fail);
   HPX_LAUNCHED("cnn forward");
   return HPX_OK;
 }
@@ -470,11 +732,19 @@ hpx_status hpx_cnn_create(int32_t num_words, int32_t num_columns, int32_t max_ba
           cudaSuccess ||
       (e = cudaMalloc(&c->d_loss, sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&c->d_pw, sizeof(float) * max_batch)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_fail, sizeof(int))) != cudaSuccess ||
+      (e = cudaMemset(c->d_fail, 0, sizeof(int))) != cudaSuccess ||
       (e = cudaMemcpy(c->d_param, host.data(), sizeof(float) * NPARAM, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemset(c->d_m, 0, sizeof(float) * NPARAM)) != cudaSuccess ||
       (e = cudaMemset(c->d_v, 0, sizeof(float) * NPARAM)) != cudaSuccess) {
     cnn_release(c);
     return hpx_cuda_status(e, "cnn buffers");
+  }
+  int dev = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) {
+    cnn_release(c);
+    return hpx_cuda_status(e, "cnn device");
   }
   const hpx_status st = refresh_bf16(c);
   if (st != HPX_OK) {
@@ -516,8 +786,8 @@ hpx_status hpx_cnn_refine(const hpx_cnn* c, hpx_cf32* csi, int32_t ccols, int32_
     __nv_bfloat16* x0 = c->d_act;
     __nv_bfloat16* pp[2] = {c->d_g, c->d_g + act};
     __nv_bfloat16* outs[LAYERS - 1] = {pp[0], pp[1], pp[0], pp[1], pp[0]};
-    HPX_TRY(prepare(c, n, cs, ccols, x0, s));
-    HPX_TRY(forward(c, n, x0, outs, cs, cs, ccols, s));
+    HPX_TRY(prepare(c, n, cs, ccols, x0, true, s));
+    HPX_TRY(forward_tc(c, n, x0, outs, cs, cs, ccols, s));
   }
   return HPX_OK;
 }
@@ -534,7 +804,7 @@ hpx_status hpx_cnn_train_step(hpx_cnn* c, const hpx_cf32* ls, const hpx_cf32* tr
   const int64_t px = (int64_t)B * c->H * c->W;
   const int blocks = (int)((px + 255) / 256);
   const float inv = 1.f / (float)(NPAIR * c->H * c->W);
-  HPX_TRY(prepare(c, B, reinterpret_cast<const float2*>(ls), ccols, a[0], s));
+  HPX_TRY(prepare(c, B, reinterpret_cast<const float2*>(ls), ccols, a[0], false, s));
   HPX_TRY(forward(c, B, a[0], a + 1, reinterpret_cast<const float2*>(ls), c->d_out, ccols, s));
   HPX_CUDA(cudaMemsetAsync(c->d_loss, 0, sizeof(double), s));
   __nv_bfloat16* g[2] = {c->d_g, c->d_g + act};
