@@ -198,11 +198,12 @@ __global__ void __launch_bounds__(128) k_conv3x3(int H, int W, const __nv_bfloat
 // bytes apart (core matrices 128 bytes apart along M), the two 8-channel halves a
 // plane apart along K. The weights of tap t and channel half kc form a 32 x 16
 // K-major block. Eighteen MMAs (M = 128, N = 32, K = 16, BF16 in, FP32 out) give
-// the tile. The CTA walks tiles persistently as a pipeline: two input stages
-// (the TMA of tile k + 2 starts as soon as the MMAs of tile k have read their
-// stage) and two accumulator slots in tensor memory (the MMAs of tile k run while
-// the epilogue of tile k - 1 reads the other slot). A tensor-core or TMA wait that
-// times out writes NaN outputs and sets *fail.
+// the tile. The CTA walks tiles persistently as a warp-specialized pipeline: warp 0
+// (one thread) issues the TMA copies into two input stages and the MMAs into two
+// accumulator slots in tensor memory; warps 1-4 each read a quarter of a slot's
+// lanes, release the slot through an mbarrier and run the epilogue, so the MMAs of
+// tile k + 1 queue while tile k is stored. No CTA-wide barrier inside the loop. A
+// tensor-core or TMA wait that times out writes NaN outputs and sets *fail.
 constexpr int TCW = 128;                           // output columns per tile
 constexpr int TC_INW = TCW + 2;                    // input columns with halo
 constexpr int TC_BOX = 3 * TC_INW * 16;            // bytes of one TMA box (one plane)
@@ -214,6 +215,7 @@ constexpr int TC_SMEM = TC_STAGES * TC_BUF + 18 * TC_WBLK + 128;  // + alignment
 constexpr uint32_t TC_IDESC = tc::idesc_f16_f32(128, CH) | (1u << 7) | (1u << 10);  // A, B: BF16
 constexpr long long TC_CONV_WAIT = 40ll * 1000 * 1000;  // cycles (~20 ms)
 constexpr int TC_CTAS_PER_SM = 3;                  // shared memory: 3 x 67 KB
+constexpr int TC_THREADS = 160;                    // warp 0: TMA + MMA issue; warps 1-4: epilogue
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)), "r"(bytes)
@@ -230,24 +232,21 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
 }
 
 template <int EPI>
-__global__ void __launch_bounds__(128, TC_CTAS_PER_SM) k_conv3x3_tc(const __grid_constant__ CUtensorMap tmap, int B,
-                                                                    int H, int W, const __nv_bfloat16* __restrict__ wt,
-                                                                    const float* __restrict__ bias,
-                                                                    __nv_bfloat16* __restrict__ out,
-                                                                    const float2* resid, float2* out_c, int ccols,
-                                                                    const float* __restrict__ pw, float inv_count,
-                                                                    int* fail) {
+__global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) k_conv3x3_tc(
+    const __grid_constant__ CUtensorMap tmap, int B, int H, int W, const __nv_bfloat16* __restrict__ wt,
+    const float* __restrict__ bias, __nv_bfloat16* __restrict__ out, const float2* resid, float2* out_c, int ccols,
+    const float* __restrict__ pw, float inv_count, int* fail) {
   extern __shared__ unsigned char sm_raw[];
   unsigned char* sm = sm_raw + ((128u - (tc::smem_u32(sm_raw) & 127u)) & 127u);
-  unsigned char* s_in = sm;                    // [TC_STAGES][4 planes]
+  unsigned char* s_in = sm;                      // [TC_STAGES][4 planes]
   unsigned char* s_w = sm + TC_STAGES * TC_BUF;  // [9 taps x 2 halves] weight blocks
-  __shared__ uint64_t bar_in[TC_STAGES], bar_mma[2];
+  __shared__ uint64_t bar_in[TC_STAGES], bar_mma[2], bar_free[2];
   __shared__ uint32_t tmem_slot;
   __shared__ float s_bias[CH];
   __shared__ int skip;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // weights: element (n, tap 32 + c) -> block (tap, c / 16), K-major inside
-  for (int q = tid; q < CH * 36; q += 128) {
+  for (int q = tid; q < CH * 36; q += TC_THREADS) {
     const int n = q / 36, r = q - n * 36, tap = r >> 2, c8 = r & 3;
     const uint4 v = __ldg(reinterpret_cast<const uint4*>(wt + n * KK + tap * CH + c8 * 8));
     *reinterpret_cast<uint4*>(s_w + (tap * 2 + (c8 >> 1)) * TC_WBLK + tc::kmajor_offset(n, (c8 & 1) * 8, 16)) = v;
@@ -256,8 +255,10 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) k_conv3x3_tc(const __grid
   if (tid == 0) {
     skip = *(volatile int*)fail;
     for (int i = 0; i < TC_STAGES; ++i) tc::mbar_init(&bar_in[i], 1);
-    tc::mbar_init(&bar_mma[0], 1);
-    tc::mbar_init(&bar_mma[1], 1);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&bar_mma[i], 1);
+      tc::mbar_init(&bar_free[i], 128);  // every epilogue thread releases the slot
+    }
   }
   if (warp == 0) {
     tc::tmem_alloc(&tmem_slot, 64);  // two accumulator slots of 32 columns
@@ -269,7 +270,6 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) k_conv3x3_tc(const __grid
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
   bool ok = skip == 0;
-  const uint64_t b_desc = tc::smem_desc(s_w, 128, 256);
   const int tiles_w = (W + TCW - 1) / TCW;
   const int64_t ntiles = (int64_t)B * H * tiles_w;
   // tiles of this CTA: blockIdx.x + k gridDim.x, k < K
@@ -281,91 +281,113 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) k_conv3x3_tc(const __grid
     b = (int)(bh / H);
     h = (int)(bh - (int64_t)b * H);
   };
-  int issued[TC_STAGES] = {}, landed[TC_STAGES] = {};  // thread 0: TMA phases per stage
-  auto issue = [&](int k) {  // thread 0: the four planes of tile k into stage k % TC_STAGES
-    const int st = k % TC_STAGES;
-    int b, h, w0;
-    decode(k, b, h, w0);
-    ++issued[st];
-    mbar_expect_tx(&bar_in[st], 4 * TC_BOX);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) tma_load_4d(s_in + st * TC_BUF + j * TC_PLANE, &tmap, 0, w0 - 1, h - 1, 4 * b + j, &bar_in[st]);
-  };
-  if (tid == 0 && ok)
-    for (int k = 0; k < TC_STAGES && k < K; ++k) issue(k);
-  // Iteration k issues the MMAs of tile k (accumulator slot k & 1) and then finishes
-  // tile k - 1: its MMAs done, its stage refilled with tile k + 2, its epilogue.
-  for (int k = 0; k <= K; ++k) {
-    if (k < K) {
+  if (warp == 0) {
+    // ---- producer: lane 0 issues the TMA into the stages and the MMAs into the two
+    // slots; the warp walks the loop together (status broadcast from lane 0)
+    int issued[TC_STAGES] = {}, landed[TC_STAGES] = {};
+    auto issue = [&](int k) {  // the four planes of tile k into stage k % TC_STAGES
       const int st = k % TC_STAGES;
-      if (ok) ok = tc::mbar_wait(&bar_in[st], (uint32_t)((k / TC_STAGES) & 1), TC_CONV_WAIT);
-      if (tid == 0 && ok) {
-        ++landed[st];
-        // every operand is a fixed offset from the two buffers: the descriptors differ
-        // from the buffers' only in the start-address field (address / 16)
-        const uint64_t a_desc = tc::smem_desc(s_in + st * TC_BUF, TC_PLANE, 128);
-        const uint32_t d = tmem + (uint32_t)((k & 1) * 32);
+      int b, h, w0;
+      decode(k, b, h, w0);
+      ++issued[st];
+      mbar_expect_tx(&bar_in[st], 4 * TC_BOX);
 #pragma unroll
-        for (int tap = 0; tap < 9; ++tap) {
-          const int dy = tap / 3, dx = tap - dy * 3;
+      for (int j = 0; j < 4; ++j)
+        tma_load_4d(s_in + st * TC_BUF + j * TC_PLANE, &tmap, 0, w0 - 1, h - 1, 4 * b + j, &bar_in[st]);
+    };
+    const uint64_t b_desc = tc::smem_desc(s_w, 128, 256);
+    if (lane == 0 && ok)
+      for (int k = 0; k < TC_STAGES && k < K; ++k) issue(k);
+    for (int k = 0; k < K && ok; ++k) {
+      bool go = true;
+      if (lane == 0) {
+        const int st = k % TC_STAGES, slot = k & 1;
+        go = tc::mbar_wait(&bar_in[st], (uint32_t)((k / TC_STAGES) & 1), TC_CONV_WAIT);
+        if (go) ++landed[st];
+        // the epilogue of tile k - 2 has read this slot
+        if (go && k >= 2) go = tc::mbar_wait(&bar_free[slot], (uint32_t)(((k - 2) >> 1) & 1), TC_CONV_WAIT);
+        tc::fence_after_sync();
+        if (go) {
+          // every operand is a fixed offset from the two buffers: the descriptors
+          // differ from the buffers' only in the start-address field (address / 16)
+          const uint64_t a_desc = tc::smem_desc(s_in + st * TC_BUF, TC_PLANE, 128);
+          const uint32_t d = tmem + (uint32_t)(slot * 32);
 #pragma unroll
-          for (int kc = 0; kc < 2; ++kc) {
-            const uint64_t ad = a_desc + (uint64_t)((2 * kc * TC_PLANE + (dy * TC_INW + dx) * 16) >> 4);
-            const uint64_t bd = b_desc + (uint64_t)(((tap * 2 + kc) * TC_WBLK) >> 4);
-            tc::mma_f16(d, ad, bd, TC_IDESC, (tap | kc) != 0);
+          for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap - dy * 3;
+#pragma unroll
+            for (int kc = 0; kc < 2; ++kc) {
+              const uint64_t ad = a_desc + (uint64_t)((2 * kc * TC_PLANE + (dy * TC_INW + dx) * 16) >> 4);
+              const uint64_t bd = b_desc + (uint64_t)(((tap * 2 + kc) * TC_WBLK) >> 4);
+              tc::mma_f16(d, ad, bd, TC_IDESC, (tap | kc) != 0);
+            }
+          }
+          tc::mma_commit(&bar_mma[slot]);
+          // tile k - 1's MMAs (queued ahead of these) have read their stage: refill it
+          if (k >= 1 && k - 1 + TC_STAGES < K) {
+            go = tc::mbar_wait(&bar_mma[(k - 1) & 1], (uint32_t)(((k - 1) >> 1) & 1), TC_CONV_WAIT);
+            if (go) issue(k - 1 + TC_STAGES);
           }
         }
-        tc::mma_commit(&bar_mma[k & 1]);
+      }
+      ok = __shfl_sync(0xffffffffu, go ? 1 : 0, 0) != 0;
+    }
+    if (lane == 0) {
+      // after a timeout: let copies still in flight land (bounded) before leaving
+      for (int st = 0; st < TC_STAGES; ++st)
+        for (; landed[st] < issued[st]; ++landed[st])
+          tc::mbar_wait(&bar_in[st], (uint32_t)(landed[st] & 1), TC_CONV_WAIT);
+      if (!ok && skip == 0) atomicExch(fail, 1);
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue warps: warp w reads TMEM lanes 32 (w % 4) .. + 31
+    const int qtr = warp & 3;
+    for (int k = 0; k < K; ++k) {
+      const int slot = k & 1;
+      if (ok) ok = tc::mbar_wait(&bar_mma[slot], (uint32_t)((k >> 1) & 1), TC_CONV_WAIT);
+      tc::fence_after_sync();
+      float acc[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(qtr * 32) << 16) + (uint32_t)(slot * 32), acc);
+      tc::fence_before_sync();
+      tc::mbar_arrive(&bar_free[slot]);  // the slot may take tile k + 2
+      int b, h, w0;
+      decode(k, b, h, w0);
+      const int w = w0 + qtr * 32 + lane;
+      if (w < W) {
+        const float nan = __int_as_float(0x7fc00000);
+        if (EPI == 0) {
+          uint32_t u[NPAIR];
+#pragma unroll
+          for (int i = 0; i < NPAIR; ++i)
+            u[i] = ok ? bf2_bits(fmaxf(acc[2 * i] + s_bias[2 * i], 0.f), fmaxf(acc[2 * i + 1] + s_bias[2 * i + 1], 0.f))
+                      : bf2_bits(nan, nan);
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            *reinterpret_cast<uint4*>(out + ((((int64_t)b * 4 + j) * H + h) * W + w) * 8) =
+                make_uint4(u[4 * j], u[4 * j + 1], u[4 * j + 2], u[4 * j + 3]);
+        } else {
+          // resid may be out_c itself: every residual of this element is read before
+          // the first store, so the 16 loads are in flight together
+          const float scale = sqrtf(pw[b] * inv_count);
+          const int64_t e0 = ((int64_t)b * NPAIR * H + h) * ccols + w, es = (int64_t)H * ccols;
+          float2 x[NPAIR];
+#pragma unroll
+          for (int i = 0; i < NPAIR; ++i) x[i] = resid[e0 + i * es];
+#pragma unroll
+          for (int i = 0; i < NPAIR; ++i)
+            out_c[e0 + i * es] = ok ? make_float2(fmaf(scale, acc[2 * i] + s_bias[2 * i], x[i].x),
+                                                  fmaf(scale, acc[2 * i + 1] + s_bias[2 * i + 1], x[i].y))
+                                    : make_float2(nan, nan);
+        }
       }
     }
-    if (k == 0) continue;
-    const int j = k - 1;
-    if (ok) ok = tc::mbar_wait(&bar_mma[j & 1], (uint32_t)((j >> 1) & 1), TC_CONV_WAIT);
-    tc::fence_after_sync();
-    // the MMAs of tile j have read their stage: refill it
-    if (tid == 0 && ok && j + TC_STAGES < K) issue(j + TC_STAGES);
-    int b, h, w0;
-    decode(j, b, h, w0);
-    float acc[32];
-    tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((j & 1) * 32), acc);
-    const int w = w0 + tid;
-    if (w < W) {
-      const float nan = __int_as_float(0x7fc00000);
-      if (EPI == 0) {
-        uint32_t u[NPAIR];
-#pragma unroll
-        for (int i = 0; i < NPAIR; ++i)
-          u[i] = ok ? bf2_bits(fmaxf(acc[2 * i] + s_bias[2 * i], 0.f), fmaxf(acc[2 * i + 1] + s_bias[2 * i + 1], 0.f))
-                    : bf2_bits(nan, nan);
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-          *reinterpret_cast<uint4*>(out + ((((int64_t)b * 4 + j) * H + h) * W + w) * 8) =
-              make_uint4(u[4 * j], u[4 * j + 1], u[4 * j + 2], u[4 * j + 3]);
-      } else {
-        // resid may be out_c itself: every residual of this element is read before the
-        // first store, so the 16 loads are in flight together
-        const float scale = sqrtf(pw[b] * inv_count);
-        const int64_t e0 = ((int64_t)b * NPAIR * H + h) * ccols + w, es = (int64_t)H * ccols;
-        float2 x[NPAIR];
-#pragma unroll
-        for (int i = 0; i < NPAIR; ++i) x[i] = resid[e0 + i * es];
-#pragma unroll
-        for (int i = 0; i < NPAIR; ++i)
-          out_c[e0 + i * es] = ok ? make_float2(fmaf(scale, acc[2 * i] + s_bias[2 * i], x[i].x),
-                                                fmaf(scale, acc[2 * i + 1] + s_bias[2 * i + 1], x[i].y))
-                                  : make_float2(nan, nan);
-      }
-    }
-    tc::fence_before_sync();
-    __syncthreads();  // slot j & 1 read by every warp before the MMAs of tile j + 2
-    tc::fence_after_sync();
+    if (!ok && skip == 0) atomicExch(fail, 1);
   }
-  if (tid == 0)  // after a timeout: let copies still in flight land (bounded) before leaving
-    for (int st = 0; st < TC_STAGES; ++st)
-      for (; landed[st] < issued[st]; ++landed[st])
-        tc::mbar_wait(&bar_in[st], (uint32_t)(landed[st] & 1), TC_CONV_WAIT);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
   if (warp == 0) tc::tmem_dealloc(tmem, 64);
-  if (!ok && skip == 0) atomicExch(fail, 1);
 }
 
 // Tensor map of a planar BF16 activation [B][4 chunks][H][W][8] with the conv tile's box:
@@ -679,14 +701,14 @@ hpx_status forward_tc(const hpx_cnn* c, int B, const __nv_bfloat16* x0, __nv_bfl
   CUtensorMap map;
   for (int l = 0; l < LAYERS - 1; ++l) {
     HPX_TRY(activation_map(in, B, c->H, c->W, &map));
-    k_conv3x3_tc<0><<<grid, 128, TC_SMEM, s>>>(map, B, c->H, c->W, c->d_w + (size_t)l * CH * KK,
+    k_conv3x3_tc<0><<<grid, TC_THREADS, TC_SMEM, s>>>(map, B, c->H, c->W, c->d_w + (size_t)l * CH * KK,
                                                c->d_param + NW + l * CH, act_out[l], nullptr, nullptr, 0, nullptr,
                                                0.f, c->d_fail);
     HPX_LAUNCHED("cnn forward");
     in = act_out[l];
   }
   HPX_TRY(activation_map(in, B, c->H, c->W, &map));
-  k_conv3x3_tc<1><<<grid, 128, TC_SMEM, s>>>(map, B, c->H, c->W, c->d_w + (size_t)(LAYERS - 1) * CH * KK,
+  k_conv3x3_tc<1><<<grid, TC_THREADS, TC_SMEM, s>>>(map, B, c->H, c->W, c->d_w + (size_t)(LAYERS - 1) * CH * KK,
                                              c->d_param + NW + (LAYERS - 1) * CH, nullptr, resid, out_c, ccols,
                                              c->d_pw, inv, c->d_fail);
   HPX_LAUNCHED("cnn forward");
