@@ -209,12 +209,12 @@ constexpr int TC_INW = TCW + 2;                    // input columns with halo
 constexpr int TC_BOX = 3 * TC_INW * 16;            // bytes of one TMA box (one plane)
 constexpr int TC_PLANE = (TC_BOX + 127) / 128 * 128;  // plane stride (TMA destinations 128-byte aligned)
 constexpr int TC_BUF = 4 * TC_PLANE;               // one input stage
-constexpr int TC_STAGES = 2;                       // input stages in flight per CTA
+constexpr int TC_STAGES = 3;                       // input stages in flight per CTA
 constexpr int TC_WBLK = CH * 16 * 2;               // one 32 x 16 bf16 weight block
 constexpr int TC_SMEM = TC_STAGES * TC_BUF + 18 * TC_WBLK + 128;  // + alignment slack
 constexpr uint32_t TC_IDESC = tc::idesc_f16_f32(128, CH) | (1u << 7) | (1u << 10);  // A, B: BF16
 constexpr long long TC_CONV_WAIT = 40ll * 1000 * 1000;  // cycles (~20 ms)
-constexpr int TC_CTAS_PER_SM = 3;                  // shared memory: 3 x 67 KB
+constexpr int TC_CTAS_PER_SM = 2;                  // shared memory: 2 x 92 KB
 constexpr int TC_THREADS = 160;                    // warp 0: TMA + MMA issue; warps 1-4: epilogue
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
