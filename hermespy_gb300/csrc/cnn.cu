@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(128) k_conv3x3(int H, int W, const __nv_bfloat
 // plane apart along K. The weights of tap t and channel half kc form a 32 x 16
 // K-major block. Eighteen MMAs (M = 128, N = 32, K = 16, BF16 in, FP32 out) give
 // the tile. The CTA walks tiles persistently as a warp-specialized pipeline: warp 0
-// (one thread) issues the TMA copies into two input stages and the MMAs into two
+// (one thread) issues the TMA copies into three input stages and the MMAs into two
 // accumulator slots in tensor memory; warps 1-4 each read a quarter of a slot's
 // lanes, release the slot through an mbarrier and run the epilogue, so the MMAs of
 // tile k + 1 queue while tile k is stored. No CTA-wide barrier inside the loop. A
