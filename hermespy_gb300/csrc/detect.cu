@@ -139,9 +139,18 @@ __global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_ideal
 }
 
 // Fused receiver for a given CSI grid (any estimator), one block per (word, drop):
-// H from csi[B][NRX][NTX][W][ccols], y from grid[B][NRX][W][gcols].
+// H from csi[B][NRX][NTX][W][ccols], y from grid[B][NRX][W][gcols]. Streaming the
+// channel from HBM is latency bound, so blocks stay small (at most 192 threads, each
+// thread several elements) and several share an SM: the 4 x 4 kernel holds 96
+// registers at 3-4 blocks per SM instead of 114 at one block of 320 threads (up to 4
+// transmit streams and 16 antenna pairs; larger systems keep the wide blocks).
 template <int NRX, int NTX>
-__global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_csi(
+constexpr bool csi_small() { return NTX <= 4 && NRX * NTX <= 16; }
+template <int NRX, int NTX>
+constexpr int csi_max_threads() { return csi_small<NRX, NTX>() ? 192 : detect_max_threads<NRX, NTX>(); }
+
+template <int NRX, int NTX>
+__global__ void __launch_bounds__(csi_max_threads<NRX, NTX>(), csi_small<NRX, NTX>() ? 3 : 1) k_detect_csi(
     int W, int C, int m, const int32_t* __restrict__ data_offset, const int32_t* __restrict__ num_data_word,
     const int32_t* __restrict__ data_column, const __grid_constant__ QamDemapTable qt, int mode,
     const float2* __restrict__ grid, int gcols, const float2* __restrict__ csi, int ccols,
@@ -369,7 +378,7 @@ hpx_status launch_detect_csi(const hpx_frame* fr, int mode, const hpx_cf32* grid
   auto kern = k_detect_csi<NRX, NTX>;
   if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid_dim(fr->info.num_words, B);
-  const int threads = detect_threads(fr->max_data_word, detect_max_threads<NRX, NTX>());
+  const int threads = detect_threads(fr->max_data_word, csi_max_threads<NRX, NTX>());
   kern<<<grid_dim, threads, smem, s>>>(fr->info.num_words, C, m, fr->d_data_offset, fr->d_num_data_word,
                                        fr->d_data_column, qt, mode, reinterpret_cast<const float2*>(grid), gcols,
                                        reinterpret_cast<const float2*>(csi), ccols, nv, seed, drop0, errors);
