@@ -14,6 +14,8 @@ struct hpx_ls {
   float* d_weights = nullptr;    // [nnz]
   int32_t* d_ref_word = nullptr;    // [num_refs]
   int32_t* d_ref_column = nullptr;  // [num_refs]
+  int32_t* d_pos = nullptr;         // [nnz] word << 16 | column of the entry's reference element
+  float2* d_coef = nullptr;         // [nnz] weight * conj(x_ref) / |x_ref|^2 (the LS division folded in)
 };
 
 namespace {
@@ -291,13 +293,14 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
 }
 
 // rows = streams * W * C (the stacked tables); blockIdx.y covers LS_ITEMS received
-// grids (drop, rx), which share every table row a thread loads.
-constexpr int LS_ITEMS = 8;
-__global__ void k_ls_estimate(int W, int rows, int items, const int32_t* __restrict__ indptr,
-                              const int32_t* __restrict__ indices, const float* __restrict__ weights,
-                              const int32_t* __restrict__ ref_word, const int32_t* __restrict__ ref_column,
-                              const float2* __restrict__ pilots, const float2* __restrict__ grid, int gcols,
-                              float2* __restrict__ est) {
+// grids (drop, rx), which share every table row a thread loads. Each table entry is
+// (position, weight conj(x) / |x|^2): the LS value y / x of a reference element and
+// its interpolation weight in one complex multiply-add.
+constexpr int LS_ITEMS = 16;
+__global__ void __launch_bounds__(256) k_ls_estimate(int W, int rows, int items, const int32_t* __restrict__ indptr,
+                                                     const int32_t* __restrict__ pos, const float2* __restrict__ coef,
+                                                     const float2* __restrict__ grid, int gcols,
+                                                     float2* __restrict__ est) {
   const int i0 = blockIdx.y * LS_ITEMS;
   const int n = min(LS_ITEMS, items - i0);
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < rows; row += gridDim.x * blockDim.x) {
@@ -305,17 +308,13 @@ __global__ void k_ls_estimate(int W, int rows, int items, const int32_t* __restr
 #pragma unroll
     for (int i = 0; i < LS_ITEMS; ++i) h[i] = make_float2(0.f, 0.f);
     for (int e = indptr[row]; e < indptr[row + 1]; ++e) {
-      const int p = indices[e];
-      const float wgt = weights[e];
-      const float2 xp = pilots[p];
-      const float den = xp.x * xp.x + xp.y * xp.y;
-      const int64_t at = (int64_t)ref_word[p] * gcols + ref_column[p];
+      const int ps = pos[e];
+      const float2 cf = coef[e];
+      const int64_t at = (int64_t)(ps >> 16) * gcols + (ps & 0xFFFF);
 #pragma unroll
       for (int i = 0; i < LS_ITEMS; ++i) {
         if (i >= n) break;
-        const float2 yp = grid[(int64_t)(i0 + i) * W * gcols + at];
-        const float2 ls = make_float2((yp.x * xp.x + yp.y * xp.y) / den, (yp.y * xp.x - yp.x * xp.y) / den);
-        h[i] = cadd(h[i], cscale(ls, wgt));
+        cfma(h[i], cf, grid[(int64_t)(i0 + i) * W * gcols + at]);
       }
     }
 #pragma unroll
@@ -458,11 +457,28 @@ hpx_status hpx_ls_create_streams(const hpx_frame* frame, int32_t C, int32_t num_
     return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
   };
   cudaError_t e;
+  std::vector<float2> pilots(frame->info.num_refs);
+  if ((e = cudaMemcpy(pilots.data(), frame->d_pilots, pilots.size() * sizeof(float2), cudaMemcpyDeviceToHost)) !=
+      cudaSuccess) {
+    hpx_ls_destroy(ls);
+    return hpx_cuda_status(e, "ls pilots");
+  }
+  std::vector<int32_t> pos(nnz);
+  std::vector<float2> coef(nnz);
+  for (int q = 0; q < nnz; ++q) {
+    const int p = indices[q];
+    const double xr = pilots[p].x, xi = pilots[p].y, den = xr * xr + xi * xi;
+    pos[q] = (rw[p] << 16) | rc[p];
+    coef[q] = den > 0 ? make_float2((float)(weights[q] * xr / den), (float)(-weights[q] * xi / den))
+                      : make_float2(NAN, NAN);  // y / 0, as the division it replaces
+  }
   if ((e = up((void**)&ls->d_indptr, indptr, (rows + 1) * sizeof(int32_t))) != cudaSuccess ||
       (e = up((void**)&ls->d_indices, indices, nnz * sizeof(int32_t))) != cudaSuccess ||
       (e = up((void**)&ls->d_weights, weights, nnz * sizeof(float))) != cudaSuccess ||
       (e = up((void**)&ls->d_ref_word, rw.data(), rw.size() * sizeof(int32_t))) != cudaSuccess ||
-      (e = up((void**)&ls->d_ref_column, rc.data(), rc.size() * sizeof(int32_t))) != cudaSuccess) {
+      (e = up((void**)&ls->d_ref_column, rc.data(), rc.size() * sizeof(int32_t))) != cudaSuccess ||
+      (e = up((void**)&ls->d_pos, pos.data(), nnz * sizeof(int32_t))) != cudaSuccess ||
+      (e = up((void**)&ls->d_coef, coef.data(), nnz * sizeof(float2))) != cudaSuccess) {
     hpx_ls_destroy(ls);
     return hpx_cuda_status(e, "ls tables");
   }
@@ -477,7 +493,7 @@ hpx_status hpx_ls_create(const hpx_frame* frame, int32_t C, const int32_t* indpt
 
 hpx_status hpx_ls_destroy(hpx_ls* ls) {
   if (!ls) return HPX_OK;
-  void* p[] = {ls->d_indptr, ls->d_indices, ls->d_weights, ls->d_ref_word, ls->d_ref_column};
+  void* p[] = {ls->d_indptr, ls->d_indices, ls->d_weights, ls->d_ref_word, ls->d_ref_column, ls->d_pos, ls->d_coef};
   for (void* q : p)
     if (q) cudaFree(q);
   delete ls;
@@ -494,8 +510,7 @@ hpx_status hpx_ls_estimate(const hpx_ls* ls, const hpx_cf32* grid, int32_t gcols
   if (ls->ntx != 1) return hpx_fail(HPX_ERR_ARG, "ls_estimate: table of %d streams (use hpx_ls_estimate_streams)", ls->ntx);
   const int W = ls->frame->info.num_words;
   dim3 grid_dim((W * ls->C + 255) / 256, (B + LS_ITEMS - 1) / LS_ITEMS);
-  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, W * ls->C, B, ls->d_indptr, ls->d_indices, ls->d_weights,
-                                                         ls->d_ref_word, ls->d_ref_column, ls->frame->d_pilots,
+  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, W * ls->C, B, ls->d_indptr, ls->d_pos, ls->d_coef,
                                                          reinterpret_cast<const float2*>(grid), gcols,
                                                          reinterpret_cast<float2*>(est));
   HPX_LAUNCHED("ls_estimate");
@@ -512,8 +527,7 @@ hpx_status hpx_ls_estimate_streams(const hpx_ls* ls, const hpx_cf32* grid, int32
   const int W = ls->frame->info.num_words;
   const int rows = ls->ntx * W * ls->C;
   dim3 grid_dim((rows + 255) / 256, (B * nrx + LS_ITEMS - 1) / LS_ITEMS);
-  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, rows, B * nrx, ls->d_indptr, ls->d_indices, ls->d_weights,
-                                                         ls->d_ref_word, ls->d_ref_column, ls->frame->d_pilots,
+  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, rows, B * nrx, ls->d_indptr, ls->d_pos, ls->d_coef,
                                                          reinterpret_cast<const float2*>(grid), gcols,
                                                          reinterpret_cast<float2*>(est));
   HPX_LAUNCHED("ls_estimate");
