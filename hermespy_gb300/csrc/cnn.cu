@@ -503,14 +503,17 @@ __global__ void __launch_bounds__(288) k_conv3x3_wgrad(int H, int W, int B, cons
 }
 
 // Per drop: pw[b] = sum of |LS|^2 over pairs, words and columns (blockIdx.y = drop).
+// One warp per (pair, word) row of a drop at a time, lanes along the columns.
 __global__ void k_cnn_power(int H, int W, int ccols, const float2* __restrict__ csi, float* __restrict__ pw) {
   const int b = blockIdx.y;
-  const int total = NPAIR * H * W;
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   float e = 0.f;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
-    const int p = q / (H * W), rem = q - p * H * W, h = rem / W, w = rem - h * W;
-    const float2 z = csi[(((int64_t)b * NPAIR + p) * H + h) * ccols + w];
-    e = fmaf(z.x, z.x, fmaf(z.y, z.y, e));
+  for (int row = blockIdx.x * wpb + (threadIdx.x >> 5); row < NPAIR * H; row += gridDim.x * wpb) {
+    const float2* r = csi + ((int64_t)b * NPAIR * H + row) * ccols;
+    for (int w = lane; w < W; w += 32) {
+      const float2 z = r[w];
+      e = fmaf(z.x, z.x, fmaf(z.y, z.y, e));
+    }
   }
   for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(pw + b, e);
