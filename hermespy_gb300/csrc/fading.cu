@@ -13,14 +13,16 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 // ---------------------------------------------------------------- parameters
 // One block per drop. MODE 0: draws from the Philox stream (domain 2);
 // MODE 1: explicit angles / phases / spatial response from device arrays.
+// MODE 0 with `staged`: the drop's uniforms (nrx ntx + 2 L + 2 L S of them) are drawn
+// once into shared memory, one Philox block per four, instead of one block per draw.
 template <int MODE>
 __global__ void k_fading_params(FadingConst fc, double nlos_rate, double los_rate, uint64_t seed, int64_t drop0,
                                 const double* __restrict__ la, const double* __restrict__ na,
                                 const double* __restrict__ lp, const double* __restrict__ np_,
                                 const double* __restrict__ sp_in, const double* __restrict__ rxc,
                                 const double* __restrict__ txc, unsigned char* state, size_t stride, size_t off_w,
-                                size_t off_p0, size_t off_sp) {
-  extern __shared__ double2 sps[];  // [nrx*ntx] spatial, then [nrx*ntx] temp
+                                size_t off_p0, size_t off_sp, int staged) {
+  extern __shared__ double2 sps[];  // [nrx*ntx] spatial, then [nrx*ntx] temp, then the staged uniforms
   const int b = blockIdx.x;
   const int64_t drop = drop0 + b;
   const int L = fc.L, S = fc.S, S1 = fc.S1, nrx = fc.nrx, ntx = fc.ntx;
@@ -29,8 +31,21 @@ __global__ void k_fading_params(FadingConst fc, double nlos_rate, double los_rat
   int64_t* Wout = reinterpret_cast<int64_t*>(base + off_w);
   int64_t* Pout = reinterpret_cast<int64_t*>(base + off_p0);
   float2* Sout = reinterpret_cast<float2*>(base + off_sp);
+  double* ud = reinterpret_cast<double*>(sps + 2 * nsp);
+  if (MODE == 0 && staged) {
+    const int num = nsp + 2 * L + 2 * L * S;
+    for (int blk = threadIdx.x; blk < (num + 3) >> 2; blk += blockDim.x) {
+      const uint4 r = hpx_random_block(seed, drop, 0u, HPX_DOMAIN_FADING, (uint32_t)blk);
+      const uint32_t wv[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (4 * blk + i < num) ud[4 * blk + i] = u01_f64(wv[i]);
+    }
+    __syncthreads();
+  }
 
   auto uniform = [&](int idx) -> double {
+    if (staged) return ud[idx];
     const uint4 r = hpx_random_block(seed, drop, 0u, HPX_DOMAIN_FADING, (uint32_t)(idx >> 2));
     return u01_f64(uint4_get(r, idx & 3));
   };
@@ -647,23 +662,27 @@ static hpx_status launch_params(const hpx_fading* f, int mode, uint64_t seed, in
   if (B == 0) return HPX_OK;
   if (B > 2147483647) return hpx_fail(HPX_ERR_ARG, "fading: too many drops");
   const FadingConst fc = fading_const(f);
-  const size_t smem = (size_t)2 * f->nrx * f->ntx * sizeof(double2);
+  const size_t smem0 = (size_t)2 * f->nrx * f->ntx * sizeof(double2);
   const double nlos_rate = f->doppler / f->fs, los_rate = f->los_doppler / f->fs;
   if (mode == 0) {
+    const size_t draws = (size_t)f->nrx * f->ntx + 2 * (size_t)f->L + 2 * (size_t)f->L * f->S;
+    const int staged = smem0 + draws * sizeof(double) <= 32 * 1024 ? 1 : 0;
+    const size_t smem = smem0 + (staged ? draws * sizeof(double) : 0);
     if (smem > 48 * 1024)
       HPX_CUDA(cudaFuncSetAttribute(k_fading_params<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_fading_params<0><<<B, 128, smem, as_stream(stream)>>>(fc, nlos_rate, los_rate, seed, drop0, nullptr, nullptr,
                                                             nullptr, nullptr, nullptr, f->d_rx_corr, f->d_tx_corr,
                                                             static_cast<unsigned char*>(state), f->stride, f->off_w,
-                                                            f->off_p0, f->off_spatial);
+                                                            f->off_p0, f->off_spatial, staged);
   } else {
+    const size_t smem = smem0;
     if ((!la || !lp) || (f->S > 0 && (!na || !np_)) || !sp) return hpx_fail(HPX_ERR_ARG, "fading_load: null array");
     if (smem > 48 * 1024)
       HPX_CUDA(cudaFuncSetAttribute(k_fading_params<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // explicit spatial responses are used as given (the caller applied any correlation)
     k_fading_params<1><<<B, 128, smem, as_stream(stream)>>>(fc, nlos_rate, los_rate, 0, 0, la, na, lp, np_, sp, nullptr,
                                                             nullptr, static_cast<unsigned char*>(state), f->stride,
-                                                            f->off_w, f->off_p0, f->off_spatial);
+                                                            f->off_w, f->off_p0, f->off_spatial, 0);
   }
   HPX_LAUNCHED("fading_params");
   return HPX_OK;
