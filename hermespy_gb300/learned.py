@@ -13,7 +13,7 @@ come from the engine's own drops over random channels: 4-23 taps with an
 exponential power-delay profile, Doppler U[0, 1000] Hz and SNR U[-5, 30] dB.
 
 ``LearnedChannelEstimation`` keeps the tap-domain LMMSE estimator as fallback and
-judge: the network is used only while its validation NMSE is within 0.5 dB of
+yardstick: the network is used only while its validation NMSE is within 0.5 dB of
 LMMSE's on the link's channel.
 """
 
