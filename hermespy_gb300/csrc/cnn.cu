@@ -694,12 +694,9 @@ hpx_status forward_tc(const hpx_cnn* c, int B, const __nv_bfloat16* x0, __nv_bfl
   const float inv = 1.f / (float)(NPAIR * c->H * c->W);
   const int64_t tiles = (int64_t)B * c->H * ((c->W + TCW - 1) / TCW);
   const int grid = (int)std::min<int64_t>(tiles, (int64_t)c->num_sms * TC_CTAS_PER_SM);
-  static bool attr = false;
-  if (!attr) {
-    HPX_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
-    HPX_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
-    attr = true;
-  }
+  // per call: the attribute belongs to the current device's context
+  HPX_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+  HPX_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
   const __nv_bfloat16* in = x0;
   CUtensorMap map;
   for (int l = 0; l < LAYERS - 1; ++l) {
