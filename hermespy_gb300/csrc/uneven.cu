@@ -447,6 +447,8 @@ __global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __
     fc.ntx = d.ntx;
     fc.D = d.D;
     fc.delay = a.delay + d.taps;
+    fc.G = 0;  // delay groups are a propagate-kernel table; this kernel walks the taps
+    fc.gfirst = fc.gdelay = nullptr;
     fc.amp = a.amp + 2 * d.taps;
     for (int l = threadIdx.x; l < d.L; l += blockDim.x) dl[l] = fc.delay[l];
     u_realize(d, a.S, a.seed, drop, Wp, P0, Sm);
