@@ -187,34 +187,38 @@ __global__ void __launch_bounds__(128) k_conv3x3(int H, int W, const __nv_bfloat
 }
 
 // ------------------------------------------------------------ tcgen05 forward
-// One tile = 128 consecutive output columns of one word of one drop (thread i <->
-// TMEM lane i <-> column w0 + i). The input rows h - 1, h, h + 1 over columns
+// One tile = 128 consecutive output columns of two words of one drop (thread i <->
+// TMEM lane i <-> column w0 + i). The input rows h0 - 1 .. h0 + 2 over columns
 // w0 - 1 .. w0 + 128 arrive by TMA as four planes of 8 channels: a 4-D tensor map
 // over the planar activation (channel in chunk, column, word, 4 drop + chunk) with
-// box (8, 130, 3, 1) delivers plane j as three contiguous 2 080-byte rows (row r,
-// column p at (r 130 + p) 16 bytes), zero outside the grid. For tap (dy, dx)
-// the A operand (128 elements x 16 channels) is then the K-major, unswizzled
-// operand that starts at element (dy, dx) of planes 2 kc and 2 kc + 1: rows 16
-// bytes apart (core matrices 128 bytes apart along M), the two 8-channel halves a
-// plane apart along K. The weights of tap t and channel half kc form a 32 x 16
-// K-major block. Eighteen MMAs (M = 128, N = 32, K = 16, BF16 in, FP32 out) give
-// the tile. The CTA walks tiles persistently as a warp-specialized pipeline: warp 0
-// (one thread) issues the TMA copies into three input stages and the MMAs into two
-// accumulator slots in tensor memory; warps 1-4 each read a quarter of a slot's
-// lanes, release the slot through an mbarrier and run the epilogue, so the MMAs of
-// tile k + 1 queue while tile k is stored. No CTA-wide barrier inside the loop. A
-// tensor-core or TMA wait that times out writes NaN outputs and sets *fail.
+// box (8, 130, 4, 1) delivers plane j as four contiguous 2 080-byte rows (row r,
+// column p at (r 130 + p) 16 bytes), zero outside the grid. For output row r and
+// tap (dy, dx) the A operand (128 elements x 16 channels) is then the K-major,
+// unswizzled operand that starts at element (r + dy, dx) of planes 2 kc and 2 kc + 1:
+// rows 16 bytes apart (core matrices 128 bytes apart along M), the two 8-channel
+// halves a plane apart along K. The weights of tap t and channel half kc form a
+// 32 x 16 K-major block. Eighteen MMAs per output row (M = 128, N = 32, K = 16, BF16
+// in, FP32 out) give the tile. The CTA walks tiles persistently as a
+// warp-specialized pipeline: warp 0 (one thread) issues the TMA copies into two input
+// stages and the MMAs into two accumulator slots (32 TMEM columns per output row);
+// warps 1-4 each read a quarter of a slot's lanes, release the slot through an
+// mbarrier and run the epilogue, so the MMAs of tile k + 1 queue while tile k is
+// stored. No CTA-wide barrier inside the loop. A tensor-core or TMA wait that times
+// out writes NaN outputs and sets *fail.
 constexpr int TCW = 128;                           // output columns per tile
 constexpr int TC_INW = TCW + 2;                    // input columns with halo
-constexpr int TC_BOX = 3 * TC_INW * 16;            // bytes of one TMA box (one plane)
+constexpr int TC_ROWS = 2;                         // output rows (words) per tile
+constexpr int TC_INH = TC_ROWS + 2;                // input rows with halo
+constexpr int TC_BOX = TC_INH * TC_INW * 16;       // bytes of one TMA box (one plane)
 constexpr int TC_PLANE = (TC_BOX + 127) / 128 * 128;  // plane stride (TMA destinations 128-byte aligned)
 constexpr int TC_BUF = 4 * TC_PLANE;               // one input stage
-constexpr int TC_STAGES = 3;                       // input stages in flight per CTA
+constexpr int TC_STAGES = 2;                       // input stages in flight per CTA
 constexpr int TC_WBLK = CH * 16 * 2;               // one 32 x 16 bf16 weight block
 constexpr int TC_SMEM = TC_STAGES * TC_BUF + 18 * TC_WBLK + 128;  // + alignment slack
 constexpr uint32_t TC_IDESC = tc::idesc_f16_f32(128, CH) | (1u << 7) | (1u << 10);  // A, B: BF16
 constexpr long long TC_CONV_WAIT = 40ll * 1000 * 1000;  // cycles (~20 ms)
-constexpr int TC_CTAS_PER_SM = 2;                  // shared memory: 2 x 92 KB
+constexpr int TC_CTAS_PER_SM = 2;                  // shared memory: 2 x 83 KB
+constexpr int TC_SLOT = TC_ROWS * 32;              // TMEM columns of one accumulator slot
 constexpr int TC_THREADS = 160;                    // warp 0: TMA + MMA issue; warps 1-4: epilogue
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
@@ -261,7 +265,7 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) k_conv3x3_tc(
     }
   }
   if (warp == 0) {
-    tc::tmem_alloc(&tmem_slot, 64);  // two accumulator slots of 32 columns
+    tc::tmem_alloc(&tmem_slot, 2 * TC_SLOT);  // two accumulator slots, 32 columns per output row
     tc::tmem_relinquish();
   }
   tc::fence_proxy_async_smem();
@@ -270,16 +274,16 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) k_conv3x3_tc(
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
   bool ok = skip == 0;
-  const int tiles_w = (W + TCW - 1) / TCW;
-  const int64_t ntiles = (int64_t)B * H * tiles_w;
+  const int tiles_w = (W + TCW - 1) / TCW, tiles_h = (H + TC_ROWS - 1) / TC_ROWS;
+  const int64_t ntiles = (int64_t)B * tiles_h * tiles_w;
   // tiles of this CTA: blockIdx.x + k gridDim.x, k < K
   const int K = blockIdx.x < ntiles ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x) + 1 : 0;
   auto decode = [&](int k, int& b, int& h, int& w0) {
     const int64_t tile = blockIdx.x + (int64_t)k * gridDim.x;
     const int64_t bh = tile / tiles_w;
     w0 = (int)(tile - bh * tiles_w) * TCW;
-    b = (int)(bh / H);
-    h = (int)(bh - (int64_t)b * H);
+    b = (int)(bh / tiles_h);
+    h = (int)(bh - (int64_t)b * tiles_h) * TC_ROWS;  // first output row of the tile
   };
   if (warp == 0) {
     // ---- producer: lane 0 issues the TMA into the stages and the MMAs into the two
@@ -311,15 +315,19 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) k_conv3x3_tc(
           // every operand is a fixed offset from the two buffers: the descriptors
           // differ from the buffers' only in the start-address field (address / 16)
           const uint64_t a_desc = tc::smem_desc(s_in + st * TC_BUF, TC_PLANE, 128);
-          const uint32_t d = tmem + (uint32_t)(slot * 32);
 #pragma unroll
-          for (int tap = 0; tap < 9; ++tap) {
-            const int dy = tap / 3, dx = tap - dy * 3;
+          for (int r = 0; r < TC_ROWS; ++r) {  // output row r reads input rows r .. r + 2
+            const uint32_t d = tmem + (uint32_t)(slot * TC_SLOT + r * 32);
 #pragma unroll
-            for (int kc = 0; kc < 2; ++kc) {
-              const uint64_t ad = a_desc + (uint64_t)((2 * kc * TC_PLANE + (dy * TC_INW + dx) * 16) >> 4);
-              const uint64_t bd = b_desc + (uint64_t)(((tap * 2 + kc) * TC_WBLK) >> 4);
-              tc::mma_f16(d, ad, bd, TC_IDESC, (tap | kc) != 0);
+            for (int tap = 0; tap < 9; ++tap) {
+              const int dy = tap / 3, dx = tap - dy * 3;
+#pragma unroll
+              for (int kc = 0; kc < 2; ++kc) {
+                const uint64_t ad =
+                    a_desc + (uint64_t)((2 * kc * TC_PLANE + ((r + dy) * TC_INW + dx) * 16) >> 4);
+                const uint64_t bd = b_desc + (uint64_t)(((tap * 2 + kc) * TC_WBLK) >> 4);
+                tc::mma_f16(d, ad, bd, TC_IDESC, (tap | kc) != 0);
+              }
             }
           }
           tc::mma_commit(&bar_mma[slot]);
@@ -347,14 +355,20 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) k_conv3x3_tc(
       const int slot = k & 1;
       if (ok) ok = tc::mbar_wait(&bar_mma[slot], (uint32_t)((k >> 1) & 1), TC_CONV_WAIT);
       tc::fence_after_sync();
-      float acc[32];
-      tc::tmem_ld32(tmem + ((uint32_t)(qtr * 32) << 16) + (uint32_t)(slot * 32), acc);
+      float accs[TC_ROWS][32];
+#pragma unroll
+      for (int r = 0; r < TC_ROWS; ++r)
+        tc::tmem_ld32(tmem + ((uint32_t)(qtr * 32) << 16) + (uint32_t)(slot * TC_SLOT + r * 32), accs[r]);
       tc::fence_before_sync();
       tc::mbar_arrive(&bar_free[slot]);  // the slot may take tile k + 2
-      int b, h, w0;
-      decode(k, b, h, w0);
+      int b, h0, w0;
+      decode(k, b, h0, w0);
       const int w = w0 + qtr * 32 + lane;
-      if (w < W) {
+#pragma unroll
+      for (int r = 0; r < TC_ROWS; ++r) {
+      const int h = h0 + r;
+      const float* acc = accs[r];
+      if (w < W && h < H) {
         const float nan = __int_as_float(0x7fc00000);
         if (EPI == 0) {
           uint32_t u[NPAIR];
@@ -381,13 +395,14 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) k_conv3x3_tc(
                                     : make_float2(nan, nan);
         }
       }
+      }
     }
     if (!ok && skip == 0) atomicExch(fail, 1);
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (warp == 0) tc::tmem_dealloc(tmem, 2 * TC_SLOT);
 }
 
 // Tensor map of a planar BF16 activation [B][4 chunks][H][W][8] with the conv tile's box:
@@ -408,7 +423,7 @@ hpx_status activation_map(const __nv_bfloat16* act, int B, int H, int W, CUtenso
   }
   const cuuint64_t dims[4] = {8, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B * 4};
   const cuuint64_t strides[3] = {16, (cuuint64_t)W * 16, (cuuint64_t)H * W * 16};
-  const cuuint32_t box[4] = {8, (cuuint32_t)TC_INW, 3, 1};
+  const cuuint32_t box[4] = {8, (cuuint32_t)TC_INW, (cuuint32_t)TC_INH, 1};
   const cuuint32_t estride[4] = {1, 1, 1, 1};
   const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(act), dims, strides,
                             box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -692,7 +707,7 @@ hpx_status forward(const hpx_cnn* c, int B, const __nv_bfloat16* x0, __nv_bfloat
 hpx_status forward_tc(const hpx_cnn* c, int B, const __nv_bfloat16* x0, __nv_bfloat16* const* act_out,
                       const float2* resid, float2* out_c, int ccols, cudaStream_t s) {
   const float inv = 1.f / (float)(NPAIR * c->H * c->W);
-  const int64_t tiles = (int64_t)B * c->H * ((c->W + TCW - 1) / TCW);
+  const int64_t tiles = (int64_t)B * ((c->H + TC_ROWS - 1) / TC_ROWS) * ((c->W + TCW - 1) / TCW);
   const int grid = (int)std::min<int64_t>(tiles, (int64_t)c->num_sms * TC_CTAS_PER_SM);
   // per call: the attribute belongs to the current device's context
   HPX_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
