@@ -424,6 +424,8 @@ hpx_status hpx_ls_create_streams(const hpx_frame* frame, int32_t C, int32_t num_
     return hpx_fail(HPX_ERR_ARG, "ls: columns must cover the frame's resource columns");
   if (frame->info.num_refs < 1) return hpx_fail(HPX_ERR_ARG, "ls: frame has no reference elements");
   if (num_streams < 1 || num_streams > 64) return hpx_fail(HPX_ERR_ARG, "ls: num_streams must be in [1, 64]");
+  if (W > 32767 || frame->info.num_columns > 65535)  // table positions pack word << 16 | column
+    return hpx_fail(HPX_ERR_UNSUPPORTED, "ls: frames up to 32767 words of 65535 columns");
   if (num_streams > 1 && frame->pilot_comb < num_streams)
     return hpx_fail(HPX_ERR_UNSUPPORTED, "Least-Squares channel estimation of %d streams needs a pilot comb of at "
                                          "least %d (frame has %d)", num_streams, num_streams, frame->pilot_comb);
