@@ -91,7 +91,8 @@ def oracle_drop(args):
     else:
         cfg = LinkConfig(massive_frame(), massive_channel(64, 0.7, 61.44e6), 61.44e6, 16, 64, "ideal", "lmmse",
                          "snr")
-    return simulate_drop(cfg, seed, drop, level)["errors"]
+    stages = {}
+    return simulate_drop(cfg, seed, drop, level, timings=stages)["errors"], stages
 
 
 def uneven_oracle_drop(seed, drop):
@@ -104,14 +105,15 @@ def uneven_oracle_drop(seed, drop):
     from oracle.link import LinkConfig, simulate_drop
 
     d = random_drops(1, 1000 + drop)[0]
+    stages = {}
     N = d.fft_size
     C, cp = int(np.floor(0.586 * N)), N * 72 // 1024
     spec = FrameSpec(N, [Resource(1, cp / N, [(DATA, C)])], [Section(d.num_words, [0])], d.modulation_order, True)
     k = np.arange(d.num_taps)
     ch = FadingConfig(k * 50e-9, d.power_profile(), np.zeros(d.num_taps), 20, d.doppler_frequency)
     cfg = LinkConfig(spec, ch, N * 30e3, d.num_tx, d.num_rx, "ideal", "lmmse", "snr")
-    simulate_drop(cfg, seed, drop, d.snr_db)
-    return d.num_words * C * int(np.log2(d.modulation_order)) * d.num_tx
+    simulate_drop(cfg, seed, drop, d.snr_db, timings=stages)
+    return d.num_words * C * int(np.log2(d.modulation_order)) * d.num_tx, stages
 
 
 def cpu_pool():
@@ -130,8 +132,9 @@ def cpu_workers(spec: Spec, cores: int) -> int:
     return min(cores, 8) if spec.name == "massive" else cores
 
 
-def time_cpu(pool, cores, spec: Spec, rounds: int, seed: int = 11) -> tuple[float, int, float]:
-    """`rounds` rounds of parallel oracle drops; returns (bits/s, drops, seconds)."""
+def time_cpu(pool, cores, spec: Spec, rounds: int, seed: int = 11, split: dict | None = None):
+    """`rounds` rounds of parallel oracle drops; returns (bits/s, drops, seconds). `split`,
+    if given, accumulates the workers' seconds per stage of the drop."""
 
     rng = np.random.default_rng(seed)
     par = cpu_workers(spec, cores)
@@ -142,8 +145,17 @@ def time_cpu(pool, cores, spec: Spec, rounds: int, seed: int = 11) -> tuple[floa
     t0 = time.perf_counter()
     res = pool.map(oracle_drop, work, chunksize=1)
     dt = time.perf_counter() - t0
-    bits = sum(res) if spec.name == "uneven" else drops * spec.bits_per_drop
+    bits = sum(r[0] for r in res) if spec.name == "uneven" else drops * spec.bits_per_drop
+    if split is not None:
+        for _, st in res:
+            for k, v in st.items():
+                split[k] = split.get(k, 0.0) + v
     return bits / dt, drops, dt
+
+
+def stage_shares(split: dict) -> dict:
+    total = sum(split.values()) or 1.0
+    return {k: round(v / total, 4) for k, v in split.items()}
 
 
 def cpu_sample_text(spec, drops, secs):
@@ -162,8 +174,9 @@ def run_reference(args, spec: Spec) -> None:
     for _ in range(args.warmup):
         time_cpu(pool, cores, spec, rounds)
     drops, secs, bits = 0, 0.0, 0.0
+    split = {}
     for k in range(args.steps):
-        v, d, s = time_cpu(pool, cores, spec, rounds, seed=100 + k)
+        v, d, s = time_cpu(pool, cores, spec, rounds, seed=100 + k, split=split)
         drops += d
         secs += s
         bits += v * s
@@ -176,7 +189,7 @@ def run_reference(args, spec: Spec) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox draws)",
         "config": dict(spec.config, drops_per_step=cpu_workers(spec, cores) * rounds, bits_per_drop=spec.bits_per_drop),
         "cpu_baseline": {"value": value, "unit": "bits/s", "cores": cpu_workers(spec, cores), "kind": "port",
-                         "sample": cpu_sample_text(spec, drops, secs)},
+                         "sample": cpu_sample_text(spec, drops, secs), "stage_share": stage_shares(split)},
         "e2e": {"value": value, "unit": "bits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -792,7 +805,9 @@ def main() -> None:
         pk = peaks()
         info = stage_report(res["stage_ms"], args.steps, res["work"], drops, pk)
         roof = roofline_of(info, pk, drops)
-        cpu_value, cpu_drops, cpu_s = time_cpu(pool, cores, spec, args.cpu_rounds if spec.name != "massive" else 1)
+        cpu_split = {}
+        cpu_value, cpu_drops, cpu_s = time_cpu(pool, cores, spec, args.cpu_rounds if spec.name != "massive" else 1,
+                                               split=cpu_split)
         if spec.name == "uneven":
             spec.config = dict(spec.config, bits_per_drop_mean=spec.bits_per_drop)
         pool.close()
@@ -809,7 +824,8 @@ def main() -> None:
             "gpu_launches": res["launches"] * args.steps,
             "roofline": roof, "stages": info,
             "cpu_baseline": {"value": cpu_value, "unit": "bits/s", "cores": cpu_workers(spec, cores), "kind": "port",
-                             "sample": cpu_sample_text(spec, cpu_drops, cpu_s)},
+                             "sample": cpu_sample_text(spec, cpu_drops, cpu_s),
+                             "stage_share": stage_shares(cpu_split)},
             "clocks": clk.summary(),
         }
         line.update(res["extra"])

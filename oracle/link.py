@@ -24,6 +24,8 @@ from __future__ import annotations
 
 from dataclasses import dataclass
 
+import time
+
 import numpy as np
 
 from . import estimation, fading, mapping, ofdm, streams
@@ -52,21 +54,39 @@ def noise_power(cfg: LinkConfig, layout: FrameLayout, level_db: float) -> float:
     return 1.0 / level * cfg.channel.gain * float(np.sum(cfg.channel.power_profile))
 
 
-def simulate_drop(cfg: LinkConfig, seed: int, drop: int, level_db: float, keep: bool = False) -> dict:
+def simulate_drop(cfg: LinkConfig, seed: int, drop: int, level_db: float, keep: bool = False,
+                  timings: dict | None = None) -> dict:
+    """One drop of the link. `timings`, if given, accumulates the seconds spent per
+    stage (transmit, fading realization, propagation, AWGN, receive, estimation,
+    detection) for the CPU baseline's split."""
+
+    clock = [time.perf_counter()]
+
+    def lap(stage: str) -> None:
+        if timings is not None:
+            now = time.perf_counter()
+            timings[stage] = timings.get(stage, 0.0) + now - clock[0]
+            clock[0] = now
+
     layout = FrameLayout(cfg.frame)
     fs = cfg.sampling_rate
     M = layout.order
     nbits = layout.bits_per_frame()
     tx_bits = np.stack([streams.data_bits(seed, drop, s, nbits) for s in range(cfg.num_tx)])
     x = np.stack([ofdm.modulate(layout, mapping.get_symbols(M, tx_bits[s]), s) for s in range(cfg.num_tx)])
+    lap("transmit")
     sample = fading.realize(cfg.channel, seed, drop, cfg.num_rx, cfg.num_tx)
+    lap("fading_realize")
     y = fading.propagate(sample, x, fs)
+    lap("fading_propagate")
     p = noise_power(cfg, layout, level_db)
     if p > 0:
         y = y + streams.awgn(seed, drop, cfg.num_rx, y.shape[1], p)
+    lap("awgn")
     T = layout.samples_per_frame
     frame = y[:, :T]
     grids = np.stack([ofdm.demodulate(layout, frame[r]) for r in range(cfg.num_rx)])  # (Nrx, W, N)
+    lap("receive")
     if cfg.estimator == "ls":
         if (cfg.num_rx != 1 or cfg.num_tx != 1) and layout.spec.pilot_comb < max(cfg.num_tx, 2):
             raise NotImplementedError("Least-Squares channel estimation is only implemented for SISO links")
@@ -75,6 +95,7 @@ def simulate_drop(cfg: LinkConfig, seed: int, drop: int, level_db: float, keep: 
         H = estimation.tap_lmmse_estimate(layout, grids, cfg.channel, fs, p, cfg.num_tx)
     else:
         H = estimation.ideal_csi(layout, sample, fs)
+    lap("estimate")
     ydata = ofdm.pick(layout, grids)           # (Nrx, K)
     hdata = ofdm.pick(layout, H)               # (Nrx, Ntx, K)
     if cfg.equalizer == "zf":
@@ -83,6 +104,7 @@ def simulate_drop(cfg: LinkConfig, seed: int, drop: int, level_db: float, keep: 
         xhat = estimation.lmmse_equalize(ydata, hdata, p)
     rx_bits = np.stack([mapping.detect_bits(M, xhat[s]) for s in range(xhat.shape[0])])
     errors = int(np.sum(np.abs(tx_bits.astype(np.int8) - rx_bits.astype(np.int8))))
+    lap("detect")
     out = {"errors": errors, "bits": int(tx_bits.size), "noise_power": p}
     if keep:
         out.update(tx_bits=tx_bits, x=x, y=y, grids=grids, H=H, xhat=xhat, rx_bits=rx_bits, sample=sample)

@@ -32,6 +32,9 @@ def test_reference_arm_contract():
     assert "workload" in d["config"]
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    share = cb["stage_share"]  # per-stage split of the oracle drop's CPU time
+    assert {"transmit", "fading_propagate", "receive", "estimate", "detect"} <= set(share)
+    assert abs(sum(share.values()) - 1.0) < 1e-2
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
