@@ -332,6 +332,15 @@ def roofline_of(info, pk, drops):
             "frac": d["frac"], "traffic": traffic, "peak_source": pk["src"]}
 
 
+def total_errors(errors) -> int:
+    """Sum of per-drop bit errors; raises if a drop carries a device failure flag
+    (bounded wait ran out, non-finite equalizer pivot) instead of summing it."""
+
+    from hermespy_gb300 import _lib
+
+    return int(_lib.drop_counts(errors.cpu().numpy()).sum())
+
+
 def e2e_time(torch, eng, p_host, dev, drop0, steps):
     """Public API end to end: pinned host noise powers in, host error counts out."""
 
@@ -386,7 +395,7 @@ def bench_link4x4(ctx, spec, args):
         ], ev, stream)
 
     total_ms, stage_ms = ctx["timer"].run(step, stages, args.steps, args.warmup, ctx["drop_base"], drops)
-    ber = float(errors.sum().item()) / (drops * spec.bits_per_drop)
+    ber = float(total_errors(errors)) / (drops * spec.bits_per_drop)
     work = {"fading_realize": (eng._fading.state_bytes, "hbm"), "ofdm_modulate_bits": (8 * 4 * T, "hbm"),
             "fading_propagate": (8 * (4 * T + 4 * (T + D)), "hbm"), "ofdm_demodulate": (8 * 4 * 14 * (1024 + 600), "hbm"),
             "detect_ideal_lmmse": (8 * 4 * 14 * 600 + 4, "hbm")}
@@ -451,7 +460,7 @@ def bench_estimators(ctx, spec, args):
         stages = [s for s, _ in calls]
         total_ms, stage_ms = ctx["timer"].run(step, stages, args.steps, args.warmup,
                                               ctx["drop_base"] + (k << 36), drops)
-        ber = float(errors.sum().item()) / (drops * spec.bits_per_drop)
+        ber = float(total_errors(errors)) / (drops * spec.bits_per_drop)
         results[name] = {"total_ms": total_ms, "stage_ms": stage_ms, "ber": ber}
     # channel-estimate quality on a validation batch (untimed): NMSE over data elements
     nval = min(drops, 1024)
@@ -469,7 +478,7 @@ def bench_estimators(ctx, spec, args):
     eng.estimator = selected
     api_ms, _ = ctx["timer"].run(lambda d0, ev: eng.run(d0, p, errors), [], args.steps, args.warmup,
                                  ctx["drop_base"] + (3 << 36), drops)
-    api_ber = float(errors.sum().item()) / (drops * spec.bits_per_drop)
+    api_ber = float(total_errors(errors)) / (drops * spec.bits_per_drop)
     # e2e of the selected path through the public API
     e2e_s, hb, db = e2e_time(torch, eng, p_host, dev, ctx["drop_base"] + (1 << 39), max(3, args.steps // 2))
     comparison = {}
@@ -610,7 +619,7 @@ def bench_massive(ctx, spec, args):
         ], ev, stream)
 
     total_ms, stage_ms = ctx["timer"].run(step, stages, args.steps, args.warmup, ctx["drop_base"], drops)
-    ber = float(errors.sum().item()) / (drops * spec.bits_per_drop)
+    ber = float(total_errors(errors)) / (drops * spec.bits_per_drop)
     fp64_frac = float(n64.sum().item()) / (drops * 14 * Cu)
     REs = 14 * Cu
     work = {"fading_realize": (fad.state_bytes, "hbm"), "ofdm_modulate_bits": (8 * NTX * T, "hbm"),
@@ -691,7 +700,7 @@ def homogeneous_persistent(ctx, args, drops: int = 4096) -> dict:
     ms = t0.elapsed_time(t1) / args.steps
     bits = float(batch.bits.sum())
     return {"drops_per_step": drops, "ms_per_step": round(ms, 4), "bits_per_s": bits / (ms / 1e3),
-            "ber": float(batch.errors.sum().item()) / bits, "launch_shape": best}
+            "ber": float(total_errors(batch.errors)) / bits, "launch_shape": best}
 
 
 def bench_uneven(ctx, spec, args):
@@ -715,7 +724,7 @@ def bench_uneven(ctx, spec, args):
     t1.record(stream)
     torch.cuda.synchronize()
     total_ms = t0.elapsed_time(t1)
-    ber = float(batch.errors.sum().item()) / total_bits
+    ber = float(total_errors(batch.errors)) / total_bits
     # algorithmic HBM bytes per drop: transmit write, propagation read + write, receive
     # read + grid write, detection grid read
     byts = 0.0

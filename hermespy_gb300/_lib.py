@@ -20,6 +20,8 @@ HPX_OK, HPX_ERR_ARG, HPX_ERR_SHAPE, HPX_ERR_UNSUPPORTED, HPX_ERR_CUDA, HPX_ERR_N
 RE_REFERENCE, RE_DATA, RE_NULL = 0, 1, 2
 EQ_ZF, EQ_LMMSE = 0, 1
 EST_IDEAL, EST_LS = 0, 1
+# flag bits of the per-drop error words (a flagged drop holds no valid count)
+DROP_TIMEOUT, DROP_NUMERIC, DROP_COUNT = 0x80000000, 0x40000000, 0x3FFFFFFF
 
 c_void_p = ctypes.c_void_p
 c_int32 = ctypes.c_int32
@@ -157,6 +159,11 @@ _SIGNATURES = {
     "hpx_uneven_replay": [c_void_p, c_void_p],
     "hpx_detect_csi": [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64,
                        c_int64, c_int32, c_void_p, c_void_p],
+    "hpx_drop_status": [c_void_p, c_int64],
+    "hpx_lmmse_status": [c_void_p, c_int32, c_void_p],
+    "hpx_lmmse_inject_timeout": [c_void_p, c_void_p],
+    "hpx_cnn_status": [c_void_p, c_int32, c_void_p],
+    "hpx_cnn_inject_timeout": [c_void_p, c_void_p],
 }
 
 _lock = threading.Lock()
@@ -205,6 +212,20 @@ def check(status: int) -> None:
     if status == HPX_ERR_UNSUPPORTED:
         raise NotImplementedError(msg)
     raise RuntimeError(msg)
+
+
+def drop_counts(errors) -> "np.ndarray":
+    """Host per-drop error words (any integer array of the device's uint32 words) ->
+    int64 bit-error counts. Raises RuntimeError (through hpx_drop_status) if a drop
+    carries a failure flag: a bounded device wait ran out (HPX_DROP_TIMEOUT) or its
+    equalizer met a non-finite pivot (HPX_DROP_NUMERIC); such a drop has no count,
+    so nothing may be summed."""
+
+    import numpy as np
+
+    words = np.ascontiguousarray(np.asarray(errors).astype(np.int64) & 0xFFFFFFFF, dtype=np.uint32)
+    check(load().hpx_drop_status(words.ctypes.data_as(c_void_p), words.size))
+    return words.astype(np.int64)
 
 
 def call(name: str, *args) -> None:

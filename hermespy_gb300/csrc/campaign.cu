@@ -29,6 +29,7 @@ struct hpx_campaign {
   int* d_level = nullptr;            // [max_batch] level of each drop of the batch (-1: none)
   float* d_noise = nullptr;          // [max_batch]
   uint32_t* d_drop_errors = nullptr; // [max_batch]
+  unsigned int* d_flags = nullptr;   // [1] HPX_DROP_* flags of drops left out of the sums
 };
 
 namespace {
@@ -53,12 +54,20 @@ __global__ void k_assign(int L, int batch, const float* __restrict__ power, cons
   }
 }
 
+// A drop whose error word carries a failure flag (HPX_DROP_TIMEOUT / NUMERIC) stays
+// out of the sums; its flag goes to *flags, which ends the run with an error status.
 __global__ void k_accumulate(int batch, const int* __restrict__ level, const uint32_t* __restrict__ errors,
                              double inv_bits, double* __restrict__ sum, double* __restrict__ sq,
-                             unsigned long long* __restrict__ count, unsigned long long* __restrict__ errsum) {
+                             unsigned long long* __restrict__ count, unsigned long long* __restrict__ errsum,
+                             unsigned int* __restrict__ flags) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < batch; i += gridDim.x * blockDim.x) {
     const int lv = level[i];
     if (lv < 0) continue;
+    const uint32_t f = errors[i] & ~HPX_DROP_COUNT;
+    if (f) {
+      atomicOr(flags, f);
+      continue;
+    }
     const double x = (double)errors[i] * inv_bits;
     atomicAdd(sum + lv, x);
     atomicAdd(sq + lv, x * x);
@@ -94,7 +103,7 @@ __global__ void k_confidence(int L, int min_samples, double accuracy, double con
 void release(hpx_campaign* c) {
   if (!c) return;
   void* p[] = {c->d_power, c->d_sum, c->d_sq, c->d_count, c->d_errors, c->d_confident, c->d_active, c->d_level,
-               c->d_noise, c->d_drop_errors};
+               c->d_noise, c->d_drop_errors, c->d_flags};
   for (void* q : p)
     if (q) cudaFree(q);
   delete c;
@@ -135,6 +144,7 @@ hpx_status hpx_campaign_create(int32_t num_levels, const float* noise_power, dou
       (e = cudaMalloc(&c->d_level, sizeof(int) * max_batch)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_noise, sizeof(float) * max_batch)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_drop_errors, sizeof(uint32_t) * max_batch)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_flags, sizeof(unsigned int))) != cudaSuccess ||
       (e = cudaMemcpy(c->d_power, noise_power, sizeof(float) * L, cudaMemcpyHostToDevice)) != cudaSuccess) {
     release(c);
     return hpx_cuda_status(e, "campaign buffers");
@@ -161,6 +171,7 @@ hpx_status hpx_campaign_reset(hpx_campaign* c) {
   HPX_CUDA(cudaMemset(c->d_count, 0, sizeof(unsigned long long) * L));
   HPX_CUDA(cudaMemset(c->d_errors, 0, sizeof(unsigned long long) * L));
   HPX_CUDA(cudaMemset(c->d_confident, 0, sizeof(int) * L));
+  HPX_CUDA(cudaMemset(c->d_flags, 0, sizeof(unsigned int)));
   const int all = c->L;
   HPX_CUDA(cudaMemcpy(c->d_active, &all, sizeof(int), cudaMemcpyHostToDevice));
   return HPX_OK;
@@ -177,6 +188,7 @@ hpx_status hpx_campaign_run(hpx_campaign* c, hpx_link* link, uint64_t seed, int6
   HPX_CUDA(cudaMemcpyAsync(&active, c->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
   HPX_CUDA(cudaStreamSynchronize(s));
   int64_t done = 0;
+  unsigned int flags = 0;
   const int acc_blocks = (batch + 255) / 256;
   for (int b = 0; b < max_batches && active > 0; ++b) {
     k_assign<<<1, 256, sizeof(int) * c->L, s>>>(c->L, batch, c->d_power, c->d_confident, c->d_count,
@@ -184,7 +196,7 @@ hpx_status hpx_campaign_run(hpx_campaign* c, hpx_link* link, uint64_t seed, int6
     HPX_LAUNCHED("campaign assign");
     HPX_TRY(hpx_link_run(link, seed, drop0 + done, batch, c->d_noise, c->d_drop_errors, stream));
     k_accumulate<<<acc_blocks, 256, 0, s>>>(batch, c->d_level, c->d_drop_errors, 1.0 / c->bits_per_drop, c->d_sum,
-                                            c->d_sq, c->d_count, c->d_errors);
+                                            c->d_sq, c->d_count, c->d_errors, c->d_flags);
     HPX_LAUNCHED("campaign accumulate");
     k_confidence<<<1, 256, 0, s>>>(c->L, c->min_samples, c->accuracy, c->confidence,
                                    (unsigned long long)c->max_drops, c->d_sum, c->d_sq, c->d_count, c->d_confident,
@@ -193,11 +205,17 @@ hpx_status hpx_campaign_run(hpx_campaign* c, hpx_link* link, uint64_t seed, int6
     done += batch;
     if ((b + 1) % check_every == 0 || b + 1 == max_batches) {
       HPX_CUDA(cudaMemcpyAsync(&active, c->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+      HPX_CUDA(cudaMemcpyAsync(&flags, c->d_flags, sizeof(flags), cudaMemcpyDeviceToHost, s));
       HPX_CUDA(cudaStreamSynchronize(s));
+      if (flags) break;
     }
   }
   if (drops_run) *drops_run = done;
   if (levels_active) *levels_active = active;
+  if (flags & HPX_DROP_TIMEOUT)
+    return hpx_fail(HPX_ERR_TIMEOUT, "campaign_run: a drop's tensor-core wait ran out (left out of the sums)");
+  if (flags)
+    return hpx_fail(HPX_ERR_NUMERIC, "campaign_run: a drop's equalizer met a non-finite pivot (left out of the sums)");
   return HPX_OK;
 }
 

@@ -829,6 +829,23 @@ hpx_status hpx_cnn_refine(const hpx_cnn* c, hpx_cf32* csi, int32_t ccols, int32_
   return HPX_OK;
 }
 
+hpx_status hpx_cnn_status(hpx_cnn* c, int32_t clear, void* stream) {
+  if (!c) return hpx_fail(HPX_ERR_ARG, "cnn_status: null argument");
+  cudaStream_t s = as_stream(stream);
+  int flag = 0;
+  HPX_CUDA(cudaMemcpyAsync(&flag, c->d_fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (clear) HPX_CUDA(cudaMemsetAsync(c->d_fail, 0, sizeof(int), s));
+  HPX_CUDA(cudaStreamSynchronize(s));
+  if (flag) return hpx_fail(HPX_ERR_TIMEOUT, "cnn_refine: a bounded TMA / tensor-core wait ran out (estimates are NaN)");
+  return HPX_OK;
+}
+
+hpx_status hpx_cnn_inject_timeout(hpx_cnn* c, void* stream) {
+  if (!c) return hpx_fail(HPX_ERR_ARG, "cnn_inject_timeout: null argument");
+  HPX_CUDA(cudaMemsetAsync(c->d_fail, 0x01, 1, as_stream(stream)));  // the int word becomes 1
+  return HPX_OK;
+}
+
 hpx_status hpx_cnn_train_step(hpx_cnn* c, const hpx_cf32* ls, const hpx_cf32* truth, int32_t ccols, int32_t B,
                               float lr, double* loss, void* stream) {
   if (!c || !ls || !truth) return hpx_fail(HPX_ERR_ARG, "cnn_train_step: null argument");

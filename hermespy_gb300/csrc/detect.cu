@@ -18,6 +18,15 @@ struct hpx_ls {
   float2* d_coef = nullptr;         // [nnz] weight * conj(x_ref) / |x_ref|^2 (the LS division folded in)
 };
 
+// True if the LS table's grid (words x columns) is the frame's: the receivers lay
+// the received grid out by the table's frame and columns.
+bool hpx_ls_matches_frame(const hpx_ls* ls, const hpx_frame* frame) {
+  const hpx_frame_info& a = ls->frame->info;
+  const hpx_frame_info& b = frame->info;
+  return ls->C == b.num_columns && a.num_words == b.num_words && a.num_columns == b.num_columns &&
+         a.num_subcarriers == b.num_subcarriers && a.num_refs == b.num_refs;
+}
+
 namespace {
 
 template <int NRX, int NTX>
@@ -33,7 +42,7 @@ __global__ void k_equalize(int mode, int64_t K, const float2* __restrict__ Hg, c
 #pragma unroll
       for (int t = 0; t < NTX; ++t) H[r][t] = Hg[(((int64_t)b * NRX + r) * NTX + t) * K + k];
     }
-    equalize_one<NRX, NTX>(mode, H, y, s2, x);
+    equalize_one<NRX, NTX>(mode, H, y, s2, x);  // equalized symbols out: NaN inputs stay visible as NaN
     for (int t = 0; t < out_streams; ++t) Xg[((int64_t)b * out_streams + t) * K + k] = x[t];
   }
 }
@@ -58,15 +67,18 @@ __device__ __forceinline__ void stage_bits(uint32_t* bitsm, int BW, int nstreams
   }
 }
 
-__device__ __forceinline__ void block_count(unsigned int local, uint32_t* out) {
+// Block sum of the threads' error counts into *out; `bad` (any thread) adds the
+// HPX_DROP_NUMERIC flag to the drop's word.
+__device__ __forceinline__ void block_count(unsigned int local, bool bad, uint32_t* out) {
   for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
   __shared__ unsigned int warp_sums[32];
   if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = local;
-  __syncthreads();
+  const int any_bad = __syncthreads_or(bad);
   if (threadIdx.x < 32) {
     unsigned int v = threadIdx.x < (blockDim.x >> 5) ? warp_sums[threadIdx.x] : 0u;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (threadIdx.x == 0 && v) atomicAdd(out, v);
+    if (threadIdx.x == 0 && any_bad) atomicOr(out, HPX_DROP_NUMERIC);
   }
 }
 
@@ -116,6 +128,7 @@ __global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_ideal
   const float s2 = nv ? nv[b] : 0.0f;
   const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
   unsigned int local = 0;
+  bool fin = true;
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
     const int64_t k = k0 + j;
     const int c = data_column[k];
@@ -127,7 +140,7 @@ __global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_ideal
 #pragma unroll
       for (int t = 0; t < NTX; ++t) H[r][t] = cmul(Sm[r * NTX + t], g);  // the ideal CSI of hpx_fading_ideal_csi
     }
-    equalize_one<NRX, NTX>(mode, H, y, s2, x);
+    fin &= equalize_one<NRX, NTX>(mode, H, y, s2, x);
 #pragma unroll
     for (int t = 0; t < NTX; ++t) {
       // streams the equalizer does not return are received as zero bits
@@ -137,7 +150,7 @@ __global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_ideal
       local += __popc(rx_v ^ tx_v);
     }
   }
-  block_count(local, errors + b);
+  block_count(local, !fin, errors + b);
 }
 
 // Fused receiver for a given CSI grid (any estimator), one block per (word, drop):
@@ -172,6 +185,7 @@ __global__ void __launch_bounds__(csi_max_threads<NRX, NTX>(), csi_small<NRX, NT
   const float2* hb = csi + (int64_t)b * NRX * NTX * hplane + (int64_t)w * ccols;
   const float2* yb = grid + (int64_t)b * NRX * W * gcols + (int64_t)w * gcols;
   unsigned int local = 0;
+  bool fin = true;
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
     const int64_t k = k0 + j;
     const int c = data_column[k];
@@ -182,7 +196,7 @@ __global__ void __launch_bounds__(csi_max_threads<NRX, NTX>(), csi_small<NRX, NT
 #pragma unroll
       for (int t = 0; t < NTX; ++t) H[r][t] = hb[(int64_t)(r * NTX + t) * hplane + c];
     }
-    equalize_one<NRX, NTX>(mode, H, y, s2, x);
+    fin &= equalize_one<NRX, NTX>(mode, H, y, s2, x);
 #pragma unroll
     for (int t = 0; t < NTX; ++t) {
       const uint32_t rx_v = t < out_streams ? qam_decide(qt, x[t]) : 0u;
@@ -190,7 +204,7 @@ __global__ void __launch_bounds__(csi_max_threads<NRX, NTX>(), csi_small<NRX, NT
       local += __popc(rx_v ^ tx_v);
     }
   }
-  block_count(local, errors + b);
+  block_count(local, !fin, errors + b);
 }
 
 // Fused receiver with the tap-domain LMMSE channel estimate, one block per drop:
@@ -223,6 +237,7 @@ __global__ void __launch_bounds__(LMMSE_THREADS, 2) k_detect_lmmse(LmmseView e, 
   lmmse_drop_taps<NP>(e, b, NRX, grid, gcols, s2, gt, gls, cw, ds);  // ends with __syncthreads
   const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
   unsigned int local = 0;
+  bool fin = true;
   for (int k = threadIdx.x; k < num_data; k += blockDim.x) {
     const int c = data_column[k], w = data_word[k];
     float2 hp[NP];
@@ -234,7 +249,7 @@ __global__ void __launch_bounds__(LMMSE_THREADS, 2) k_detect_lmmse(LmmseView e, 
 #pragma unroll
       for (int t = 0; t < NTX; ++t) H[r][t] = hp[r * NTX + t];
     }
-    equalize_one<NRX, NTX>(mode, H, y, s2, x);
+    fin &= equalize_one<NRX, NTX>(mode, H, y, s2, x);
 #pragma unroll
     for (int t = 0; t < NTX; ++t) {
       const uint32_t rx_v = t < out_streams ? qam_decide(qt, x[t]) : 0u;
@@ -242,7 +257,7 @@ __global__ void __launch_bounds__(LMMSE_THREADS, 2) k_detect_lmmse(LmmseView e, 
       local += __popc(rx_v ^ tx_v);
     }
   }
-  block_count(local, errors + b);
+  block_count(local, !fin, errors + b);
 }
 
 // Fused SISO LS receiver, one block per (word, drop).
@@ -270,6 +285,7 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
   const float s2 = nv ? nv[b] : 0.0f;
   const float2* gb = grid + (int64_t)b * W * gcols;
   unsigned int local = 0;
+  bool fin = true;
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
     const int64_t k = k0 + j;
     const int c = data_column[k];
@@ -284,12 +300,12 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
       h = cadd(h, cscale(ls, weights[e]));
     }
     float2 H[1][1] = {{h}}, y[1] = {gb[w * gcols + c]}, x[1];
-    equalize_one<1, 1>(mode, H, y, s2, x);
+    fin &= equalize_one<1, 1>(mode, H, y, s2, x);
     const uint32_t rx_v = qam_decide(qt, x[0]);
     const uint32_t tx_v = extract_bits_msb(bitsm - wofs, k * m, m);
     local += __popc(rx_v ^ tx_v);
   }
-  block_count(local, errors + b);
+  block_count(local, !fin, errors + b);
 }
 
 // rows = streams * W * C (the stacked tables); blockIdx.y covers LS_ITEMS received
@@ -641,6 +657,27 @@ hpx_status hpx_detect_lmmse(const hpx_lmmse* lm, int32_t nrx, int32_t mode, cons
   if (ntx == 1) return launch(k_detect_lmmse<4, 1>);
   if (ntx == 2) return launch(k_detect_lmmse<4, 2>);
   return launch(k_detect_lmmse<4, 4>);
+}
+
+// Sticky status word of the tensor-core receiver (d_tc_fail): 1 after a bounded
+// wait ran out. Handles without the tensor-core path have no word and report OK.
+hpx_status hpx_lmmse_status(hpx_lmmse* lm, int32_t clear, void* stream) {
+  if (!lm) return hpx_fail(HPX_ERR_ARG, "lmmse_status: null argument");
+  if (!lm->d_tc_fail) return HPX_OK;
+  cudaStream_t s = as_stream(stream);
+  int flag = 0;
+  HPX_CUDA(cudaMemcpyAsync(&flag, lm->d_tc_fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (clear) HPX_CUDA(cudaMemsetAsync(lm->d_tc_fail, 0, sizeof(int), s));
+  HPX_CUDA(cudaStreamSynchronize(s));
+  if (flag) return hpx_fail(HPX_ERR_TIMEOUT, "detect_lmmse: a bounded tensor-core wait ran out (drops flagged)");
+  return HPX_OK;
+}
+
+hpx_status hpx_lmmse_inject_timeout(hpx_lmmse* lm, void* stream) {
+  if (!lm) return hpx_fail(HPX_ERR_ARG, "lmmse_inject_timeout: null argument");
+  if (!lm->d_tc_fail) return hpx_fail(HPX_ERR_UNSUPPORTED, "lmmse_inject_timeout: the handle has no tensor-core path");
+  HPX_CUDA(cudaMemsetAsync(lm->d_tc_fail, 0x01, 1, as_stream(stream)));  // the int word becomes 1
+  return HPX_OK;
 }
 
 hpx_status hpx_detect_ls(const hpx_ls* ls, int32_t mode, const hpx_cf32* grid, int32_t gcols, const float* nv,

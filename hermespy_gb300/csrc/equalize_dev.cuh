@@ -7,10 +7,15 @@
 
 // --------------------------------------------------------------- solvers
 
+// false for NaN and +-inf
+__device__ __forceinline__ bool finite_f(float v) { return fabsf(v) < __int_as_float(0x7f800000); }
+
 // Cholesky solve of the Hermitian positive definite A x = b (lower triangle of A
-// used and overwritten). Returns false if a pivot is not positive.
+// used and overwritten). Returns false if a pivot is not positive; `fin` turns
+// false if a pivot is not finite (NaN or inf inputs, as opposed to a singular but
+// finite system, whose NaN solution the reference produces too).
 template <int n>
-__device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], float2 (&x)[n]) {
+__device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], float2 (&x)[n], bool& fin) {
   bool ok = true;
   float inv[n];  // reciprocal pivots 1 / L[j][j]
 #pragma unroll
@@ -19,6 +24,7 @@ __device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], fl
 #pragma unroll
     for (int k = 0; k < j; ++k) d -= A[j][k].x * A[j][k].x + A[j][k].y * A[j][k].y;
     ok = ok && (d > 0.0f);
+    fin = fin && finite_f(d);
     inv[j] = rsqrtf(d);
 #pragma unroll
     for (int i = j + 1; i < n; ++i) {
@@ -50,11 +56,12 @@ __device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], fl
   return ok;
 }
 
-// Equalize one resource element. Returns the number of output streams
-// (1 for ZF with a single receive antenna, which divides by sum_tx h like the
-// reference, NTX otherwise).
+// Equalize one resource element: NTX outputs (ZF with a single receive antenna
+// divides by sum_tx h like the reference and returns one stream, the others zero).
+// Returns false if a pivot (or the ZF denominator) is not finite: the element's
+// inputs held NaN or inf, which the caller reports as HPX_DROP_NUMERIC.
 template <int NRX, int NTX>
-__device__ __forceinline__ void equalize_one(int mode, const float2 (&H)[NRX][NTX], const float2 (&y)[NRX], float s2,
+__device__ __forceinline__ bool equalize_one(int mode, const float2 (&H)[NRX][NTX], const float2 (&y)[NRX], float s2,
                                              float2 (&x)[NTX]) {
   if (mode == HPX_EQ_ZF && NRX == 1) {
     float2 hs = make_float2(0.f, 0.f);
@@ -65,8 +72,9 @@ __device__ __forceinline__ void equalize_one(int mode, const float2 (&H)[NRX][NT
     x[0] = make_float2((y[0].x * hs.x + y[0].y * hs.y) / den, (y[0].y * hs.x - y[0].x * hs.y) / den);
 #pragma unroll
     for (int t = 1; t < NTX; ++t) x[t] = make_float2(0.f, 0.f);
-    return;
+    return finite_f(den);
   }
+  bool fin = true;
   const float reg = mode == HPX_EQ_LMMSE ? s2 : 0.0f;
   if (mode == HPX_EQ_ZF && NRX < NTX) {
     // minimum-norm pseudo-inverse: x = H^H (H H^H)^-1 y
@@ -82,10 +90,10 @@ __device__ __forceinline__ void equalize_one(int mode, const float2 (&H)[NRX][NT
         A[i][j] = acc;
       }
     }
-    if (!chol_solve<NRX>(A, yy, w)) {
+    if (!chol_solve<NRX>(A, yy, w, fin)) {
 #pragma unroll
       for (int t = 0; t < NTX; ++t) x[t] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
-      return;
+      return fin;
     }
 #pragma unroll
     for (int t = 0; t < NTX; ++t) {
@@ -94,7 +102,7 @@ __device__ __forceinline__ void equalize_one(int mode, const float2 (&H)[NRX][NT
       for (int i = 0; i < NRX; ++i) cfmac(acc, H[i][t], w[i]);
       x[t] = acc;
     }
-    return;
+    return fin;
   }
   float2 A[NTX][NTX], b[NTX];
 #pragma unroll
@@ -113,9 +121,10 @@ __device__ __forceinline__ void equalize_one(int mode, const float2 (&H)[NRX][NT
     A[i][i].x += reg;
     A[i][i].y = 0.0f;
   }
-  if (!chol_solve<NTX>(A, b, x)) {
+  if (!chol_solve<NTX>(A, b, x, fin)) {
 #pragma unroll
     for (int t = 0; t < NTX; ++t) x[t] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
   }
+  return fin;
 }
 

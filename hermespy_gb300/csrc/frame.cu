@@ -52,6 +52,20 @@ int hpx_version(void) { return 10000; }
 
 const char* hpx_last_error(void) { return g_last_error.c_str(); }
 
+hpx_status hpx_drop_status(const uint32_t* errors, int64_t num_drops) {
+  if (num_drops < 0 || (num_drops > 0 && !errors)) return hpx_fail(HPX_ERR_ARG, "drop_status: bad arguments");
+  int64_t first_numeric = -1;
+  for (int64_t i = 0; i < num_drops; ++i) {
+    if (errors[i] & HPX_DROP_TIMEOUT)
+      return hpx_fail(HPX_ERR_TIMEOUT, "drop %lld: a bounded tensor-core wait ran out (result invalid)", (long long)i);
+    if ((errors[i] & HPX_DROP_NUMERIC) && first_numeric < 0) first_numeric = i;
+  }
+  if (first_numeric >= 0)
+    return hpx_fail(HPX_ERR_NUMERIC, "drop %lld: non-finite pivot in the equalizer (NaN or inf channel, samples or "
+                    "noise power)", (long long)first_numeric);
+  return HPX_OK;
+}
+
 hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out) {
   if (!desc || !out) return hpx_fail(HPX_ERR_ARG, "frame: null argument");
   *out = nullptr;

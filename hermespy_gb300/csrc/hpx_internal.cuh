@@ -14,6 +14,8 @@
 
 hpx_status hpx_fail(hpx_status code, const char* fmt, ...);
 hpx_status hpx_cuda_status(cudaError_t err, const char* what);
+// True if an LS table was built for a grid of this frame's layout (detect.cu).
+bool hpx_ls_matches_frame(const hpx_ls* ls, const hpx_frame* frame);
 
 #define HPX_TRY(expr)                      \
   do {                                     \

@@ -48,6 +48,8 @@ hpx_status hpx_link_create(const hpx_frame* frame, const hpx_fading* fading, con
   if (estimator == HPX_EST_LS && !ls) return hpx_fail(HPX_ERR_ARG, "link: LS estimation needs an hpx_ls table");
   if (estimator == HPX_EST_LS && (fading->nrx != 1 || fading->ntx != 1))
     return hpx_fail(HPX_ERR_UNSUPPORTED, "Least-Squares channel estimation is only implemented for SISO links");
+  if (estimator == HPX_EST_LS && !hpx_ls_matches_frame(ls, frame))
+    return hpx_fail(HPX_ERR_SHAPE, "link: the LS table was built for another frame layout");
   if (equalizer != HPX_EQ_ZF && equalizer != HPX_EQ_LMMSE) return hpx_fail(HPX_ERR_ARG, "link: unknown equalizer");
   if (max_drops < 1 || max_drops > 65535) return hpx_fail(HPX_ERR_ARG, "link: max_drops must be in [1, 65535]");
   hpx_link* l = new hpx_link();

@@ -12,9 +12,12 @@
 // every GPU that loads this library holds it until the process exits. Host code
 // cannot use the array's name as a device address, so the first call on each
 // device looks its address up with cudaGetSymbolAddress while that device is
-// current and caches it; make that first call before any stream capture. All
-// calls on a device share the array and each call overwrites what it uses, so
-// calls whose work overlaps on the GPU (different streams, or host threads
+// current and caches it. Under CUDA's lazy module loading that lookup is also when
+// the device reserves the 64 MiB, so a caller whose pool allocator takes the rest
+// of device memory makes this first call at start-up, before the pool grows (a call
+// with num_drops = 0 does the set-up and nothing else), and before any stream
+// capture. All calls on a device share the array and each call overwrites what it
+// uses, so calls whose work overlaps on the GPU (different streams, or host threads
 // without ordering) race and must be serialized by the caller.
 #include <mutex>
 
@@ -59,6 +62,9 @@ extern "C" hpx_status hpx_link_run_static(const hpx_frame* frame, const hpx_fadi
   if (equalizer == HPX_EQ_LMMSE && !noise_power) return hpx_fail(HPX_ERR_ARG, "link_run_static: LMMSE needs noise powers");
   if (ls && (fading->nrx != 1 || fading->ntx != 1))
     return hpx_fail(HPX_ERR_UNSUPPORTED, "Least-Squares channel estimation is only implemented for SISO links");
+  // the LS receiver lays the grid out by its table's frame: it must be this frame's
+  if (ls && !hpx_ls_matches_frame(ls, frame))
+    return hpx_fail(HPX_ERR_SHAPE, "link_run_static: the LS table was built for another frame layout");
   if (num_drops < 0 || drop0 < 0) return hpx_fail(HPX_ERR_ARG, "link_run_static: bad drop range");
   const size_t T = frame->info.samples_per_frame, D = fading->max_delay, C = frame->info.num_columns,
                W = frame->info.num_words;
@@ -75,9 +81,9 @@ extern "C" hpx_status hpx_link_run_static(const hpx_frame* frame, const hpx_fadi
                     "(at most about %zu drops of this link per call)",
                     num_drops, state_bytes + x_bytes + y_bytes + grid_bytes, kStaticScratchBytes,
                     per_drop ? kStaticScratchBytes / per_drop : (size_t)0);
-  if (num_drops == 0) return HPX_OK;
   void* base = nullptr;
-  HPX_TRY(scratch_address(&base));
+  HPX_TRY(scratch_address(&base));  // also the set-up call: num_drops = 0 stops after it
+  if (num_drops == 0) return HPX_OK;
   unsigned char* p = static_cast<unsigned char*>(base);
   void* state = p;
   hpx_cf32* x = reinterpret_cast<hpx_cf32*>(p + state_bytes);

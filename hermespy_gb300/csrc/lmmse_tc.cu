@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, con
   if (tid == 0) skip = *(volatile int*)fail;
   __syncthreads();
   if (skip) {  // an earlier CTA timed out on the tensor core: flag and leave
-    if (tid == 0) atomicOr(errors + b, 0x80000000u);
+    if (tid == 0) atomicOr(errors + b, HPX_DROP_TIMEOUT);
     return;
   }
   if (warp == 0) {
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, con
   const float s2 = nv ? nv[b] : 0.0f;
   const int c0 = mt * TC_M;
   const unsigned char* bop = reinterpret_cast<const unsigned char*>(v.bop) + (size_t)b * (v.nwl / TC_WORDS) * 2 * opbytes;
-  bool ok = true;
+  bool ok = true, fin = true;
   unsigned int local = 0;
   const uint32_t idesc = tc::idesc_f16_f32(TC_M, TC_N);
   const int npass = v.nwl / TC_WORDS;
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, con
 #pragma unroll
         for (int t = 0; t < 4; ++t) H[r][t] = make_float2(acc[r * 4 + t] * scl, acc[16 + r * 4 + t] * scl);
       }
-      equalize_one<4, 4>(mode, H, y, s2, x);
+      fin &= equalize_one<4, 4>(mode, H, y, s2, x);
       const int kf = v.kfirst[w * v.mtiles + mt];
       const int64_t pos = (int64_t)k * m - ((((int64_t)kf * m) >> 7) << 7);
 #pragma unroll
@@ -251,20 +251,19 @@ __global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, con
   // block error count
   for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
   __shared__ unsigned int wsum[TC_THREADS / 32];
-  __shared__ int okall;
-  if (tid == 0) okall = 1;
-  __syncthreads();
-  if (!ok) okall = 0;
   if (lane == 0) wsum[warp] = local;
-  __syncthreads();
+  const int okall = __syncthreads_and(ok);
+  const int any_bad = __syncthreads_or(!fin);
   if (tid == 0) {
     unsigned int tot = 0;
     for (int i = 0; i < TC_THREADS / 32; ++i) tot += wsum[i];
     if (!okall) {  // the tensor core never signalled completion
-      atomicOr(errors + b, 0x80000000u);
+      atomicOr(errors + b, HPX_DROP_TIMEOUT);
       atomicExch(fail, 1);
+    } else {
+      if (tot) atomicAdd(errors + b, tot);
+      if (any_bad) atomicOr(errors + b, HPX_DROP_NUMERIC);
     }
-    else if (tot) atomicAdd(errors + b, tot);
   }
 }
 

@@ -198,6 +198,7 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
   const int j8 = lane >> 3, r8 = lane & 7;
   const int half = lane >> 4, row = lane & 15;
   unsigned int local = 0, n64 = 0;
+  bool bad = false;  // an element of this thread had a non-finite pivot
 
   // received samples of the next element pair are loaded one iteration ahead
   constexpr int YR = (NRX + 31) / 32;
@@ -348,13 +349,14 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
     }
     float2 bi = bs[half * MT + row];
     float pmin = INFINITY, pmax = 0.f, inv_i = 0.f;
-    bool ok = true;
+    bool ok = true, fin = true;
     // right-looking Cholesky; column k of L goes through shared memory, every loop has
     // a fixed trip count so that a[] stays in registers
 #pragma unroll
     for (int k = 0; k < MT; ++k) {
       const float dkk = __shfl_sync(0xffffffffu, a[k].x, k, 16);
       ok = ok && (dkk > 0.f);
+      fin = fin && (fabsf(dkk) < INFINITY);  // NaN / inf inputs (fminf / fmaxf below drop NaN)
       const float ik = rsqrtf(fmaxf(dkk, 1e-30f));
       const float pk = dkk * ik;
       pmin = fminf(pmin, pk);
@@ -437,6 +439,7 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
       n64 += (row == 0 && mine) ? 1u : 0u;
     }
     if (valid) {
+      bad = bad || !fin;
       const int64_t k = k0 + jme;
       const uint32_t rx_v = qam_decide(qt, xi);
       const uint32_t tx_v = extract_bits_msb(bitsm + row * BW - wofs, k * m, m);
@@ -450,8 +453,10 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
     local += __shfl_down_sync(0xffffffffu, local, o);
     n64 += __shfl_down_sync(0xffffffffu, n64, o);
   }
+  const bool any_bad = __any_sync(0xffffffffu, bad);
   if (lane == 0) {
     if (local) atomicAdd(errors + b, local);
+    if (any_bad) atomicOr(errors + b, HPX_DROP_NUMERIC);
     if (n64 && fp64_count) atomicAdd(fp64_count + b, n64);
   }
 }

@@ -332,11 +332,13 @@ __device__ void u_propagate(const UDrop& d, const FadingConst& fc, int T, const 
   }
 }
 
-// Ideal CSI + equalization + demap + count of one element (k_detect_ideal).
+// Ideal CSI + equalization + demap + count of one element (k_detect_ideal); `fin`
+// turns false on a non-finite equalizer pivot.
 template <int NRX, int NTX>
 __device__ __forceinline__ unsigned int u_element(int mode, float2 g, const float2* Sm, const float2* grid, int W,
                                                   int C, int w, int c, float s2, const QamDemapTable& qt,
-                                                  const uint32_t* bitsm, int BW, int64_t wofs, int64_t k, int m) {
+                                                  const uint32_t* bitsm, int BW, int64_t wofs, int64_t k, int m,
+                                                  bool& fin) {
   const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
   float2 H[NRX][NTX], yv[NRX], xv[NTX];
 #pragma unroll
@@ -345,7 +347,7 @@ __device__ __forceinline__ unsigned int u_element(int mode, float2 g, const floa
 #pragma unroll
     for (int t = 0; t < NTX; ++t) H[r][t] = cmul(Sm[r * NTX + t], g);
   }
-  equalize_one<NRX, NTX>(mode, H, yv, s2, xv);
+  fin &= equalize_one<NRX, NTX>(mode, H, yv, s2, xv);
   unsigned int e = 0;
 #pragma unroll
   for (int t = 0; t < NTX; ++t) {
@@ -360,18 +362,20 @@ template <int NRX>
 __device__ __forceinline__ unsigned int u_element_tx(int ntx, int mode, float2 g, const float2* Sm,
                                                      const float2* grid, int W, int C, int w, int c, float s2,
                                                      const QamDemapTable& qt, const uint32_t* bitsm, int BW,
-                                                     int64_t wofs, int64_t k, int m) {
+                                                     int64_t wofs, int64_t k, int m, bool& fin) {
   switch (ntx) {
-    case 1: return u_element<NRX, 1>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m);
-    case 2: return u_element<NRX, 2>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m);
-    case 4: return u_element<NRX, 4>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m);
-    default: return u_element<NRX, 8>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m);
+    case 1: return u_element<NRX, 1>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
+    case 2: return u_element<NRX, 2>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
+    case 4: return u_element<NRX, 4>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
+    default: return u_element<NRX, 8>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
   }
 }
 
+// The thread's share of the drop's bit errors; `fin` turns false if one of its
+// elements had a non-finite equalizer pivot.
 __device__ unsigned int u_detect(const UDrop& d, const UFrame& fr, const FadingConst& fc, const int64_t* Wp,
                                  const int64_t* P0, const float2* Sm, const int* dl, const float2* grid, float s2,
-                                 const QamDemapTable& qt, uint64_t seed, int64_t drop, unsigned char* sm) {
+                                 const QamDemapTable& qt, uint64_t seed, int64_t drop, unsigned char* sm, bool& fin) {
   float2* hb = reinterpret_cast<float2*>(sm);
   float2* scratch = hb + d.L;
   uint32_t* bitsm = reinterpret_cast<uint32_t*>(scratch + d.L * fc.S1);
@@ -398,10 +402,10 @@ __device__ unsigned int u_detect(const UDrop& d, const UFrame& fr, const FadingC
       const float2 g = tap_response(fc, hb, dl, fr.twiddle, fr.bins[j], fr.N);
       const int64_t k = k0 + j;
       switch (d.nrx) {
-        case 1: local += u_element_tx<1>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m); break;
-        case 2: local += u_element_tx<2>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m); break;
-        case 4: local += u_element_tx<4>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m); break;
-        default: local += u_element_tx<8>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m); break;
+        case 1: local += u_element_tx<1>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
+        case 2: local += u_element_tx<2>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
+        case 4: local += u_element_tx<4>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
+        default: local += u_element_tx<8>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
       }
     }
     __syncthreads();
@@ -469,16 +473,17 @@ __global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __
       case 1024: u_rx<1024>(fr, d.nrx, fr.T + d.D, y, grid, work); break;
       default: u_rx<2048>(fr, d.nrx, fr.T + d.D, y, grid, work); break;
     }
-    const unsigned int e = u_detect(d, fr, fc, Wp, P0, Sm, dl, grid, np, qts.t[fr.m], a.seed, drop, work);
+    bool fin = true;
+    const unsigned int e = u_detect(d, fr, fc, Wp, P0, Sm, dl, grid, np, qts.t[fr.m], a.seed, drop, work, fin);
     // drop total
     unsigned int v = e;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = v;
-    __syncthreads();
+    const int any_bad = __syncthreads_or(!fin);
     if (threadIdx.x == 0) {
       unsigned int tot = 0;
       for (int i = 0; i < (int)(blockDim.x >> 5); ++i) tot += s_sum[i];
-      a.errors[b] = tot;
+      a.errors[b] = any_bad ? (tot | HPX_DROP_NUMERIC) : tot;
     }
     __syncthreads();
   }

@@ -227,6 +227,29 @@ class LinkEngine:
                   _lib.stream_ptr(stream))
         return errors
 
+    def status(self, clear: bool = True, stream: torch.cuda.Stream | None = None) -> None:
+        """Raise RuntimeError if a bounded tensor-core wait of the engine's kernels (the
+        LMMSE receiver, the learned estimator's network) ran out since the last check;
+        ``clear`` resets the handles' sticky status words. Synchronizes the stream."""
+
+        sp = _lib.stream_ptr(stream)
+        try:
+            if self._lmmse is not None:
+                _lib.call("hpx_lmmse_status", self._lmmse, int(clear), sp)
+        finally:
+            if self.model is not None:
+                self.model.status(clear, stream)
+
+    def counts(self, errors: torch.Tensor, stream: torch.cuda.Stream | None = None) -> np.ndarray:
+        """Host int64 bit-error counts of a ``run``'s per-drop words, after checking the
+        device status (``status``) and every drop's failure flags (``_lib.drop_counts``):
+        a drop whose wait ran out or whose equalizer met NaN / inf raises instead of being
+        counted."""
+
+        words = errors.cpu().numpy()
+        self.status(True, stream)
+        return _lib.drop_counts(words)
+
     def simulate(self, noise_power_host: np.ndarray, drop0: int = 0) -> np.ndarray:
         """Host noise powers in, host per-drop bit errors out (batched by max_drops)."""
 
@@ -235,7 +258,7 @@ class LinkEngine:
         for s in range(0, p.size, self.max_drops):
             chunk = torch.from_numpy(p[s:s + self.max_drops]).to(self.device, non_blocking=True)
             e = self.run(drop0 + s, chunk)
-            out[s:s + chunk.numel()] = e.cpu().numpy().astype(np.int64)
+            out[s:s + chunk.numel()] = self.counts(e)
         return out
 
     def ber_curve(self, levels_db, drops_per_level: int, drop0: int = 0) -> list[BerPoint]:

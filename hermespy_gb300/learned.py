@@ -103,6 +103,12 @@ class CnnChannelEstimator:
         _lib.call("hpx_cnn_refine", self.handle, _lib.ptr(csi), C, B, _lib.stream_ptr(stream))
         return csi
 
+    def status(self, clear: bool = True, stream: torch.cuda.Stream | None = None) -> None:
+        """Raise RuntimeError if a bounded TMA / tensor-core wait of ``refine`` ran out
+        since the last check (its estimates are then NaN); ``clear`` resets the word."""
+
+        _lib.call("hpx_cnn_status", self.handle, int(clear), _lib.stream_ptr(stream))
+
     def train_step(self, ls: torch.Tensor, truth: torch.Tensor, lr: float,
                    stream: torch.cuda.Stream | None = None) -> torch.Tensor:
         """One Adam step; returns the device scalar sum |out - truth|^2 (not synchronized)."""

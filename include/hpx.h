@@ -46,6 +46,26 @@ int hpx_version(void);
 /* Message of the last failed call on this thread ("" if none). */
 const char* hpx_last_error(void);
 
+/* ----------------------------------------------------------- device status
+ * Failures found on the device reach the caller in two ways, replacing the
+ * reference's per-sample exception path (core/pymonte/actors.py:444-452, where a
+ * failing drop raises into the actor and the campaign stops):
+ *   - per drop: the bit-error word of every detection entry point (hpx_link_run,
+ *     hpx_detect_*, hpx_uneven_run, ...) carries flag bits; a drop whose word has
+ *     one of them holds no valid count;
+ *   - per handle: handles whose kernels wait on the tensor cores or on TMA
+ *     (hpx_lmmse, hpx_cnn) keep a sticky status word that their entry points set
+ *     when a bounded wait runs out (~20 ms); later launches on the handle then skip
+ *     their work and flag their drops, until hpx_*_status clears the word. */
+#define HPX_DROP_TIMEOUT 0x80000000u /* a bounded tensor-core / TMA wait ran out */
+#define HPX_DROP_NUMERIC 0x40000000u /* a non-finite pivot in the drop's equalizer (NaN / inf input) */
+#define HPX_DROP_COUNT 0x3fffffffu   /* mask of the bit-error count */
+
+/* HPX_OK if no word of a HOST copy of per-drop error words carries a flag, else
+ * HPX_ERR_TIMEOUT or HPX_ERR_NUMERIC (timeouts first) with the first flagged
+ * drop's index in hpx_last_error(). */
+hpx_status hpx_drop_status(const uint32_t* errors, int64_t num_drops);
+
 /* ------------------------------------------------------------------ frames */
 
 /* Element types of the resource grid, as ElementType
@@ -267,6 +287,14 @@ hpx_status hpx_lmmse_estimate(const hpx_lmmse* lmmse, const hpx_cf32* grid, int3
  * memory -> per data element the channel, equalization (ZF / LMMSE), hard demap and
  * bit-error count -> errors[B]. Antenna pairs: 1x1, 2x1, 2x2, 4x1, 4x2, 4x4. The CSI
  * grid never reaches HBM. No counterpart in the reference. */
+/* Sticky device status of the handle: synchronizes `stream`, returns
+ * HPX_ERR_TIMEOUT if a bounded tensor-core wait of hpx_detect_lmmse ran out since
+ * the last clear (HPX_OK otherwise) and clears the word when `clear` != 0. */
+hpx_status hpx_lmmse_status(hpx_lmmse* lmmse, int32_t clear, void* stream);
+/* Host-side fault injection for tests of the error path: marks the handle as if a
+ * wait had run out (stream-ordered write of the status word; nothing faults on the
+ * device). Later hpx_detect_lmmse launches skip and flag every drop HPX_DROP_TIMEOUT. */
+hpx_status hpx_lmmse_inject_timeout(hpx_lmmse* lmmse, void* stream);
 hpx_status hpx_detect_lmmse(const hpx_lmmse* lmmse, int32_t num_rx, int32_t mode, const hpx_cf32* grid,
                             int32_t grid_columns, const float* noise_var, uint64_t seed, int64_t drop0,
                             int32_t num_drops, uint32_t* errors, void* stream);
@@ -333,6 +361,13 @@ hpx_status hpx_cnn_get_params(const hpx_cnn* cnn, float* params);
 hpx_status hpx_cnn_get_grads(const hpx_cnn* cnn, float* grads);
 /* In place: csi[B][16][num_words][csi_columns] (LS estimate) -> refined estimate. */
 hpx_status hpx_cnn_refine(const hpx_cnn* cnn, hpx_cf32* csi, int32_t csi_columns, int32_t batch, void* stream);
+/* Sticky device status of the network's tensor-core forward pass (as
+ * hpx_lmmse_status): HPX_ERR_TIMEOUT if a TMA or MMA wait ran out, in which case
+ * the refined estimates of that launch are NaN. */
+hpx_status hpx_cnn_status(hpx_cnn* cnn, int32_t clear, void* stream);
+/* Host-side fault injection (as hpx_lmmse_inject_timeout): later hpx_cnn_refine
+ * launches skip their tiles and write NaN estimates. */
+hpx_status hpx_cnn_inject_timeout(hpx_cnn* cnn, void* stream);
 /* One Adam step on ls/truth[B][16][num_words][num_columns] (B <= max_batch), loss =
  * sum |out - truth|^2 written to the device double `loss` (may be NULL). */
 hpx_status hpx_cnn_train_step(hpx_cnn* cnn, const hpx_cf32* ls, const hpx_cf32* truth, int32_t csi_columns,
@@ -443,10 +478,13 @@ hpx_status hpx_link_run(const hpx_link* link, uint64_t seed, int64_t drop0, int3
  * the library until the process exits; the largest batch is what fits in it
  * (about 50 drops of the 4x4, 1024-subcarrier link), larger batches fail with
  * HPX_ERR_ARG and a message giving the limit. `ls` selects LS estimation (SISO,
- * table built on the frame's columns); NULL selects ideal CSI. The first call on a
- * device looks up the array's device address and must come before any stream
- * capture. Calls share the array: calls that overlap on the GPU race. Never calls
- * cudaMalloc or cudaFree. */
+ * table built on this frame's layout, else HPX_ERR_SHAPE); NULL selects ideal CSI.
+ * The first call on a device looks up the array's device address; under CUDA's lazy
+ * module loading that is also when the device reserves the 64 MiB, so make it at
+ * start-up, before a pool allocator of the host takes the remaining device memory,
+ * and before any stream capture (a call with num_drops = 0 does this set-up and
+ * nothing else). Calls share the array: calls that overlap on the GPU race. Never
+ * calls cudaMalloc or cudaFree. */
 hpx_status hpx_link_run_static(const hpx_frame* frame, const hpx_fading* fading, const hpx_ls* ls,
                                int32_t equalizer, uint64_t seed, int64_t drop0, int32_t num_drops,
                                const float* noise_power, uint32_t* errors, void* stream);

@@ -28,7 +28,7 @@ import time
 
 import numpy as np
 
-from . import estimation, fading, mapping, ofdm, streams
+from . import cnn, estimation, fading, mapping, ofdm, streams
 from .frame import FrameLayout, FrameSpec
 
 
@@ -39,9 +39,10 @@ class LinkConfig:
     sampling_rate: float
     num_tx: int = 1
     num_rx: int = 1
-    estimator: str = "ls"        # "ls" | "ideal" | "lmmse" (tap-domain LMMSE, engine extension)
+    estimator: str = "ls"        # "ls" | "ideal" | "lmmse" (tap-domain LMMSE) | "learned" (LS + CNN)
     equalizer: str = "zf"        # "zf" | "lmmse"
     noise: str = "ebn0"          # "ebn0" | "snr"
+    cnn_params: np.ndarray | None = None  # parameter vector of the learned estimator
 
 
 def noise_power(cfg: LinkConfig, layout: FrameLayout, level_db: float) -> float:
@@ -87,10 +88,13 @@ def simulate_drop(cfg: LinkConfig, seed: int, drop: int, level_db: float, keep: 
     frame = y[:, :T]
     grids = np.stack([ofdm.demodulate(layout, frame[r]) for r in range(cfg.num_rx)])  # (Nrx, W, N)
     lap("receive")
-    if cfg.estimator == "ls":
+    if cfg.estimator in ("ls", "learned"):
         if (cfg.num_rx != 1 or cfg.num_tx != 1) and layout.spec.pilot_comb < max(cfg.num_tx, 2):
             raise NotImplementedError("Least-Squares channel estimation is only implemented for SISO links")
         H = estimation.mimo_ls_estimate(layout, grids, cfg.num_tx)
+        if cfg.estimator == "learned":
+            U = layout.num_used
+            H[..., :U] = cnn.refine(cfg.cnn_params, H[..., :U])
     elif cfg.estimator == "lmmse":
         H = estimation.tap_lmmse_estimate(layout, grids, cfg.channel, fs, p, cfg.num_tx)
     else:

@@ -1,6 +1,7 @@
 """Generate the golden fixtures of the HermesPy reference (run where its source is available).
 
-Usage:  python tests/golden/make_golden.py [path-to-hermespy-checkout] [fixture ...]
+Usage:  python tests/golden/make_golden.py <path-to-hermespy-checkout> [fixture ...]
+        (or with HERMESPY_REFERENCE=<path> set and the path argument omitted)
 
 With fixture names (``qam``, ``ofdm``, ``fading``, ``ls``, ``ideal``, ``zf``, ``ber``,
 ``drops``, ``presets``) only those are regenerated.
@@ -51,7 +52,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 import refimport  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else refimport.DEFAULT_REFERENCE
+REF = refimport.reference_path(sys.argv[1] if len(sys.argv) > 1 else None)
 ONLY = set(sys.argv[2:])
 refimport.import_reference(REF)
 
@@ -85,6 +86,7 @@ from hermespy.simulation import SimulatedUniformArray, SimulatedIdealAntenna  # 
 
 from oracle import fading as ofad  # noqa: E402
 from oracle import streams  # noqa: E402
+from refdrops import RefLink, c1_waveform, c2_waveform  # noqa: E402
 
 OUT = HERE
 
@@ -96,29 +98,6 @@ def save(name: str, **arrays) -> None:
 
 
 # ----------------------------------------------------------------------------- frames
-def c1_waveform(order: int = 16) -> OFDMWaveform:
-    """SISO 256-point frame: 200 used subcarriers, CP 18, 14 words, comb pilots
-    on every 4th subcarrier of words 0 and 7."""
-
-    N, U, CP = 256, 200, 18
-    res = [
-        GridResource(1, prefix_ratio=CP / N, elements=[GridElement(ElementType.DATA, U)]),
-        GridResource(U // 4, prefix_ratio=CP / N,
-                     elements=[GridElement(ElementType.REFERENCE, 1), GridElement(ElementType.DATA, 3)]),
-    ]
-    struct = [SymbolSection(1, [1, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0])]
-    return OFDMWaveform(grid_resources=res, grid_structure=struct, num_subcarriers=N, modulation_order=order)
-
-
-def c2_waveform(order: int = 64) -> OFDMWaveform:
-    """1024-point frame: 600 used data subcarriers, CP 72, 14 words."""
-
-    N, U, CP = 1024, 600, 72
-    res = [GridResource(1, prefix_ratio=CP / N, elements=[GridElement(ElementType.DATA, U)])]
-    struct = [SymbolSection(14, [0])]
-    return OFDMWaveform(grid_resources=res, grid_structure=struct, num_subcarriers=N, modulation_order=order)
-
-
 # ----------------------------------------------------------------------------- QAM
 def make_qam() -> None:
     rng = np.random.default_rng(7)
@@ -279,119 +258,26 @@ def make_ber() -> None:
 
 
 # ----------------------------------------------------------------------------- full drops
-class InjectedBits(BitsSource):
-    """Bits source returning the engine's Philox bits for the current drop."""
-
-    def __init__(self, seed, num_streams):
-        BitsSource.__init__(self)
-        self.seed, self.num_streams, self.drop = seed, num_streams, 0
-
-    def generate_bits(self, num_bits):
-        per = num_bits // self.num_streams
-        return np.concatenate([streams.data_bits(self.seed, self.drop, s, per) for s in range(self.num_streams)])
-
-    def serialize(self, process):
-        pass
-
-
-class InjectedNoise(AWGN):
-    """Noise model adding the engine's Philox AWGN for the current drop."""
-
-    def __init__(self, seed):
-        AWGN.__init__(self)
-        self.inj_seed, self.drop = seed, 0
-
-    def realize(self, power):
-        model = self
-
-        class _R(AWGNRealization):
-            def add_to(self, signal):
-                if self.power == 0.0:
-                    return signal
-                noisy = signal.copy()
-                arr = noisy.view(np.ndarray)
-                n = streams.awgn(model.inj_seed, model.drop, arr.shape[0], arr.shape[1], self.power)
-                for block in noisy.blocks:
-                    block += n
-                noisy.noise_power = self.power
-                return noisy
-
-        return _R(power, 0)
-
-
-def _drop_scenario(wf, cfg: ofad.FadingConfig, fs, num_tx, num_rx, seed, ideal):
-    sc = SimulationScenario(seed=3)
-    tx = sc.new_device(carrier_frequency=0.0, bandwidth=fs, oversampling_factor=1,
-                       antennas=SimulatedUniformArray(SimulatedIdealAntenna, 0.01, [num_tx, 1, 1]))
-    rx = sc.new_device(carrier_frequency=0.0, bandwidth=fs, oversampling_factor=1,
-                       antennas=SimulatedUniformArray(SimulatedIdealAntenna, 0.01, [num_rx, 1, 1]))
-    link = SimplexLink()
-    tx.transmitters.add(link)
-    rx.receivers.add(link)
-    ch = MultipathFadingChannel(cfg.delays, cfg.power_profile, cfg.rice_factors,
-                                num_sinusoids=cfg.num_sinusoids, doppler_frequency=cfg.doppler_frequency)
-    sc.set_channel(tx, rx, ch)
-    if ideal:
-        wf.channel_estimation = OFDMIdealChannelEstimation(ch, tx, rx)
-    else:
-        wf.channel_estimation = OrthogonalLeastSquaresChannelEstimation()
-    wf.channel_equalization = OrthogonalZeroForcingChannelEqualization()
-    link.waveform = wf
-    bits = InjectedBits(seed, num_tx)
-    link.bits_source = bits
-    noise = InjectedNoise(seed)
-    rx.noise_model = noise
-    tx.noise_model = InjectedNoise(seed + 1)
-    ber = BitErrorEvaluator(link, link)
-    return sc, ch, link, rx, bits, noise, ber
-
-
-def _inject_fading(ch, cfg, seed, drop, num_rx, num_tx):
-    """Route the engine's fading uniforms through the reference's own variables."""
-
-    L, S = cfg.num_taps, cfg.num_sinusoids
-    u = streams.fading_uniforms(seed, drop, cfg.num_draws(num_rx, num_tx))
-    ref_u = np.full(100 + 2 * L * (1 + S), 0.5)
-    # SimulationScenario.propagate (simulation/scenario.py:575-609) samples the link
-    # (device 1 -> device 0) and serves device 0 -> device 1 with its reciprocal, whose
-    # spatial response is the transpose: entry [rx, tx] comes from variable entry [tx, rx].
-    sp = np.full((10, 10), 0.5)
-    sp[:num_tx, :num_rx] = u[: num_rx * num_tx].reshape(num_rx, num_tx).T
-    ref_u[:100] = sp.reshape(-1)
-    ref_u[100:] = u[num_rx * num_tx:]
-    scalars = norm.ppf(ref_u)
-    gen = ch._MultipathFadingChannel__rng
-    gen.realize = lambda distance, *a, **k: StaticConsistentRealization(scalars)
-
-
 def make_drops() -> None:
     out = {}
     seed = 20240611
     fs = 15.36e6
     cfg = ofad.FadingConfig(np.arange(6) / fs, 10 ** (-0.3 * np.arange(6)), np.zeros(6), 20, 100.0)
     for i, (drop, ebn0_db) in enumerate(((0, 0.0), (1, 10.0), (2, 20.0))):
-        wf = c1_waveform()
-        sc, ch, link, rx, bits, noise, ber = _drop_scenario(wf, cfg, fs, 1, 1, seed, ideal=False)
-        rx.noise_level = EBN0(link, 10 ** (ebn0_db / 10))
-        bits.drop = noise.drop = drop
-        _inject_fading(ch, cfg, seed, drop, 1, 1)
-        dr = sc.drop()
-        e = ber.evaluate()
+        link = RefLink(c1_waveform(), cfg, fs, 1, 1, seed, "ls")
+        link.set_ebn0(ebn0_db)
+        errors, dr = link.drop(drop)
         out[f"c1_{i}_drop"], out[f"c1_{i}_ebn0_db"] = drop, ebn0_db
-        out[f"c1_{i}_errors"] = int(np.sum(e.evaluation))
+        out[f"c1_{i}_errors"] = errors
         out[f"c1_{i}_rx_bits"] = np.packbits(dr.device_receptions[1].operator_receptions[0].bits)
     # 2x2 ideal CSI + ZF on the 1024/600 frame with 23 taps
     fs2 = 30.72e6
     d, p, k, S, fd, flos, g, _, _, _, _ = FADING_CASES["c2"]
     cfg2 = ofad.FadingConfig(np.asarray(d, float) / fs2, p, k, S, fd, flos, g)
-    wf = c2_waveform(16)
-    sc, ch, link, rx, bits, noise, ber = _drop_scenario(wf, cfg2, fs2, 2, 2, seed, ideal=True)
-    rx.noise_level = EBN0(link, 10 ** (15 / 10))
-    bits.drop = noise.drop = 5
-    _inject_fading(ch, cfg2, seed, 5, 2, 2)
-    dr = sc.drop()
-    e = ber.evaluate()
-    out["c2_errors"] = int(np.sum(e.evaluation))
+    link = RefLink(c2_waveform(16), cfg2, fs2, 2, 2, seed, "ideal")
+    link.set_ebn0(15.0)
+    errors, dr = link.drop(5)
+    out["c2_errors"] = errors
     out["c2_rx_bits"] = np.packbits(dr.device_receptions[1].operator_receptions[0].bits)
     out["seed"] = seed
     save("drops.npz", **out)

@@ -20,7 +20,17 @@ from unittest.mock import MagicMock
 
 import numpy as np
 
-DEFAULT_REFERENCE = os.environ.get("HERMESPY_REFERENCE", "/root/reference")
+ENV = "HERMESPY_REFERENCE"
+
+
+def reference_path(path: str | None = None) -> str:
+    """The checkout to import: ``path`` if given, else the ``HERMESPY_REFERENCE``
+    environment variable; raises with a usage hint when neither is set."""
+
+    path = path or os.environ.get(ENV)
+    if not path:
+        raise SystemExit(f"no HermesPy checkout given: pass its path or set {ENV}=<path to the source tree>")
+    return path
 
 
 class _DenseSparse(np.ndarray):
@@ -112,9 +122,12 @@ class _MockFinder:
         return None
 
 
-def import_reference(path: str = DEFAULT_REFERENCE):
-    """Return the ``hermespy`` package from ``path`` (raises ImportError if absent)."""
+def import_reference(path: str | None = None):
+    """Return the ``hermespy`` package from ``path`` (or ``$HERMESPY_REFERENCE``;
+    raises ImportError if the checkout is absent)."""
 
+    path = reference_path(path)
+    os.environ[ENV] = path  # worker processes of the fixture generators import the same checkout
     if not os.path.isdir(os.path.join(path, "hermespy")):
         raise ImportError(f"HermesPy reference not found under {path}")
     _install_stubs()

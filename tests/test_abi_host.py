@@ -148,3 +148,18 @@ def test_clopper_pearson():
     assert lo == 0.0 and hi == pytest.approx(0.0362, abs=1e-3)
     lo, hi = clopper_pearson(50, 100)
     assert lo == pytest.approx(0.3983, abs=1e-3) and hi == pytest.approx(0.6017, abs=1e-3)
+
+
+def test_drop_status_flags_without_device():
+    """Per-drop failure flags of a host copy of error words raise instead of being counted."""
+
+    assert _lib.drop_counts(np.array([0, 7, 123456], dtype=np.uint32)).tolist() == [0, 7, 123456]
+    with pytest.raises(RuntimeError, match="drop 2: non-finite pivot"):
+        _lib.drop_counts(np.array([0, 5, _lib.DROP_NUMERIC | 3], dtype=np.uint32))
+    with pytest.raises(RuntimeError, match="drop 1: a bounded tensor-core wait ran out"):
+        _lib.drop_counts(np.array([_lib.DROP_NUMERIC, _lib.DROP_TIMEOUT], dtype=np.uint32))
+    # int32 views of the device words (torch has no uint32 arithmetic) carry the same flags
+    with pytest.raises(RuntimeError, match="wait ran out"):
+        _lib.drop_counts(np.array([-2147483648], dtype=np.int32))
+    with pytest.raises(ValueError):
+        _lib.check(_lib.load().hpx_drop_status(None, 3))

@@ -58,3 +58,35 @@ def test_tap_lmmse_beats_ls():
     n_lm = estimation.nmse_db(res["lmmse"]["H"], H, lay.data_mask)
     assert n_lm < n_ls - 5.0
     assert res["ideal"]["errors"] <= res["lmmse"]["errors"] < res["ls"]["errors"]
+
+
+def test_cnn_oracle_matches_torch_conv():
+    """The oracle's CNN (im2col over (word, column), taps 3 dy + dx, BF16 rounding
+    points) equals the same network written with torch's float64 conv2d."""
+
+    import torch
+
+    from oracle import cnn
+
+    rng = np.random.default_rng(5)
+    params = rng.normal(0, 0.05, cnn.LAYERS * 32 * 9 * 32 + cnn.LAYERS * 32).astype(np.float32)
+    ls = rng.normal(size=(4, 4, 5, 37)) + 1j * rng.normal(size=(4, 4, 5, 37))
+    out = cnn.refine(params, ls)
+    w, b = cnn.split(params)
+    z = ls.reshape(16, 5, 37)
+    s = np.sqrt(np.mean(np.abs(z) ** 2))
+    x = np.empty((32, 5, 37))
+    x[0::2], x[1::2] = z.real, z.imag
+    h = torch.from_numpy(cnn.bf16(x / s).astype(np.float64))[None]
+    for layer in range(cnn.LAYERS):
+        # [out][tap][in] with tap = 3 dy + dx -> conv2d's [out][in][dy][dx]
+        wt = torch.from_numpy(w[layer].reshape(32, 3, 3, 32).transpose(0, 3, 1, 2).copy())
+        h = torch.nn.functional.conv2d(h, wt, torch.from_numpy(b[layer]), padding=1)
+        if layer < cnn.LAYERS - 1:
+            h = torch.from_numpy(cnn.bf16(torch.relu(h).numpy()).astype(np.float64))
+    d = h[0].numpy() * s
+    ref = (z + d[0::2] + 1j * d[1::2]).reshape(ls.shape)
+    assert np.max(np.abs(out - ref)) < 1e-9
+    # the round trip through bf16 is round-to-nearest-even
+    v = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, -2.5e-3], dtype=np.float32)
+    assert cnn.bf16(v).tolist() == [1.0, 1.0, 1.0 + 2 ** -6, np.float32(-0.0025024414)]

@@ -91,3 +91,27 @@ def test_ill_conditioned_elements_take_fp64():
         rx_ref = np.stack([mapping.detect_bits(lay.order, xr[s]) for s in range(16)])
         ref = int(np.sum(tx != rx_ref))
         assert int(errs[d]) <= 1.2 * ref + 20, (int(errs[d]), ref)
+
+
+def test_config4_full_frame_matches_fp64():
+    """Config 4 at its own size: 64 x 16, 4096-point FFT with 3300 used subcarriers,
+    CP 288, 14 words, 16-QAM, 8 taps, rho = 0.7, 61.44 MHz; four drops at 15 dB against
+    a float64 solve of the same systems (relative RMS of the equalized symbols)."""
+
+    lay = FrameLayout(massive_frame())
+    fs = 61.44e6
+    cfg = massive_channel(64, 0.7, fs)
+    level = 10 ** (-1.5)
+    nd = 4
+    grid, errs, n64, xe = _run(lay, cfg, 64, fs, _lib.EQ_LMMSE, level, nd=nd)
+    worst = 0.0
+    for d in range(nd):
+        xr = _oracle_x(lay, cfg, 64, fs, grid, d, _lib.EQ_LMMSE, level)
+        worst = max(worst, rel_rms(xe[d], xr))
+        tx = np.stack([streams.data_bits(SEED, d, s, lay.bits_per_frame()) for s in range(16)])
+        rx = np.stack([mapping.detect_bits(lay.order, xe[d, s].astype(np.complex128)) for s in range(16)])
+        assert int(np.sum(tx != rx)) == int(errs[d])
+        rx_ref = np.stack([mapping.detect_bits(lay.order, xr[s]) for s in range(16)])
+        ref = int(np.sum(tx != rx_ref))
+        assert abs(int(errs[d]) - ref) <= max(3, 0.01 * ref), (d, int(errs[d]), ref)
+    assert worst < 1e-4, worst

@@ -1,5 +1,6 @@
 """GPU: the uneven batch (one persistent launch over drops of different shapes)
-against the homogeneous engine drop by drop, and its CUDA-graph replay."""
+against the homogeneous engine drop by drop (equal counts), and its CUDA-graph
+replay. The comparison with the oracle's drops is in test_gpu_ber_curves.py."""
 
 import numpy as np
 import pytest
@@ -13,7 +14,7 @@ SEED = 7171
 SCS, TAP = 30e3, 50e-9
 
 
-def _homogeneous_errors(d: DropConfig, drop: int, noise_power: float) -> int:
+def _homogeneous_errors(d: DropConfig, drop: int, noise_power: float, seed: int = SEED) -> int:
     N = d.fft_size
     C, cp = int(np.floor(0.586 * N)), N * 72 // 1024
     wf = hg.OFDMWaveform([hg.GridResource(1, prefix_ratio=cp / N, elements=[hg.GridElement(hg.ElementType.DATA, C)])],
@@ -21,7 +22,7 @@ def _homogeneous_errors(d: DropConfig, drop: int, noise_power: float) -> int:
     k = np.arange(d.num_taps)
     ch = hg.MultipathFadingChannel(list(k * TAP), list(d.power_profile()), [0.0] * d.num_taps, num_sinusoids=20,
                                    doppler_frequency=d.doppler_frequency)
-    eng = hg.LinkEngine(wf, ch, d.num_tx, d.num_rx, N * SCS, "ideal", "lmmse", "snr", max_drops=1, seed=SEED)
+    eng = hg.LinkEngine(wf, ch, d.num_tx, d.num_rx, N * SCS, "ideal", "lmmse", "snr", max_drops=1, seed=seed)
     p = torch.tensor([noise_power], dtype=torch.float32, device="cuda")
     return int(eng.run(drop, p).cpu()[0])
 
@@ -39,8 +40,10 @@ def test_uneven_drops_equal_homogeneous_engine():
     errs = batch.run(SEED, 100).cpu().numpy()
     p = batch.noise_power.cpu().numpy()
     for i, d in enumerate(drops):
+        # the persistent kernel runs the homogeneous kernels' arithmetic (same FMA order,
+        # noise streams and solver): the counts are equal, not merely close
         ref = _homogeneous_errors(d, 100 + i, float(p[i]))
-        assert abs(int(errs[i]) - ref) <= max(2, ref // 500), (i, d, int(errs[i]), ref)
+        assert int(errs[i]) == ref, (i, d, int(errs[i]), ref)
     # the 8x8 drop at 25 dB and the 1x1 drop at 5 dB are neither error-free nor all wrong
     assert 0 < errs[0] < batch.bits[0] // 2 and 0 < errs[1] < batch.bits[1] // 2
 

@@ -1,5 +1,7 @@
 """The oracle against outputs recorded from the HermesPy reference (tests/golden/*.npz)."""
 
+import os
+
 import numpy as np
 import pytest
 
@@ -7,6 +9,8 @@ from oracle import estimation, fading, mapping, ofdm, streams
 from oracle.frame import FrameLayout
 from oracle.link import LinkConfig, simulate_drop
 from tests.configs import fading_case, mimo_channel, mimo_frame, siso_channel, siso_frame
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 @pytest.mark.parametrize("order", [2, 4, 16, 64, 256])
@@ -154,3 +158,42 @@ def test_stream_statistics():
     assert abs(np.var(n.real) - 1) < 0.02 and abs(np.var(n.imag) - 1) < 0.02
     u = streams.fading_uniforms(1, 2, 100_000)
     assert 0 < u.min() and u.max() < 1 and abs(u.mean() - 0.5) < 0.005
+
+
+def test_ber_fixtures_reference_equals_oracle(golden):
+    """The oracle's drops reproduce the reference's own SimulationScenario.drop() bit
+    errors exactly on every fixture drop (11 000 SISO LS + ZF drops over Eb/N0 0..20 dB,
+    256 4x4 ideal-CSI + ZF drops over SNR U[0, 30] dB), at the same noise powers."""
+
+    z = golden("ber_siso.npz")
+    assert z["ref_errors"].size == 11 * 1000
+    assert np.array_equal(z["ref_errors"], z["oracle_errors"])
+    assert np.array_equal(z["ref_noise_power"], z["oracle_noise_power"])
+    m = golden("ber_mimo.npz")
+    assert m["ref_zf_errors"].size == 256
+    assert np.array_equal(m["ref_zf_errors"], m["oracle_zf_errors"])
+    assert np.allclose(m["ref_noise_power"], m["oracle_noise_power"], rtol=1e-14, atol=0)
+    # LMMSE detection beats ZF on the same drops (what the engine's LMMSE path adds)
+    assert m["oracle_lmmse_errors"].astype(np.int64).sum() < m["oracle_zf_errors"].astype(np.int64).sum()
+
+
+def test_ber_fixtures_match_their_inputs(golden):
+    """Fixture bookkeeping: the shipped CNN weights are the ones the learned-path
+    fixture was made with, and the uneven fixture's noise powers are the engine's."""
+
+    import hashlib
+
+    from hermespy_gb300.uneven import DropConfig
+
+    p = golden("ber_pilot.npz")
+    with open(os.path.join(ROOT, "hermespy_gb300", "weights", "cnn_4x4_1024.npz"), "rb") as f:
+        assert hashlib.sha256(f.read()).hexdigest() == str(p["weights_sha256"])
+    n = 512 * 172800
+    ber = {k: p[f"{k}_errors"].astype(np.int64).sum() / n for k in ("lmmse", "ls", "learned")}
+    assert ber["lmmse"] < ber["learned"] < ber["ls"]
+    u = golden("uneven.npz")
+    fields = ("num_rx", "num_tx", "fft_size", "num_words", "modulation_order", "num_taps", "tap_decay_db",
+              "doppler_frequency", "snr_db")
+    for i in range(u["errors"].size):
+        d = DropConfig(*[u[f][i].item() for f in fields])
+        assert abs(d.noise_power() / u["noise_power"][i] - 1) < 1e-12

@@ -67,9 +67,35 @@ def test_static_scratch_matches_link_run(case):
     # two calls in a row: the shared array keeps the first call's contents, which
     # the second call must not depend on
     first = _run_static(eng, 1000, powers, eng._ls)
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
     second = _run_static(eng, 1000, powers, eng._ls)
+    free_after, _ = torch.cuda.mem_get_info()
     np.testing.assert_array_equal(first, reference)
     np.testing.assert_array_equal(second, reference)
+    # the call the entry point exists for: no device memory taken or given back
+    assert free_after == free_before, (free_before, free_after)
+
+
+def test_static_setup_call_and_foreign_ls_table():
+    """A zero-drop call performs the per-device set-up only (callers make it at
+    start-up); an LS table of another frame layout is refused before any launch."""
+
+    siso, _ = _waveforms()
+    fs = 15.36e6
+    eng = hg.LinkEngine(siso, _channel(siso_channel(fs)), 1, 1, fs, "ls", "zf", "ebn0", max_drops=2, seed=SEED)
+    errors = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.call("hpx_link_run_static", eng._frame, eng._fading.handle, eng._ls, _lib.EQ_ZF, SEED, 0, 0, None,
+              _lib.ptr(errors), _lib.stream_ptr())
+    other = hg.OFDMWaveform(
+        [hg.GridResource(1, prefix_ratio=18 / 256, elements=[hg.GridElement(hg.ElementType.DATA, 200)]),
+         hg.GridResource(50, prefix_ratio=18 / 256, elements=[hg.GridElement(hg.ElementType.REFERENCE, 1),
+                                                              hg.GridElement(hg.ElementType.DATA, 3)])],
+        [hg.SymbolSection(1, [1, 0, 0, 0, 0, 0, 0, 1, 0, 0])], num_subcarriers=256, modulation_order=16)
+    powers = torch.ones(1, dtype=torch.float32, device="cuda")
+    with pytest.raises(ValueError, match="another frame layout"):
+        _lib.call("hpx_link_run_static", other._frame(), eng._fading.handle, eng._ls, _lib.EQ_ZF, SEED, 0, 1,
+                  _lib.ptr(powers), _lib.ptr(errors), _lib.stream_ptr())
 
 
 def test_static_scratch_rejects_oversized_batches():
