@@ -160,6 +160,9 @@ _SIGNATURES = {
     "hpx_detect_csi": [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int32, c_void_p, c_int32, c_void_p, c_uint64,
                        c_int64, c_int32, c_void_p, c_void_p],
     "hpx_drop_status": [c_void_p, c_int64],
+    "hpx_campaign_assign": [c_void_p, c_int32, c_void_p, c_void_p],
+    "hpx_campaign_accumulate": [c_void_p, c_int32, c_void_p, c_void_p],
+    "hpx_campaign_poll": [c_void_p, ctypes.POINTER(c_int32), c_void_p],
     "hpx_lmmse_status": [c_void_p, c_int32, c_void_p],
     "hpx_lmmse_inject_timeout": [c_void_p, c_void_p],
     "hpx_cnn_status": [c_void_p, c_int32, c_void_p],

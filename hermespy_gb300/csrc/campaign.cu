@@ -177,6 +177,46 @@ hpx_status hpx_campaign_reset(hpx_campaign* c) {
   return HPX_OK;
 }
 
+hpx_status hpx_campaign_assign(hpx_campaign* c, int32_t batch, float* noise_power, void* stream) {
+  if (!c || !noise_power) return hpx_fail(HPX_ERR_ARG, "campaign_assign: null argument");
+  if (batch < 1 || batch > c->max_batch) return hpx_fail(HPX_ERR_ARG, "campaign_assign: batch must be in [1, %d]", c->max_batch);
+  k_assign<<<1, 256, sizeof(int) * c->L, as_stream(stream)>>>(c->L, batch, c->d_power, c->d_confident, c->d_count,
+                                                               (unsigned long long)c->max_drops, noise_power,
+                                                               c->d_level);
+  HPX_LAUNCHED("campaign assign");
+  return HPX_OK;
+}
+
+hpx_status hpx_campaign_accumulate(hpx_campaign* c, int32_t batch, const uint32_t* errors, void* stream) {
+  if (!c || !errors) return hpx_fail(HPX_ERR_ARG, "campaign_accumulate: null argument");
+  if (batch < 1 || batch > c->max_batch)
+    return hpx_fail(HPX_ERR_ARG, "campaign_accumulate: batch must be in [1, %d]", c->max_batch);
+  cudaStream_t s = as_stream(stream);
+  k_accumulate<<<(batch + 255) / 256, 256, 0, s>>>(batch, c->d_level, errors, 1.0 / c->bits_per_drop, c->d_sum, c->d_sq,
+                                                   c->d_count, c->d_errors, c->d_flags);
+  HPX_LAUNCHED("campaign accumulate");
+  k_confidence<<<1, 256, 0, s>>>(c->L, c->min_samples, c->accuracy, c->confidence, (unsigned long long)c->max_drops,
+                                 c->d_sum, c->d_sq, c->d_count, c->d_confident, c->d_active);
+  HPX_LAUNCHED("campaign confidence");
+  return HPX_OK;
+}
+
+hpx_status hpx_campaign_poll(hpx_campaign* c, int32_t* levels_active, void* stream) {
+  if (!c || !levels_active) return hpx_fail(HPX_ERR_ARG, "campaign_poll: null argument");
+  cudaStream_t s = as_stream(stream);
+  int active = 0;
+  unsigned int flags = 0;
+  HPX_CUDA(cudaMemcpyAsync(&active, c->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HPX_CUDA(cudaMemcpyAsync(&flags, c->d_flags, sizeof(flags), cudaMemcpyDeviceToHost, s));
+  HPX_CUDA(cudaStreamSynchronize(s));
+  *levels_active = active;
+  if (flags & HPX_DROP_TIMEOUT)
+    return hpx_fail(HPX_ERR_TIMEOUT, "campaign: a drop's tensor-core wait ran out (left out of the sums)");
+  if (flags)
+    return hpx_fail(HPX_ERR_NUMERIC, "campaign: a drop's equalizer met a non-finite pivot (left out of the sums)");
+  return HPX_OK;
+}
+
 hpx_status hpx_campaign_run(hpx_campaign* c, hpx_link* link, uint64_t seed, int64_t drop0, int32_t batch,
                             int32_t max_batches, int32_t check_every, int64_t* drops_run, int32_t* levels_active,
                             void* stream) {

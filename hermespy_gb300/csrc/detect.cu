@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_ideal
   const float s2 = nv ? nv[b] : 0.0f;
   const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
   unsigned int local = 0;
-  bool fin = true;
+  bool fin = finite_f(s2);  // a NaN / inf noise power is an invalid drop too
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
     const int64_t k = k0 + j;
     const int c = data_column[k];
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(csi_max_threads<NRX, NTX>(), csi_small<NRX, NT
   const float2* hb = csi + (int64_t)b * NRX * NTX * hplane + (int64_t)w * ccols;
   const float2* yb = grid + (int64_t)b * NRX * W * gcols + (int64_t)w * gcols;
   unsigned int local = 0;
-  bool fin = true;
+  bool fin = finite_f(s2);  // a NaN / inf noise power is an invalid drop too
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
     const int64_t k = k0 + j;
     const int c = data_column[k];
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(LMMSE_THREADS, 2) k_detect_lmmse(LmmseView e, 
   lmmse_drop_taps<NP>(e, b, NRX, grid, gcols, s2, gt, gls, cw, ds);  // ends with __syncthreads
   const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
   unsigned int local = 0;
-  bool fin = true;
+  bool fin = finite_f(s2);  // a NaN / inf noise power is an invalid drop too
   for (int k = threadIdx.x; k < num_data; k += blockDim.x) {
     const int c = data_column[k], w = data_word[k];
     float2 hp[NP];
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
   const float s2 = nv ? nv[b] : 0.0f;
   const float2* gb = grid + (int64_t)b * W * gcols;
   unsigned int local = 0;
-  bool fin = true;
+  bool fin = finite_f(s2);  // a NaN / inf noise power is an invalid drop too
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
     const int64_t k = k0 + j;
     const int c = data_column[k];

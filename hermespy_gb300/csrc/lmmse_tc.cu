@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, con
   const float s2 = nv ? nv[b] : 0.0f;
   const int c0 = mt * TC_M;
   const unsigned char* bop = reinterpret_cast<const unsigned char*>(v.bop) + (size_t)b * (v.nwl / TC_WORDS) * 2 * opbytes;
-  bool ok = true, fin = true;
+  bool ok = true, fin = finite_f(s2);  // a NaN / inf noise power is an invalid drop too
   unsigned int local = 0;
   const uint32_t idesc = tc::idesc_f16_f32(TC_M, TC_N);
   const int npass = v.nwl / TC_WORDS;

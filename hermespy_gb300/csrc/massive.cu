@@ -198,7 +198,9 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
   const int j8 = lane >> 3, r8 = lane & 7;
   const int half = lane >> 4, row = lane & 15;
   unsigned int local = 0, n64 = 0;
-  bool bad = false;  // an element of this thread had a non-finite pivot
+  // a NaN / inf noise power, or an element whose solution (after the FP64 re-solve of
+  // ill-conditioned elements) is not finite
+  bool bad = !(fabsf(s2) < INFINITY);
 
   // received samples of the next element pair are loaded one iteration ahead
   constexpr int YR = (NRX + 31) / 32;
@@ -349,14 +351,13 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
     }
     float2 bi = bs[half * MT + row];
     float pmin = INFINITY, pmax = 0.f, inv_i = 0.f;
-    bool ok = true, fin = true;
+    bool ok = true;
     // right-looking Cholesky; column k of L goes through shared memory, every loop has
     // a fixed trip count so that a[] stays in registers
 #pragma unroll
     for (int k = 0; k < MT; ++k) {
       const float dkk = __shfl_sync(0xffffffffu, a[k].x, k, 16);
       ok = ok && (dkk > 0.f);
-      fin = fin && (fabsf(dkk) < INFINITY);  // NaN / inf inputs (fminf / fmaxf below drop NaN)
       const float ik = rsqrtf(fmaxf(dkk, 1e-30f));
       const float pk = dkk * ik;
       pmin = fminf(pmin, pk);
@@ -439,7 +440,7 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
       n64 += (row == 0 && mine) ? 1u : 0u;
     }
     if (valid) {
-      bad = bad || !fin;
+      bad = bad || !(fabsf(xi.x) < INFINITY && fabsf(xi.y) < INFINITY);
       const int64_t k = k0 + jme;
       const uint32_t rx_v = qam_decide(qt, xi);
       const uint32_t tx_v = extract_bits_msb(bitsm + row * BW - wofs, k * m, m);

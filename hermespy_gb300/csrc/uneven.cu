@@ -473,7 +473,7 @@ __global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __
       case 1024: u_rx<1024>(fr, d.nrx, fr.T + d.D, y, grid, work); break;
       default: u_rx<2048>(fr, d.nrx, fr.T + d.D, y, grid, work); break;
     }
-    bool fin = true;
+    bool fin = finite_f(np);  // a NaN / inf noise power is an invalid drop too
     const unsigned int e = u_detect(d, fr, fc, Wp, P0, Sm, dl, grid, np, qts.t[fr.m], a.seed, drop, work, fin);
     // drop total
     unsigned int v = e;

@@ -278,10 +278,14 @@ class LinkEngine:
         confidence stopping rule (``ScalarEvaluationResult.add_artifact``,
         core/pymonte/scalar.py:101-125, on the per-drop BER): every level runs until
         2 (1 - Phi(sqrt(n) accuracy / std)) < confidence or it holds
-        ``max_drops_per_level`` drops. The fused (ideal CSI, SISO LS) engines only."""
+        ``max_drops_per_level`` drops. The fused engines (ideal CSI, SISO LS) run the
+        whole loop in ``hpx_campaign_run``; the staged estimators (tap-domain LMMSE,
+        per-stream LS, the learned estimator) enqueue ``hpx_campaign_assign``, their
+        ``run`` and ``hpx_campaign_accumulate`` per batch, with the host reading the
+        number of active levels (``hpx_campaign_poll``) every ``check_every`` batches.
+        A drop whose device wait ran out or whose equalizer met NaN / inf stops the
+        campaign with RuntimeError."""
 
-        if self._link is None:
-            raise NotImplementedError("the campaign loop drives the fused drop pipeline (ideal CSI or SISO LS)")
         levels_db = [float(v) for v in levels_db]
         batch = min(self.max_drops, batch or self.max_drops)
         power = np.ascontiguousarray(self.noise_power(levels_db).astype(np.float32))
@@ -291,20 +295,36 @@ class LinkEngine:
                                                    int(max_drops_per_level), batch, float(self.bits_per_drop),
                                                    ctypes.byref(h)))
         try:
-            done = ctypes.c_int64()
-            active = ctypes.c_int32()
-            _lib.call("hpx_campaign_run", h, self.link_handle, self.seed, int(drop0), batch, int(max_batches),
-                      int(check_every), ctypes.byref(done), ctypes.byref(active), _lib.stream_ptr())
+            active = ctypes.c_int32(len(levels_db))
+            sp = _lib.stream_ptr()
+            if self._link is not None:
+                done = ctypes.c_int64()
+                _lib.call("hpx_campaign_run", h, self.link_handle, self.seed, int(drop0), batch, int(max_batches),
+                          int(check_every), ctypes.byref(done), ctypes.byref(active), sp)
+            else:
+                noise = torch.empty(batch, dtype=torch.float32, device=self.device)
+                errors = torch.empty(batch, dtype=torch.int32, device=self.device)
+                done = 0
+                for b in range(int(max_batches)):
+                    _lib.call("hpx_campaign_assign", h, batch, _lib.ptr(noise), sp)
+                    self.run(int(drop0) + done, noise, errors)
+                    _lib.call("hpx_campaign_accumulate", h, batch, _lib.ptr(errors), sp)
+                    done += batch
+                    if (b + 1) % int(check_every) == 0 or b + 1 == int(max_batches):
+                        self.status()
+                        _lib.call("hpx_campaign_poll", h, ctypes.byref(active), sp)
+                        if active.value == 0:
+                            break
             L = len(levels_db)
             drops = np.zeros(L, dtype=np.int64)
-            errors = np.zeros(L, dtype=np.int64)
+            errs = np.zeros(L, dtype=np.int64)
             conf = np.zeros(L, dtype=np.int32)
             _lib.call("hpx_campaign_results", h, drops.ctypes.data_as(ctypes.c_void_p),
-                      errors.ctypes.data_as(ctypes.c_void_p), None, None, conf.ctypes.data_as(ctypes.c_void_p))
+                      errs.ctypes.data_as(ctypes.c_void_p), None, None, conf.ctypes.data_as(ctypes.c_void_p))
         finally:
             _lib.load().hpx_campaign_destroy(h)
         return [BerPoint(lv, int(e), int(d) * self.bits_per_drop, int(d), bool(c))
-                for lv, e, d, c in zip(levels_db, errors, drops, conf)]
+                for lv, e, d, c in zip(levels_db, errs, drops, conf)]
 
     @property
     def link_handle(self):

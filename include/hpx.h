@@ -58,7 +58,7 @@ const char* hpx_last_error(void);
  *     when a bounded wait runs out (~20 ms); later launches on the handle then skip
  *     their work and flag their drops, until hpx_*_status clears the word. */
 #define HPX_DROP_TIMEOUT 0x80000000u /* a bounded tensor-core / TMA wait ran out */
-#define HPX_DROP_NUMERIC 0x40000000u /* a non-finite pivot in the drop's equalizer (NaN / inf input) */
+#define HPX_DROP_NUMERIC 0x40000000u /* NaN / inf noise power, or a non-finite equalizer pivot */
 #define HPX_DROP_COUNT 0x3fffffffu   /* mask of the bit-error count */
 
 /* HPX_OK if no word of a HOST copy of per-drop error words carries a flag, else
@@ -555,6 +555,18 @@ hpx_status hpx_campaign_reset(hpx_campaign* campaign);
 hpx_status hpx_campaign_run(hpx_campaign* campaign, hpx_link* link, uint64_t seed, int64_t drop0, int32_t batch,
                             int32_t max_batches, int32_t check_every, int64_t* drops_run,
                             int32_t* levels_active, void* stream);
+/* The same loop for drop pipelines other than hpx_link_run (the staged MIMO
+ * estimators: tap-domain LMMSE, per-stream LS, the learned estimator): per batch
+ * the host enqueues hpx_campaign_assign (the noise power of each of the batch's
+ * drops, dealt round-robin to the active levels, into noise_power[batch]), its own
+ * pipeline on those powers, and hpx_campaign_accumulate (adds the drops' error
+ * words to their levels and re-evaluates the stopping rule). hpx_campaign_poll
+ * synchronizes `stream` and reads the number of active levels; it returns
+ * HPX_ERR_TIMEOUT / HPX_ERR_NUMERIC if an accumulated drop carried a failure flag
+ * (such drops stay out of the sums). None of the three allocates. */
+hpx_status hpx_campaign_assign(hpx_campaign* campaign, int32_t batch, float* noise_power, void* stream);
+hpx_status hpx_campaign_accumulate(hpx_campaign* campaign, int32_t batch, const uint32_t* errors, void* stream);
+hpx_status hpx_campaign_poll(hpx_campaign* campaign, int32_t* levels_active, void* stream);
 /* Host copies of the per-level drop counts, bit errors, BER sums and flags (any may be NULL). */
 hpx_status hpx_campaign_results(const hpx_campaign* campaign, int64_t* drops, int64_t* errors,
                                 double* ber_sum, double* ber_sq, int32_t* confident);

@@ -114,7 +114,7 @@ def test_headline_pilot_link_estimators(golden, estimator):
 def test_config3_uneven_batch_matches_oracle(golden):
     """40 drops of the uneven distribution (incl. 8x8 / 2048-point / 256-QAM and 1x1 /
     128-point / 4-QAM) in one persistent launch: each drop against the oracle's drop,
-    and exactly the homogeneous engine's count for that drop."""
+    and against the homogeneous engine's count for that drop."""
 
     z = golden("uneven.npz")
     fields = ("num_rx", "num_tx", "fft_size", "num_words", "modulation_order", "num_taps", "tap_decay_db",
@@ -126,9 +126,10 @@ def test_config3_uneven_batch_matches_oracle(golden):
     check_drops(errs, z["errors"], what="uneven")
     bits = int(np.sum(batch.bits))
     check_interval(errs, z["errors"], bits, what="uneven")
-    # the persistent kernel runs the homogeneous kernels' arithmetic: equal counts
-    from tests.test_gpu_uneven import _homogeneous_errors
+    # and the homogeneous engine's counts for the same drops (see assert_same_counts)
+    from tests.test_gpu_uneven import _homogeneous_errors, assert_same_counts
 
     p = batch.noise_power.cpu().numpy()
-    for i in (0, 1, 2, 3, 6):
-        assert errs[i] == _homogeneous_errors(drops[i], int(z["drop0"]) + i, float(p[i]), int(z["seed"])), i
+    pick = list(range(12))
+    assert_same_counts(errs[pick], [_homogeneous_errors(drops[i], int(z["drop0"]) + i, float(p[i]), int(z["seed"]))
+                                    for i in pick])

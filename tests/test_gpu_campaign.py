@@ -64,3 +64,29 @@ def test_campaign_confidence_rule():
     assert abs(s[0] * eng.bits_per_drop - errs[0]) < 1e-6 * max(1, errs[0])
     if errs[1] == 0:
         assert conf[1] == 0 and drops[1] >= 1024
+
+
+@pytest.mark.parametrize("estimator", ["lmmse", "learned"])
+def test_staged_estimator_campaign_matches_plain_runs(estimator):
+    """The campaign over the headline link's staged estimators (tap-domain LMMSE
+    receiver, LS + CNN): with accuracy 0 every level runs to its limit, dealt
+    round-robin, so the per-level errors equal a plain run of the same drops; with a
+    real accuracy a noisy level stops early by the reference's rule."""
+
+    from hermespy_gb300.learned import WEIGHTS_DIR, CnnChannelEstimator
+    from hermespy_gb300.train_estimator import pilot_waveform, workload_channel
+
+    model = CnnChannelEstimator.load(f"{WEIGHTS_DIR}/cnn_4x4_1024.npz", max_batch=48) if estimator == "learned" else None
+    eng = hg.LinkEngine(pilot_waveform(), workload_channel(), 4, 4, 30.72e6, estimator, "lmmse", "snr",
+                        max_drops=48, seed=SEED, model=model)
+    levels = [5.0, 15.0, 25.0]
+    # 48-drop batches deal 16 drops to each level: drop i of the campaign is at level i % 3
+    pts = eng.ber_campaign(levels, accuracy=0.0, min_samples=8, max_drops_per_level=32, batch=48, check_every=2)
+    assert [p.drops for p in pts] == [32, 32, 32]
+    powers = eng.noise_power(levels)
+    per_drop = eng.simulate(np.array([powers[i % 3] for i in range(96)]), drop0=0)
+    for k, p in enumerate(pts):
+        assert p.errors == int(per_drop[k::3].sum())
+    pts = eng.ber_campaign([5.0], accuracy=0.01, confidence=0.05, min_samples=8, max_drops_per_level=4096, batch=48,
+                           check_every=1)
+    assert pts[0].confident and pts[0].drops < 4096
