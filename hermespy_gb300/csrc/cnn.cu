@@ -517,21 +517,32 @@ __global__ void __launch_bounds__(288) k_conv3x3_wgrad(int H, int W, int B, cons
   if (threadIdx.x < CH) atomicAdd(db + threadIdx.x, bsum);
 }
 
-// Per drop: pw[b] = sum of |LS|^2 over pairs, words and columns (blockIdx.y = drop).
-// One warp per (pair, word) row of a drop at a time, lanes along the columns.
-__global__ void k_cnn_power(int H, int W, int ccols, const float2* __restrict__ csi, float* __restrict__ pw) {
-  const int b = blockIdx.y;
-  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+// Per drop: pw[b] = sum of |LS|^2 over pairs, words and columns, one block per drop
+// (blockIdx.x): every warp takes (pair, word) rows in a fixed order and the block
+// adds the warp sums in warp order, so the sum (and every refined estimate that the
+// input scale enters) is the same from run to run.
+constexpr int POWER_THREADS = 512;
+__global__ void __launch_bounds__(POWER_THREADS) k_cnn_power(int H, int W, int ccols, const float2* __restrict__ csi,
+                                                             float* __restrict__ pw) {
+  __shared__ float wsum[POWER_THREADS / 32];
+  const int b = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float e = 0.f;
-  for (int row = blockIdx.x * wpb + (threadIdx.x >> 5); row < NPAIR * H; row += gridDim.x * wpb) {
+  for (int row = warp; row < NPAIR * H; row += POWER_THREADS / 32) {
     const float2* r = csi + ((int64_t)b * NPAIR * H + row) * ccols;
     for (int w = lane; w < W; w += 32) {
       const float2 z = r[w];
       e = fmaf(z.x, z.x, fmaf(z.y, z.y, e));
     }
   }
-  for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(pw + b, e);
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+  if (lane == 0) wsum[warp] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int i = 0; i < POWER_THREADS / 32; ++i) t += wsum[i];
+    pw[b] = t;
+  }
 }
 
 // complex planes [drop][pair][word][ccols] / s -> bf16 NHWC [drop][word][column][32]
@@ -672,9 +683,8 @@ int conv_tiles(int H, int W) { return ((H + TH - 1) / TH) * ((W + TW - 1) / TW);
 // Power sums and the packed, scaled input of B drops of complex planes.
 hpx_status prepare(const hpx_cnn* c, int B, const float2* csi, int ccols, __nv_bfloat16* x0, bool planar,
                    cudaStream_t s) {
-  HPX_CUDA(cudaMemsetAsync(c->d_pw, 0, sizeof(float) * B, s));
   const float inv = 1.f / (float)(NPAIR * c->H * c->W);
-  k_cnn_power<<<dim3(16, B), 256, 0, s>>>(c->H, c->W, ccols, csi, c->d_pw);
+  k_cnn_power<<<B, POWER_THREADS, 0, s>>>(c->H, c->W, ccols, csi, c->d_pw);
   HPX_LAUNCHED("cnn power");
   const int64_t px = (int64_t)B * c->H * c->W;
   if (planar)
