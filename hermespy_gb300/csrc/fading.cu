@@ -427,210 +427,6 @@ __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(Fading
   }
 }
 
-// ------------------------------------------------ register-window propagation
-// The Taylor-tile propagation of k_propagate with the work arranged around the
-// transmit samples instead of the tap groups. Every output value is bit-identical
-// to k_propagate's: the same per-tile coefficients, the same FMA sequence per
-// (output sample, transmit antenna) over the delay groups in ascending delay, the
-// same spatial mixing order and the same noise. What changes is how often shared
-// memory is read: each thread owns R consecutive output samples n0 .. n0 + R - 1 and
-// keeps the transmit samples x[n - d] that delay d needs in a register window of R
-// slots per antenna pair. Stepping from delay d to d + 1 shifts the window by one
-// sample, so each step loads one new sample per antenna pair (the sample of output j
-// sits in slot (j - d) mod R, a compile-time index inside the R-fold unrolled step
-// loop); a delay without a tap group costs only that load. k_propagate reads two
-// samples from shared memory per (tap group, antenna, sample pair) instead.
-// Antennas are packed in pairs so that one FP32x2 FMA serves the same sample of two
-// antennas; the tap response therefore comes as duplicated pairs (h, h), evaluated
-// from the broadcast coefficient pairs (re, re, im, im) with (u^k, u^k).
-// Tile layout: the DP + BT samples of the tile (DP = delay steps rounded up to R) as
-// R planes (plane s mod R, entry s / R, QP entries per plane) of float4 (re tx0,
-// re tx1, im tx0, im tx1) per antenna pair: at every step the 32 lanes of a warp read
-// 32 consecutive 16-byte entries.
-template <int NTX, int K, int R>
-__global__ void __launch_bounds__(tile_len<NTX>() / R, R == 4 ? 2 : 3)
-    k_propagate_w(FadingConst fc, FadingView v, int T, const float2* __restrict__ x, float2* __restrict__ y,
-                  const float* __restrict__ noise_power, uint64_t seed, int64_t drop0, int nb, int QP) {
-  constexpr int BT = tile_len<NTX>();
-  constexpr int PT = BT / R;                 // threads
-  constexpr int NP = NTX / 2;                // antenna pairs
-  constexpr int PF = (BT + 256) / PT;        // tile entries per thread and pair (DP <= 256)
-  extern __shared__ float4 smem4[];
-  const int b = blockIdx.y;
-  const int m0 = blockIdx.x * BT;
-  const int L = fc.L, G = fc.G, S1 = fc.S1, D = fc.D, nrx = fc.nrx;
-  const int DP = nb * R, ns = DP + BT;
-  float4* xs = smem4;                                                     // [NP][R][QP]
-  float2* terms = reinterpret_cast<float2*>(smem4);                       // [L*S1][K+1], before the tile
-  const int region = max(2 * NP * R * QP, (L * S1 * (K + 1) + 1) & ~1);  // in float2
-  float4* coef = reinterpret_cast<float4*>(reinterpret_cast<float2*>(smem4) + region);  // [G][K+1]
-  float2* Sm = reinterpret_cast<float2*>(coef + G * (K + 1));            // [nrx * NTX]
-  int* gidx = reinterpret_cast<int*>(Sm + nrx * NTX);                    // [DP] group of delay d, -1: none
-  int* gf = gidx + DP;                                                    // [G + 1] first tap of each group
-  const int tid = threadIdx.x;
-
-  const float2* Sg = v.spatial(b);
-  for (int i = tid; i < nrx * NTX; i += PT) Sm[i] = Sg[i];
-  for (int i = tid; i < DP; i += PT) gidx[i] = -1;
-  for (int g = tid; g <= G; g += PT) gf[g] = fc.gfirst[g];
-  const int64_t* Wg = v.W(b);
-  const int64_t* Pg = v.P0(b);
-  // the tile's transmit samples, fetched first so that their latency overlaps the set-up
-  const float2* xb = x + (int64_t)b * NTX * T;
-  float4 xpf[PF][NP];
-#pragma unroll
-  for (int i = 0; i < PF; ++i) {
-    const int s = tid + i * PT, t = m0 - DP + s;
-    const bool in = s < ns && t >= 0 && t < T;
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      const float2 a = in ? __ldg(xb + (int64_t)(2 * p) * T + t) : make_float2(0.f, 0.f);
-      const float2 c = in ? __ldg(xb + (int64_t)(2 * p + 1) * T + t) : make_float2(0.f, 0.f);
-      xpf[i][p] = make_float4(a.x, c.x, a.y, c.y);
-    }
-  }
-  {  // Taylor coefficients of every tap around the tile centre (as k_propagate)
-    const float H = 0.5f * BT;
-    for (int q = tid; q < L * S1; q += PT) {
-      const int l = q / S1, n = q - l * S1;
-      const int64_t tc = (int64_t)m0 - fc.delay[l] + BT / 2;
-      const uint64_t p = (uint64_t)Pg[q] + (uint64_t)Wg[q] * (uint64_t)tc;
-      float sn, cs;
-      __sincosf(fixed_to_angle(p), &sn, &cs);
-      const float a = fc.amp[2 * l + (n < fc.S ? 0 : 1)];
-      const float wh = fixed_rate(Wg[q]) * H;
-      float2 t = make_float2(a * cs, a * sn);
-      float2* dst = terms + q * (K + 1);
-      dst[0] = t;
-#pragma unroll
-      for (int k = 1; k <= K; ++k) {
-        const float f = wh / (float)k;
-        t = make_float2(-t.y * f, t.x * f);  // t *= i w H / k
-        dst[k] = t;
-      }
-    }
-  }
-  __syncthreads();
-  for (int g = tid; g < G; g += PT) gidx[fc.gdelay[g]] = g;
-  for (int q = tid; q < G * (K + 1); q += PT) {
-    const int g = q / (K + 1), k = q - g * (K + 1);
-    float2 acc = make_float2(0.f, 0.f);
-    for (int l = gf[g]; l < gf[g + 1]; ++l)
-      for (int n = 0; n < S1; ++n) acc = cadd(acc, terms[(l * S1 + n) * (K + 1) + k]);
-    coef[q] = make_float4(acc.x, acc.x, acc.y, acc.y);
-  }
-  __syncthreads();  // terms consumed: the tile may overwrite them
-#pragma unroll
-  for (int i = 0; i < PF; ++i) {
-    const int s = tid + i * PT;
-    if (s < ns) {
-#pragma unroll
-      for (int p = 0; p < NP; ++p) xs[(p * R + s % R) * QP + s / R] = xpf[i][p];
-    }
-  }
-  __syncthreads();
-  const int TD = T + D;
-  if (m0 + R * (tid & ~31) >= TD) return;  // warps whose samples all lie past the signal
-
-  const int j0 = R * tid;  // first output sample of the thread in the tile
-  float2 ud[R][K + 1];     // (u^k, u^k) of each output sample, as k_propagate's powers
-#pragma unroll
-  for (int j = 0; j < R; ++j) {
-    const float u = ((float)(j0 + j) - 0.5f * BT) / (0.5f * BT);
-    float p = 1.0f;
-    ud[j][0] = make_float2(1.0f, 1.0f);
-#pragma unroll
-    for (int k = 1; k <= K; ++k) {
-      p = p * u;
-      ud[j][k] = make_float2(p, p);
-    }
-  }
-  float4 win[R][NP];  // slot r of each antenna pair
-#pragma unroll
-  for (int j = 0; j < R; ++j)
-#pragma unroll
-    for (int p = 0; p < NP; ++p) win[j][p] = xs[(p * R + j) * QP + tid + nb];  // s = DP + j0 + j
-  float2 zr[R][NP], zi[R][NP];
-#pragma unroll
-  for (int j = 0; j < R; ++j)
-#pragma unroll
-    for (int p = 0; p < NP; ++p) zr[j][p] = zi[j][p] = make_float2(0.f, 0.f);
-#pragma unroll 1
-  for (int bb = 0; bb < nb; ++bb) {
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int g = gidx[bb * R + i];
-      if (g >= 0) {
-        const float4* cl = coef + g * (K + 1);
-        float4 ck[K + 1];
-#pragma unroll
-        for (int k = 0; k <= K; ++k) ck[k] = cl[k];
-#pragma unroll
-        for (int j = 0; j < R; ++j) {
-          float2 hx = make_float2(ck[0].x, ck[0].y), hy = make_float2(ck[0].z, ck[0].w);
-#pragma unroll
-          for (int k = 1; k <= K; ++k) {
-            hx = __ffma2_rn(make_float2(ck[k].x, ck[k].y), ud[j][k], hx);
-            hy = __ffma2_rn(make_float2(ck[k].z, ck[k].w), ud[j][k], hy);
-          }
-          const float2 nhy = make_float2(-hy.x, -hy.y);
-#pragma unroll
-          for (int p = 0; p < NP; ++p) {
-            const float4 w = win[(j - i + R) % R][p];
-            const float2 re = make_float2(w.x, w.y), im = make_float2(w.z, w.w);
-            zr[j][p] = __ffma2_rn(hx, re, zr[j][p]);
-            zr[j][p] = __ffma2_rn(nhy, im, zr[j][p]);
-            zi[j][p] = __ffma2_rn(hx, im, zi[j][p]);
-            zi[j][p] = __ffma2_rn(hy, re, zi[j][p]);
-          }
-        }
-      }
-      // delay bb R + i + 1 needs x[n0 - bb R - i - 1]: plane R - 1 - i, entry tid + nb - bb - 1
-#pragma unroll
-      for (int p = 0; p < NP; ++p) win[R - 1 - i][p] = xs[(p * R + R - 1 - i) * QP + tid + nb - bb - 1];
-    }
-  }
-
-  // ---- spatial mixing (k_propagate's order: antennas 0 .. NTX - 1), AWGN, store
-  const float np = noise_power ? noise_power[b] : 0.0f;
-  const float sigma = sqrtf(0.5f * np);
-#pragma unroll 1
-  for (int rx = 0; rx < nrx; ++rx) {
-    float2* yr = y + ((int64_t)b * nrx + rx) * TD;
-    const bool even_row = ((((int64_t)b * nrx + rx) * TD) & 1) == 0;  // 16-byte stores of sample pairs
-#pragma unroll
-    for (int j = 0; j < R; j += 2) {
-      float2 ore = make_float2(0.f, 0.f), oim = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int tx = 0; tx < NTX; ++tx) {
-        const int p = tx >> 1;
-        const float2 zrs = (tx & 1) ? make_float2(zr[j][p].y, zr[j + 1][p].y) : make_float2(zr[j][p].x, zr[j + 1][p].x);
-        const float2 zis = (tx & 1) ? make_float2(zi[j][p].y, zi[j + 1][p].y) : make_float2(zi[j][p].x, zi[j + 1][p].x);
-        const float2 sv = Sm[rx * NTX + tx];
-        const float2 sr = make_float2(sv.x, sv.x), si = make_float2(sv.y, sv.y), nsi = make_float2(-sv.y, -sv.y);
-        ore = __ffma2_rn(sr, zrs, ore);
-        ore = __ffma2_rn(nsi, zis, ore);
-        oim = __ffma2_rn(sr, zis, oim);
-        oim = __ffma2_rn(si, zrs, oim);
-      }
-      const int m = m0 + j0 + j;
-      if (noise_power && np > 0.0f) {
-        const uint4 w = hpx_random_block(seed, drop0 + b, (uint32_t)rx, HPX_DOMAIN_NOISE, (uint32_t)(m >> 1));
-        const float2 n0 = box_muller(w.x, w.y);
-        const float2 n1 = box_muller(w.z, w.w);
-        ore = __ffma2_rn(make_float2(sigma, sigma), make_float2(n0.x, n1.x), ore);
-        oim = __ffma2_rn(make_float2(sigma, sigma), make_float2(n0.y, n1.y), oim);
-      }
-      if (even_row && m + 1 < TD) {
-        *reinterpret_cast<float4*>(yr + m) = make_float4(ore.x, oim.x, ore.y, oim.y);
-      } else {
-        if (m < TD) yr[m] = make_float2(ore.x, oim.x);
-        if (m + 1 < TD) yr[m + 1] = make_float2(ore.y, oim.y);
-      }
-    }
-  }
-}
-
 // --------------------------------------------------------- ideal CSI (API)
 __global__ void k_ideal_csi(FadingConst fc, FadingView v, int N, int W, const int32_t* __restrict__ window_start,
                             const int32_t* __restrict__ bins, const float2* __restrict__ tw, int ncols,
@@ -719,52 +515,9 @@ hpx_status dispatch_degree_xs(const hpx_fading* f, const void* state, int B, con
   }
 }
 
-#ifndef HPX_PROPAGATE_R
-#define HPX_PROPAGATE_R 4
-#endif
-
-// The register-window kernel for 2 or 4 transmit antennas and channels up to 255
-// samples long (Taylor degree 2 or 3).
-template <int NTX, int K>
-hpx_status launch_propagate_w(const hpx_fading* f, const void* state, int B, const hpx_cf32* x, int T, hpx_cf32* y,
-                              const float* np, uint64_t seed, int64_t drop0, cudaStream_t s) {
-  constexpr int R = HPX_PROPAGATE_R > 0 ? HPX_PROPAGATE_R : 4;
-  constexpr int BT = tile_len<NTX>();
-  const FadingConst fc = fading_const(f);
-  const FadingView v = fading_view(f, state);
-  const int nb = (fc.D + 1 + R - 1) / R;  // steps of R delays covering 0 .. D
-  const int DP = nb * R;
-  // plane length: 8-lane phases of the tile stores hit 8 distinct 16-byte bank groups
-  int QP = (DP + BT + R - 1) / R;
-  if (R == 4)
-    while ((QP & 7) != 2) ++QP;
-  else
-    QP |= 1;
-  const size_t tile = (size_t)(NTX / 2) * R * QP * sizeof(float4);
-  const size_t terms = (((size_t)fc.L * fc.S1 * (K + 1) + 1) & ~(size_t)1) * sizeof(float2);
-  const size_t smem = (tile > terms ? tile : terms) + (size_t)fc.G * (K + 1) * sizeof(float4) +
-                      (size_t)fc.nrx * NTX * sizeof(float2) + (size_t)(DP + fc.G + 1) * sizeof(int) + 16;
-  if (smem > 200 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "propagate: channel too long for one tile");
-  auto kern = k_propagate_w<NTX, K, R>;
-  if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int TD = T + fc.D;
-  dim3 grid((TD + BT - 1) / BT, B);
-  kern<<<grid, BT / R, smem, s>>>(fc, v, T, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(y), np, seed,
-                                  drop0, nb, QP);
-  HPX_LAUNCHED("propagate");
-  return HPX_OK;
-}
-
 template <int NTX>
 hpx_status dispatch_degree(const hpx_fading* f, const void* state, int B, const hpx_cf32* x, int T, hpx_cf32* y,
                            const float* np, uint64_t seed, int64_t drop0, cudaStream_t s) {
-  if constexpr ((NTX == 2 || NTX == 4) && HPX_PROPAGATE_R > 0) {
-    if (f->max_delay + 1 <= 256) {
-      const int K = taylor_degree(f, tile_len<NTX>());
-      if (K == 2) return launch_propagate_w<NTX, 2>(f, state, B, x, T, y, np, seed, drop0, s);
-      if (K == 3) return launch_propagate_w<NTX, 3>(f, state, B, x, T, y, np, seed, drop0, s);
-    }
-  }
   constexpr int XS = tile_len<NTX>() + 64;
   if (NTX <= 4 && tile_width(tile_len<NTX>(), f->max_delay) <= XS)
     return dispatch_degree_xs<NTX, NTX <= 4 ? XS : 0>(f, state, B, x, T, y, np, seed, drop0, s);
