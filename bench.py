@@ -503,7 +503,8 @@ def bench_estimators(ctx, spec, args):
     extra["stages_note"] = ("stages: CUDA events around each kernel of a serialised run of the same path "
                             f"({sel['total_ms'] / args.steps:.3f} ms per step); ms_per_step: LinkEngine.run")
     return {"drops": drops, "total_ms": api_ms, "stage_ms": sel["stage_ms"], "work": work,
-            "ber": api_ber, "e2e_s": e2e_s, "h2d": hb, "d2h": db, "launches": launches, "extra": extra}
+            "ber": api_ber, "e2e_s": e2e_s, "h2d": hb, "d2h": db, "launches": launches, "extra": extra,
+            "engine": eng}
 
 
 def sync_report(ctx, args, signals: int = 2048, slack: int = 256) -> dict:
@@ -561,8 +562,7 @@ def fec_report(ctx, args, blocks: int = 65535, snr_db: float = 3.0) -> dict:
     `blocks` BPSK code blocks over AWGN at `snr_db` per step, channel LLRs resident."""
 
     torch, hg = ctx["torch"], ctx["hg"]
-    g = np.load(os.path.join(ROOT, "tests", "golden", "ldpc.npz"))
-    code = hg.LDPCCoding.from_edges(int(g["N"]), int(g["M"]), g["edge_var"], g["edge_chk"], 100, True, 10)
+    code = hg.LDPCCoding.ofdm_code(100, True, 10)
     K, N = code.bit_block_size, code.code_block_size
     gen = torch.Generator(device=ctx["dev"]).manual_seed(SEED)
     data = torch.randint(0, 2, (blocks, K), dtype=torch.uint8, device=ctx["dev"], generator=gen)
@@ -761,6 +761,57 @@ def bench_uneven(ctx, spec, args):
             "h2d": 4 * drops, "d2h": 4 * drops, "launches": 1, "extra": extra}
 
 
+def oracle_check(ctx, eng) -> dict:
+    """The headline path on the drops of the oracle's BER fixture (the same seed, drop
+    indices and SNRs; tests/golden/ber_pilot.npz): the engine's BER beside the oracle's
+    95 % Clopper-Pearson interval on those drops."""
+
+    z = np.load(os.path.join(ROOT, "tests", "golden", "ber_pilot.npz"))
+    est = eng.estimator
+    if f"{est}_errors" not in z.files:
+        return {"unavailable": f"no oracle fixture for estimator {est}"}
+    seed = eng.seed
+    eng.seed = int(z["seed"])
+    try:
+        errs = eng.simulate(eng.noise_power(z["snr_db"]))
+    finally:
+        eng.seed = seed
+    from hermespy_gb300 import clopper_pearson
+
+    ref = z[f"{est}_errors"].astype(np.int64)
+    bits = ref.size * int(z["bits_per_drop"])
+    lo, hi = clopper_pearson(int(ref.sum()), bits)
+    ber = float(errs.sum()) / bits
+    return {"estimator": est, "drops": int(ref.size), "engine_ber": ber, "oracle_ber": float(ref.sum()) / bits,
+            "oracle_ci95": [lo, hi], "inside": bool(lo <= ber <= hi),
+            "per_drop_max_abs_diff": int(np.max(np.abs(errs - ref)))}
+
+
+def side_workload(name, ctx, args) -> dict:
+    """A second workload timed on the same GPU after the headline (fewer steps)."""
+
+    import copy
+
+    a = copy.copy(args)
+    a.steps, a.warmup, a.drops = min(args.steps, 5), 3, None
+    spec = copy.deepcopy(SPECS[name])
+    res = {"massive": bench_massive, "uneven": bench_uneven, "link4x4": bench_link4x4}[name](ctx, spec, a)
+    ms = res["total_ms"] / a.steps
+    pk = peaks()
+    info = stage_report(res["stage_ms"], a.steps, res["work"], res["drops"], pk)
+    out = {"workload": spec.config["workload"], "drops_per_step": res["drops"], "steps": a.steps,
+           "ms_per_step": round(ms, 4), "bits_per_s": res["drops"] * spec.bits_per_drop / (ms / 1e3),
+           "drops_per_s": res["drops"] / (ms / 1e3), "ber": res["ber"],
+           "e2e_bits_per_s": res["drops"] * spec.bits_per_drop / res["e2e_s"],
+           "stages": {k: {kk: v[kk] for kk in ("ms", "frac", "bound")} for k, v in info.items()}}
+    for k in ("error_vs_fp64", "fp64_pivot_fraction", "homogeneous_4x4"):
+        if k in res["extra"]:
+            out[k] = res["extra"][k]
+    if "autotuner" in res["extra"]:
+        out["launch_shape"] = res["extra"]["autotuner"]["chosen"]
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -807,6 +858,10 @@ def main() -> None:
     with Clocks(local) as clk:
         res = {"estimators": bench_estimators, "link4x4": bench_link4x4, "massive": bench_massive,
                "uneven": bench_uneven}[spec.name](ctx, spec, args)
+    if spec.name == "estimators" and rank == 0 and args.drops is None:
+        # untimed parity check of the headline path, then the other workloads' own lines
+        res["extra"]["oracle_check"] = oracle_check(ctx, res["engine"])
+        res["extra"]["workloads"] = {w: side_workload(w, ctx, args) for w in ("link4x4", "massive", "uneven")}
     # the slowest rank's times (drops are sharded by index; no data-path collective)
     total_ms, e2e_s = max_over_ranks(res["total_ms"]), max_over_ranks(res["e2e_s"])
     drops = res["drops"]

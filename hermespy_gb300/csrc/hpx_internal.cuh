@@ -213,6 +213,7 @@ struct hpx_lmmse {
   uint16_t* d_tc_bop = nullptr;    // [tc_ws_drops][passes][2][128 x KP] FP16 gains operand
   float* d_tc_scale = nullptr;     // [tc_ws_drops]
   int* d_tc_fail = nullptr;        // set if a tensor-core wait timed out (later CTAs skip)
+  int32_t* d_tc_etab = nullptr;    // [W][FC] data element index, -1 for other elements
 };
 constexpr int kLmmseTcChunk = 8192;  // drops per gains/GEMM launch pair (workspace 72 KB per drop)
 hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays);

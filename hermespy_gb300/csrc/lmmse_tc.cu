@@ -38,13 +38,13 @@ constexpr int TC_N = TC_WORDS * 32;
 constexpr int TC_BITBLK = 10;     // Philox blocks staged per (word slot, stream)
 constexpr int TC_NP = 16;         // antenna pairs (4 x 4)
 constexpr long long TC_WAIT = 40ll * 1000 * 1000;  // cycles (~20 ms) before a wait gives up
+constexpr int TC_CTAS = 3;        // CTAs per SM: 3 x 128 TMEM columns, ~68 KB shared memory, 85 registers
 
 struct TcView {
   int W, FC, U, KP, mtiles, nwl, m;
   const int32_t* wlist;   // [nwl] data words, -1 padding
   const int32_t* kfirst;  // [W][mtiles] first data element of row w in tile, -1: none
-  const int8_t* kind;     // [W][FC]
-  const int32_t* index;   // [W][FC]
+  const int32_t* etab;    // [W][FC] data element index, -1 for reference / null elements
   const uint16_t* ftab;   // [mtiles][2][TC_M x KP] K-major FP16 (hi, lo)
   const uint16_t* bop;    // [drops][passes][2][TC_M x KP] FP16 gains operand (hi, lo)
   const float* scale;     // [drops]
@@ -129,13 +129,24 @@ __global__ void __launch_bounds__(512, 2) k_lmmse_gains(LmmseView e, const float
 }
 
 // ------------------------------------------------------- kernel 2: GEMM + detect
-__global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, const float2* __restrict__ grid,
-                                                             int gcols, const float* __restrict__ nv,
-                                                             const __grid_constant__ QamDemapTable qt, int mode,
-                                                             uint64_t seed, int64_t drop0,
-                                                             uint32_t* __restrict__ errors, int* fail) {
+// Operands and received samples arrive by bulk copies issued by thread 0 at the start
+// of each pass (the twiddle tile with the first pass), completing on mbar_ld: the
+// pass's gains operand (hi, lo) and, when the grid's rows are 16-byte aligned, the
+// pass's received rows (4 words x 4 antennas x this tile's columns) into `ys`. The
+// epilogue thus reads its received samples from shared memory; every thread waits
+// on mbar_ld itself before reading them. The tile's element table (data element
+// index of each column of each data word, -1 for other elements) and the drop's
+// gains scale are read before the tensor-memory load of each word.
+// The equalizer works on the unscaled GEMM output A = H / scale with the regularizer
+// s2 / scale^2 and divides the solution by scale: the scale is a power of two, so
+// the result is the one of H itself.
+__global__ void __launch_bounds__(TC_THREADS, TC_CTAS) k_lmmse_tc(TcView v, int W, const float2* __restrict__ grid,
+                                                                  int gcols, int bulk_y, const float* __restrict__ nv,
+                                                                  const __grid_constant__ QamDemapTable qt, int mode,
+                                                                  uint64_t seed, int64_t drop0,
+                                                                  uint32_t* __restrict__ errors, int* fail) {
   extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t mbar;
+  __shared__ uint64_t mbar, mbar_ld;
   __shared__ uint32_t tmem_slot;
   const int mt = blockIdx.x, b = blockIdx.y;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -145,7 +156,8 @@ __global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, con
   unsigned char* a_lo = sm + opbytes;
   unsigned char* b_hi = sm + 2 * opbytes;
   unsigned char* b_lo = sm + 3 * opbytes;
-  uint32_t* bits = reinterpret_cast<uint32_t*>(sm + 4 * opbytes);  // [4 slots][4 streams][TC_BITBLK * 4]
+  float2* ys = reinterpret_cast<float2*>(sm + 4 * opbytes);  // [TC_WORDS][4 antennas][TC_M]
+  uint32_t* bits = reinterpret_cast<uint32_t*>(sm + 4 * opbytes + TC_WORDS * 4 * TC_M * sizeof(float2));
 
   __shared__ int skip;
   if (tid == 0) skip = *(volatile int*)fail;
@@ -158,32 +170,49 @@ __global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, con
     tc::tmem_alloc(&tmem_slot, TC_N);
     tc::tmem_relinquish();
   }
-  if (tid == 0) tc::mbar_init(&mbar, 1);
-  // twiddle operand of this tile
-  {
-    const uint4* src = reinterpret_cast<const uint4*>(v.ftab + (size_t)mt * 2 * TC_M * KP);
-    uint4* dst = reinterpret_cast<uint4*>(a_hi);
-    for (int i = tid; i < (int)(2 * opbytes / 16); i += TC_THREADS) dst[i] = src[i];
+  if (tid == 0) {
+    tc::mbar_init(&mbar, 1);
+    tc::mbar_init(&mbar_ld, 1);
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
+  const int c0 = mt * TC_M;
+  const int ncol = min(TC_M, v.FC - c0);
+  const uint32_t rowbytes = (uint32_t)ncol * sizeof(float2);  // ncol even when bulk_y (checked on the host)
+  const unsigned char* bop = reinterpret_cast<const unsigned char*>(v.bop) + (size_t)b * (v.nwl / TC_WORDS) * 2 * opbytes;
   const float scl = v.scale[b];
   const float s2 = nv ? nv[b] : 0.0f;
-  const int c0 = mt * TC_M;
-  const unsigned char* bop = reinterpret_cast<const unsigned char*>(v.bop) + (size_t)b * (v.nwl / TC_WORDS) * 2 * opbytes;
-  bool ok = true, fin = finite_f(s2);  // a NaN / inf noise power is an invalid drop too
+  const float inv_scl = 1.0f / scl;          // powers of two: exact
+  const float s2a = s2 * inv_scl * inv_scl;  // regularizer of the unscaled system
+  bool ok = true, fin = finite_f(s2);        // a NaN / inf noise power is an invalid drop too
   unsigned int local = 0;
   const uint32_t idesc = tc::idesc_f16_f32(TC_M, TC_N);
   const int npass = v.nwl / TC_WORDS;
+  const int qtr = warp & 3;
+  const int cl = qtr * 32 + lane;  // this thread's column in the tile (TMEM lane)
+  const int c = c0 + cl;
+  int issued = 0;                  // mbar_ld phases armed by thread 0
   for (int p = 0; p < npass; ++p) {
-    if (p > 0) __syncthreads();  // every thread is done with the previous pass's bits
-    // ---- the pass's gains operand (hi, lo), prepared by k_lmmse_gains
-    {
-      const uint4* src = reinterpret_cast<const uint4*>(bop + (size_t)p * 2 * opbytes);
-      uint4* dst = reinterpret_cast<uint4*>(b_hi);
-      for (int i = tid; i < (int)(2 * opbytes / 16); i += TC_THREADS) dst[i] = src[i];
+    if (p > 0) __syncthreads();  // every thread is done with the previous pass's bits and samples
+    if (tid == 0) {
+      uint32_t bytes = 2 * opbytes + (p == 0 ? 2 * opbytes : 0);
+      if (bulk_y)
+        for (int s = 0; s < TC_WORDS; ++s) bytes += v.wlist[p * TC_WORDS + s] >= 0 ? 4 * rowbytes : 0;
+      tc::mbar_arrive_expect_tx(&mbar_ld, bytes);
+      if (p == 0) tc::bulk_g2s(a_hi, v.ftab + (size_t)mt * 2 * TC_M * KP, 2 * opbytes, &mbar_ld);
+      tc::bulk_g2s(b_hi, bop + (size_t)p * 2 * opbytes, 2 * opbytes, &mbar_ld);
+      if (bulk_y) {
+        for (int s = 0; s < TC_WORDS; ++s) {
+          const int w = v.wlist[p * TC_WORDS + s];
+          if (w < 0) continue;
+          for (int r = 0; r < 4; ++r)
+            tc::bulk_g2s(ys + (s * 4 + r) * TC_M, grid + (((int64_t)b * 4 + r) * W + w) * gcols + c0, rowbytes,
+                         &mbar_ld);
+        }
+      }
+      ++issued;
     }
     // ---- Philox bits of the elements of the pass's rows in this tile
     for (int it = tid; it < TC_WORDS * 4 * TC_BITBLK; it += TC_THREADS) {
@@ -198,47 +227,51 @@ __global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, con
       }
       *reinterpret_cast<uint4*>(bits + (size_t)(s * 4 + t) * TC_BITBLK * 4 + j * 4) = blk;
     }
-    tc::fence_proxy_async_smem();
     tc::fence_before_sync();
-    __syncthreads();  // operands written; previous pass's TMEM reads done
+    __syncthreads();  // bits written; previous pass's TMEM reads done
     tc::fence_after_sync();
+    const bool landed = tc::mbar_wait(&mbar_ld, (uint32_t)(p & 1), TC_WAIT);  // operands and samples in place
+    ok = ok && landed;
     if (tid == 0) {
-      for (int ks = 0; ks < KP / 16; ++ks) {
-        const uint32_t koff = (uint32_t)ks * 256;  // two core matrices along K
-        const uint64_t ah = tc::smem_desc(a_hi + koff, 128, KP * 16), al = tc::smem_desc(a_lo + koff, 128, KP * 16);
-        const uint64_t bh = tc::smem_desc(b_hi + koff, 128, KP * 16), bl = tc::smem_desc(b_lo + koff, 128, KP * 16);
-        tc::mma_f16(tmem, ah, bh, idesc, ks > 0);
-        tc::mma_f16(tmem, ah, bl, idesc, true);
-        tc::mma_f16(tmem, al, bh, idesc, true);
+      if (landed) {
+        for (int ks = 0; ks < KP / 16; ++ks) {
+          const uint32_t koff = (uint32_t)ks * 256;  // two core matrices along K
+          const uint64_t ah = tc::smem_desc(a_hi + koff, 128, KP * 16), al = tc::smem_desc(a_lo + koff, 128, KP * 16);
+          const uint64_t bh = tc::smem_desc(b_hi + koff, 128, KP * 16), bl = tc::smem_desc(b_lo + koff, 128, KP * 16);
+          tc::mma_f16(tmem, ah, bh, idesc, ks > 0);
+          tc::mma_f16(tmem, ah, bl, idesc, true);
+          tc::mma_f16(tmem, al, bh, idesc, true);
+        }
       }
-      tc::mma_commit(&mbar);
+      tc::mma_commit(&mbar);  // arrives at once if nothing was issued
     }
     ok = ok && tc::mbar_wait(&mbar, (uint32_t)(p & 1), TC_WAIT);
     tc::fence_after_sync();
     // ---- epilogue: thread = subcarrier (TMEM lane), two word slots per warp
-    const int qtr = warp & 3;
-    const int c = c0 + qtr * 32 + lane;
 #pragma unroll 1
     for (int s = warp >> 2; s < TC_WORDS; s += 2) {
+      const int w = v.wlist[p * TC_WORDS + s];
+      const bool mine = ok && w >= 0 && c < v.FC;
+      const int k = mine ? v.etab[w * v.FC + c] : -1;  // data element index, -1: not a data element
+      float2 y[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        y[r] = k < 0 ? make_float2(0.f, 0.f)
+                     : (bulk_y ? ys[(s * 4 + r) * TC_M + cl] : grid[(((int64_t)b * 4 + r) * W + w) * gcols + c]);
       float acc[32];
       tc::tmem_ld32(tmem + ((uint32_t)(qtr * 32) << 16) + (uint32_t)(s * 32), acc);
-      const int w = v.wlist[p * TC_WORDS + s];
-      if (!ok || w < 0 || c >= v.FC) continue;
-      if (v.kind[w * v.FC + c] != HPX_RE_DATA) continue;
-      const int k = v.index[w * v.FC + c];
-      float2 H[4][4], y[4], x[4];
+      if (k < 0) continue;
+      float2 A[4][4], x[4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        y[r] = grid[(((int64_t)b * 4 + r) * W + w) * gcols + c];
+      for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int t = 0; t < 4; ++t) H[r][t] = make_float2(acc[r * 4 + t] * scl, acc[16 + r * 4 + t] * scl);
-      }
-      fin &= equalize_one<4, 4>(mode, H, y, s2, x);
+        for (int t = 0; t < 4; ++t) A[r][t] = make_float2(acc[r * 4 + t], acc[16 + r * 4 + t]);
+      fin &= equalize_one<4, 4>(mode, A, y, s2a, x);
       const int kf = v.kfirst[w * v.mtiles + mt];
       const int64_t pos = (int64_t)k * m - ((((int64_t)kf * m) >> 7) << 7);
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
-        const uint32_t rx_v = qam_decide(qt, x[t]);
+        const uint32_t rx_v = qam_decide(qt, make_float2(x[t].x * inv_scl, x[t].y * inv_scl));
         const uint32_t tx_v = extract_bits_msb(bits + (size_t)(s * 4 + t) * TC_BITBLK * 4, pos, m);
         local += __popc(rx_v ^ tx_v);
       }
@@ -248,6 +281,9 @@ __global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, con
   __syncthreads();
   tc::fence_after_sync();
   if (warp == 0) tc::tmem_dealloc(tmem, TC_N);
+  // copies of a pass whose wait gave up may still be landing: let them land (bounded)
+  if (tid == 0 && !ok)
+    for (int p = 0; p < issued; ++p) tc::mbar_wait(&mbar_ld, (uint32_t)(p & 1), TC_WAIT);
   // block error count
   for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
   __shared__ unsigned int wsum[TC_THREADS / 32];
@@ -257,7 +293,7 @@ __global__ void __launch_bounds__(TC_THREADS, 4) k_lmmse_tc(TcView v, int W, con
   if (tid == 0) {
     unsigned int tot = 0;
     for (int i = 0; i < TC_THREADS / 32; ++i) tot += wsum[i];
-    if (!okall) {  // the tensor core never signalled completion
+    if (!okall) {  // the tensor core or a bulk copy never signalled completion
       atomicOr(errors + b, HPX_DROP_TIMEOUT);
       atomicExch(fail, 1);
     } else {
@@ -312,6 +348,9 @@ hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays) {
     if (any) wl.push_back(w);
   }
   while (wl.empty() || wl.size() % TC_WORDS) wl.push_back(-1);
+  std::vector<int32_t> etab((size_t)W * FC, -1);
+  for (size_t i = 0; i < etab.size(); ++i)
+    if (fr->h_kind[i] == HPX_RE_DATA) etab[i] = fr->h_index[i];
   std::vector<int32_t> kfirst((size_t)W * mtiles, -1);
   for (int w = 0; w < W; ++w)
     for (int c = 0; c < FC; ++c)
@@ -327,6 +366,7 @@ hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays) {
   upload_raw(reinterpret_cast<void**>(&e->d_tc_ftab), ftab.data(), ftab.size() * 2, &err);
   upload_raw(reinterpret_cast<void**>(&e->d_tc_wlist), wl.data(), wl.size() * 4, &err);
   upload_raw(reinterpret_cast<void**>(&e->d_tc_kfirst), kfirst.data(), kfirst.size() * 4, &err);
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_etab), etab.data(), etab.size() * 4, &err);
   upload_raw(reinterpret_cast<void**>(&e->d_tc_bop), nullptr,
              (size_t)kLmmseTcChunk * (wl.size() / TC_WORDS) * 2 * TC_M * KP * 2, &err);
   upload_raw(reinterpret_cast<void**>(&e->d_tc_scale), nullptr, (size_t)kLmmseTcChunk * 4, &err);
@@ -337,15 +377,16 @@ hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays) {
 }
 
 void lmmse_tc_release(hpx_lmmse* e) {
-  void* p[] = {e->d_tc_ftab, e->d_tc_wlist, e->d_tc_kfirst, e->d_tc_bop, e->d_tc_scale, e->d_tc_fail};
+  void* p[] = {e->d_tc_ftab, e->d_tc_wlist, e->d_tc_kfirst, e->d_tc_bop, e->d_tc_scale, e->d_tc_fail, e->d_tc_etab};
   for (void* q : p)
     if (q) cudaFree(q);
 }
 
 // At least 48 KB, so that at most four CTAs (4 x 128 TMEM columns) share an SM.
 size_t lmmse_tc_smem(const hpx_lmmse* e) {
-  const size_t need = (size_t)4 * TC_M * e->tc_KP * 2 + (size_t)TC_WORDS * 4 * TC_BITBLK * 16 + 128;
-  return std::max(need, (size_t)48 * 1024);
+  // operands (twiddles, gains: hi and lo), received samples of a pass, staged bits
+  return (size_t)4 * TC_M * e->tc_KP * 2 + (size_t)TC_WORDS * 4 * TC_M * sizeof(float2) +
+         (size_t)TC_WORDS * 4 * TC_BITBLK * 16 + 128;
 }
 
 // The 4 x 4 receiver over B drops in chunks of the workspace size.
@@ -362,7 +403,10 @@ hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int
   HPX_CUDA(cudaFuncSetAttribute(k_lmmse_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
   const LmmseView lv = lmmse_view(e);
   TcView tv{e->W, fr->info.num_columns, e->U, e->tc_KP, e->tc_mtiles, e->tc_nwl, fr->info.bits_per_symbol,
-            e->d_tc_wlist, e->d_tc_kfirst, fr->d_kind, fr->d_index, e->d_tc_ftab, e->d_tc_bop, e->d_tc_scale};
+            e->d_tc_wlist, e->d_tc_kfirst, e->d_tc_etab, e->d_tc_ftab, e->d_tc_bop, e->d_tc_scale};
+  // received rows by bulk copy: 16-byte aligned rows and an even number of columns per tile
+  const int bulk_y = (gcols % 2 == 0) && (fr->info.num_columns % 2 == 0) &&
+                     (reinterpret_cast<uintptr_t>(grid) % 16 == 0);
   const int64_t per_drop = (int64_t)4 * e->W * gcols;  // grid samples per drop
   for (int d = 0; d < B; d += e->tc_ws_drops) {
     const int nb = std::min(e->tc_ws_drops, B - d);
@@ -371,8 +415,8 @@ hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int
     k_lmmse_gains<<<nb, 512, smem_g, s>>>(lv, g, gcols, n, e->d_tc_wlist, e->tc_nwl, e->tc_KP, e->d_tc_bop,
                                           e->d_tc_scale);
     HPX_LAUNCHED("lmmse_gains");
-    k_lmmse_tc<<<dim3(e->tc_mtiles, nb), TC_THREADS, smem_t, s>>>(tv, e->W, g, gcols, n, qt, mode, seed, drop0 + d,
-                                                                  errors + d, e->d_tc_fail);
+    k_lmmse_tc<<<dim3(e->tc_mtiles, nb), TC_THREADS, smem_t, s>>>(tv, e->W, g, gcols, bulk_y, n, qt, mode, seed,
+                                                                  drop0 + d, errors + d, e->d_tc_fail);
     HPX_LAUNCHED("lmmse_tc");
   }
   return HPX_OK;

@@ -17,6 +17,7 @@ published algorithms rather than aff3ct bit for bit.
 from __future__ import annotations
 
 import ctypes
+import os
 from math import ceil
 
 import numpy as np
@@ -116,6 +117,17 @@ class LDPCCoding(Encoder):
         obj.min_num_iterations = int(min_num_iterations)
         obj._create(int(N), int(M), np.asarray(edge_var, np.int32), np.asarray(edge_chk, np.int32))
         return obj
+
+    @classmethod
+    def ofdm_code(cls, num_iterations: int = 100, enable_syndrome_checking: bool = True,
+                  min_num_iterations: int = 10) -> "LDPCCoding":
+        """The (128, 64) code of the reference's 5G NR OFDM modem resources
+        (modem/resources/ofdm_ldpc.alist), shipped as the edges of its parity-check
+        matrix in ``codes/ofdm_ldpc.npz``."""
+
+        z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "codes", "ofdm_ldpc.npz"))
+        return cls.from_edges(int(z["N"]), int(z["M"]), z["edge_var"], z["edge_chk"], num_iterations,
+                              enable_syndrome_checking, min_num_iterations)
 
     def _create(self, N: int, M: int, ev: np.ndarray, ec: np.ndarray) -> None:
         lib = _lib.load()

@@ -66,3 +66,17 @@ def test_alist_reader_matches_oracle(golden, tmp_path):
     N, M, ev, ec = read_alist(str(path))
     assert (N, M) == (128, 64)
     np.testing.assert_array_equal(ldpc.dense_h(N, M, ev, ec), h)
+
+
+def test_shipped_code_is_the_reference_matrix(golden):
+    """The package's copy of the OFDM modem's parity-check edges (used by the benchmark)
+    is the fixture recorded from the reference's alist file."""
+
+    import os
+
+    import hermespy_gb300
+
+    g = golden("ldpc.npz")
+    z = np.load(os.path.join(os.path.dirname(hermespy_gb300.__file__), "codes", "ofdm_ldpc.npz"))
+    for k in ("N", "M", "edge_var", "edge_chk"):
+        assert np.array_equal(z[k], g[k])
