@@ -122,7 +122,7 @@ __device__ __forceinline__ void sync_group() {
 
 // Stage twiddles: stage s with span Ns and radix R reads exp(-2 pi i r k / (Ns R))
 // from entry (r Ns + k) of its table, so lanes with consecutive k load consecutive
-// entries. Tables of the second and third stage are stored back to back
+// entries; radix 8 and 16 stages load r = 1..4 and multiply up the rest. Tables of the second and third stage are stored back to back
 // (stage 2 at 0, stage 3 at R0 R1); 2 N entries cover every plan.
 template <int N>
 __host__ __device__ constexpr int stage_table_offset(int s) {
@@ -150,11 +150,30 @@ __device__ __forceinline__ void stage(float2* buf, int t, int Ns, const float2* 
     const int j = t + b * TP;
     const int k = j & (Ns - 1);
     if (Ns > 1) {
+      if constexpr (R <= 4) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) {
-        float2 w = __ldg(tw + r * Ns + k);
-        if (INV) w.y = -w.y;
-        a[b][r] = cmul(a[b][r], w);
+        for (int r = 1; r < R; ++r) {
+          float2 w = __ldg(tw + r * Ns + k);
+          if (INV) w.y = -w.y;
+          a[b][r] = cmul(a[b][r], w);
+        }
+      } else {
+        // twiddles 1..4 from the table, r > 4 as w_(r-4) w_4 (at most three products
+        // deep, a few 1e-7 relative): 4 loads instead of R - 1 per butterfly
+        float2 wv[4];
+#pragma unroll
+        for (int r = 1; r <= 4; ++r) wv[r & 3] = __ldg(tw + r * Ns + k);
+        const float2 w4 = wv[0];
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          float2 w = wv[r & 3];
+          if (r > 4) {
+            w = cmul(w, w4);
+            wv[r & 3] = w;
+          }
+          if (INV) w.y = -w.y;
+          a[b][r] = cmul(a[b][r], w);
+        }
       }
     }
     dft<R, INV>(a[b]);
