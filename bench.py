@@ -416,7 +416,7 @@ def bench_estimators(ctx, spec, args):
     chunk = min(drops, 1024)
     model = CnnChannelEstimator.load(wpath, max_batch=chunk)
     eng = hg.LinkEngine(wf, workload_channel(), 4, 4, spec.fs, "learned", "lmmse", "snr", max_drops=drops, seed=SEED,
-                        model=model, also=("lmmse",))
+                        model=model, also=("lmmse", "lmmse_robust"))
     fh, fd = eng._fading.handle, eng._frame
     T, D = eng._T, eng._D
     p_host = eng.noise_power(ctx["rng"].uniform(0.0, 30.0, size=drops)).astype(np.float32)
@@ -441,6 +441,9 @@ def bench_estimators(ctx, spec, args):
         "lmmse": front + [("detect_lmmse_fused", lambda d0: _lib.call("hpx_detect_lmmse", eng._lmmse, 4, _lib.EQ_LMMSE,
                                                                       _lib.ptr(grid), C, _lib.ptr(p), SEED, d0, drops,
                                                                       _lib.ptr(errors), sp))],
+        "lmmse_robust": front + [("detect_lmmse_fused", lambda d0: _lib.call(
+            "hpx_detect_lmmse", eng._lmmse_robust, 4, _lib.EQ_LMMSE, _lib.ptr(grid), C, _lib.ptr(p), SEED, d0, drops,
+            _lib.ptr(errors), sp))],
         "ls": front + [ls_est, detect],
     }
     HWp = W * C
@@ -469,7 +472,7 @@ def bench_estimators(ctx, spec, args):
     truth = torch.empty((nval, 4, 4, W, C), dtype=torch.complex64, device=dev)
     _lib.call("hpx_fading_ideal_csi", fh, _lib.ptr(st), nval, fd, C, _lib.ptr(truth), sp)
     nm = {}
-    for est in ("ls", "lmmse", "learned"):
+    for est in ("ls", "lmmse", "lmmse_robust", "learned"):
         e = eng.estimate(nval, pv, estimator=est)
         nm[est] = round(nmse_db(*csi_error(fd, e, truth)), 3)
     selected = "learned" if nm["learned"] <= nm["lmmse"] + 0.5 else "lmmse"
@@ -498,7 +501,13 @@ def bench_estimators(ctx, spec, args):
         "validation_drops": nval,
         "lmmse_is_genie": "the tap-domain LMMSE judge is given the channel's true tap delays, powers and Doppler; "
                           "the CNN sees only the per-stream LS estimate and was trained on random 4-23-tap "
-                          "channels; its 3x3 layers see 13 x 13 grid elements after six layers"},
+                          "channels; its 3x3 layers see 13 x 13 grid elements after six layers",
+        "fair_comparison": {
+            "robust_lmmse": "tap-domain LMMSE with design statistics only: uniform profile over 64 sample delays "
+                            "(2.1 us) carrying the channel's expected energy, 1000 Hz design Doppler",
+            "nmse_db": {"learned": nm["learned"], "lmmse_robust": nm["lmmse_robust"], "lmmse_genie": nm["lmmse"]},
+            "ber": {k: results[k]["ber"] for k in ("learned", "lmmse_robust", "lmmse")},
+            "learned_beats_robust_nmse": bool(nm["learned"] < nm["lmmse_robust"])}},
         "weights": os.path.relpath(wpath, ROOT)}
     extra["stages_note"] = ("stages: CUDA events around each kernel of a serialised run of the same path "
                             f"({sel['total_ms'] / args.steps:.3f} ms per step); ms_per_step: LinkEngine.run")

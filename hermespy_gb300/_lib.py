@@ -129,6 +129,7 @@ _SIGNATURES = {
     "hpx_ls_create_streams": [c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p],
     "hpx_ls_estimate_streams": [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p],
     "hpx_lmmse_create": [c_void_p, c_void_p, c_int32, c_void_p],
+    "hpx_lmmse_create_regularized": [c_void_p, c_void_p, c_int32, c_double, c_void_p],
     "hpx_lmmse_destroy": [c_void_p],
     "hpx_lmmse_estimate": [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
     "hpx_csi_error": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],

@@ -19,6 +19,7 @@
 // Steps 1's matrices and 2's R_u, r_u depend only on frame and channel and are
 // built once on the host in double precision; the noise-dependent solve of step 2
 // runs per drop on the device.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <vector>
@@ -259,7 +260,14 @@ void release(hpx_lmmse* e) {
 extern "C" {
 
 hpx_status hpx_lmmse_create(const hpx_frame* frame, const hpx_fading* fading, int32_t C, hpx_lmmse** out) {
+  return hpx_lmmse_create_regularized(frame, fading, C, 0.0, out);
+}
+
+hpx_status hpx_lmmse_create_regularized(const hpx_frame* frame, const hpx_fading* fading, int32_t C,
+                                        double ridge_noise, hpx_lmmse** out) {
   if (!frame || !fading || !out) return hpx_fail(HPX_ERR_ARG, "lmmse: null argument");
+  if (!(ridge_noise >= 0.0) || !std::isfinite(ridge_noise))
+    return hpx_fail(HPX_ERR_ARG, "lmmse: ridge noise variance must be finite and non-negative");
   *out = nullptr;
   const int N = frame->info.num_subcarriers, W = frame->info.num_words, FC = frame->info.num_columns;
   const int ntx = fading->ntx;
@@ -331,7 +339,28 @@ hpx_status hpx_lmmse_create(const hpx_frame* frame, const hpx_fading* fading, in
           for (int i = 0; i < n; ++i) s += std::conj(A[(size_t)i * U + u]) * A[(size_t)i * U + v];
           AhA[(size_t)u * U + v] = s;
         }
+      // plain: (A^H A)^-1 A^H, noise per tap diag((A^H A)^-1); regularized with the prior
+      // profile: M = A^H A + ridge diag(1 / P_u), M^-1 A^H, noise per tap diag(M^-1 A^H A M^-1)
+      std::vector<cd> AhA0;
+      if (ridge_noise > 0.0) {
+        AhA0 = AhA;
+        for (int u = 0; u < U; ++u) AhA[(size_t)u * U + u] += ridge_noise / std::max(Pu[u], 1e-300);
+      }
       if (!invert(AhA, U)) return hpx_fail(HPX_ERR_UNSUPPORTED, "lmmse: pilot geometry of word %d is singular", w);
+      std::vector<double> noise_tap(U);
+      for (int u = 0; u < U; ++u) {
+        if (ridge_noise > 0.0) {
+          cd sum = 0.0;  // (M^-1 A^H A M^-1)[u][u]
+          for (int a = 0; a < U; ++a) {
+            cd t = 0.0;
+            for (int b = 0; b < U; ++b) t += AhA0[(size_t)a * U + b] * std::conj(AhA[(size_t)u * U + b]);
+            sum += AhA[(size_t)u * U + a] * t;
+          }
+          noise_tap[u] = sum.real();
+        } else {
+          noise_tap[u] = AhA[(size_t)u * U + u].real();
+        }
+      }
       pw_word[t * kMaxPilotWords + np] = w;
       pw_count[t * kMaxPilotWords + np] = n;
       pw_off[t * kMaxPilotWords + np] = (int)pcol.size();
@@ -339,7 +368,7 @@ hpx_status hpx_lmmse_create(const hpx_frame* frame, const hpx_fading* fading, in
       const size_t g0 = G.size();
       G.resize(g0 + (size_t)U * n);
       for (int u = 0; u < U; ++u) {
-        E[(t * kMaxPilotWords + np) * U + u] = (float)AhA[(size_t)u * U + u].real();
+        E[(t * kMaxPilotWords + np) * U + u] = (float)noise_tap[u];
         for (int i = 0; i < n; ++i) {
           cd s = 0.0;
           for (int v = 0; v < U; ++v) s += AhA[(size_t)u * U + v] * std::conj(A[(size_t)i * U + v]);

@@ -25,7 +25,7 @@ from scipy.stats import beta
 
 from . import _lib
 from .channel import MultipathFadingChannel
-from .estimation import ls_interpolation_table, ls_stream_tables
+from .estimation import ls_interpolation_table, ls_stream_tables, robust_statistics
 from .waveform import OFDMWaveform
 
 
@@ -59,8 +59,8 @@ class LinkEngine:
     def __init__(self, waveform: OFDMWaveform, channel: MultipathFadingChannel, num_tx: int, num_rx: int,
                  sampling_rate: float, estimator: str = "ideal", equalizer: str = "lmmse", noise: str = "snr",
                  max_drops: int = 4096, seed: int = 0, model=None, also: tuple = ()) -> None:
-        if estimator not in ("ideal", "ls", "lmmse", "learned"):
-            raise ValueError("estimator must be 'ideal', 'ls', 'lmmse' or 'learned'")
+        if estimator not in ("ideal", "ls", "lmmse", "lmmse_robust", "learned"):
+            raise ValueError("estimator must be 'ideal', 'ls', 'lmmse', 'lmmse_robust' or 'learned'")
         if estimator == "learned" and model is None:
             raise ValueError("the learned estimator needs a model")
         if equalizer not in ("zf", "lmmse"):
@@ -79,6 +79,7 @@ class LinkEngine:
         self._frame = waveform._frame()
         self._ls = None
         self._lmmse = None
+        self._lmmse_robust = None
         self._link = None
         self.model = model
         comb = waveform.pilot_comb
@@ -87,7 +88,7 @@ class LinkEngine:
         siso = num_tx == 1 and num_rx == 1
         if estimator == "ls" and not siso and comb < max(num_tx, 2):
             raise NotImplementedError("Least-Squares channel estimation is only implemented for SISO links")
-        self.staged = estimator in ("lmmse", "learned") or (estimator == "ls" and not siso)
+        self.staged = estimator in ("lmmse", "lmmse_robust", "learned") or (estimator == "ls" and not siso)
         # `also`: further estimators whose tables are built too, for estimate(estimator=...)
         wanted = {estimator, *also}
         if self.staged and wanted & {"ls", "learned"} or estimator in ("ls", "learned"):
@@ -106,6 +107,14 @@ class LinkEngine:
             h = ctypes.c_void_p()
             _lib.check(_lib.load().hpx_lmmse_create(self._frame, self._fading.handle, cols, ctypes.byref(h)))
             self._lmmse = h
+        if "lmmse_robust" in wanted:
+            # the non-genie counterpart: design statistics instead of the channel's
+            design, ridge = robust_statistics(channel, sampling_rate)
+            self._robust_fading = design.handle(num_rx, num_tx, sampling_rate)
+            h = ctypes.c_void_p()
+            _lib.check(_lib.load().hpx_lmmse_create_regularized(self._frame, self._robust_fading.handle, cols,
+                                                                float(ridge), ctypes.byref(h)))
+            self._lmmse_robust = h
         self.num_columns = cols
         if self.staged:
             self._alloc(self.max_drops)
@@ -142,6 +151,8 @@ class LinkEngine:
                     _lib._lib.hpx_ls_destroy(self._ls)
                 if self._lmmse is not None:
                     _lib._lib.hpx_lmmse_destroy(self._lmmse)
+                if self._lmmse_robust is not None:
+                    _lib._lib.hpx_lmmse_destroy(self._lmmse_robust)
         except Exception:
             pass
 
@@ -175,9 +186,9 @@ class LinkEngine:
                       _lib.ptr(out), sp)
         elif est == "ls":
             _lib.call("hpx_ls_estimate_streams", self._ls, _lib.ptr(self._grid), C, self.num_rx, n, _lib.ptr(out), sp)
-        elif est == "lmmse":
-            _lib.call("hpx_lmmse_estimate", self._lmmse, _lib.ptr(self._grid), C, self.num_rx, n,
-                      _lib.ptr(noise_power), _lib.ptr(out), sp)
+        elif est in ("lmmse", "lmmse_robust"):
+            _lib.call("hpx_lmmse_estimate", self._lmmse if est == "lmmse" else self._lmmse_robust,
+                      _lib.ptr(self._grid), C, self.num_rx, n, _lib.ptr(noise_power), _lib.ptr(out), sp)
         elif est == "learned":
             _lib.call("hpx_ls_estimate_streams", self._ls, _lib.ptr(self._grid), C, self.num_rx, n, _lib.ptr(out), sp)
             self.model.refine(out, stream)
@@ -214,9 +225,10 @@ class LinkEngine:
             errors = torch.empty(n, dtype=torch.int32, device=self.device)
         if self.staged:
             self.receive(drop0, noise_power, stream)
-            if self.estimator == "lmmse" and self._lmmse is not None:
+            lm = {"lmmse": self._lmmse, "lmmse_robust": self._lmmse_robust}.get(self.estimator)
+            if lm is not None:
                 # fused: the LMMSE estimate stays on chip (hpx_detect_lmmse)
-                _lib.call("hpx_detect_lmmse", self._lmmse, self.num_rx,
+                _lib.call("hpx_detect_lmmse", lm, self.num_rx,
                           _lib.EQ_ZF if self.equalizer == "zf" else _lib.EQ_LMMSE, _lib.ptr(self._grid),
                           self.num_columns, _lib.ptr(noise_power), self.seed, int(drop0), n, _lib.ptr(errors),
                           _lib.stream_ptr(stream))
@@ -234,8 +246,9 @@ class LinkEngine:
 
         sp = _lib.stream_ptr(stream)
         try:
-            if self._lmmse is not None:
-                _lib.call("hpx_lmmse_status", self._lmmse, int(clear), sp)
+            for lm in (self._lmmse, self._lmmse_robust):
+                if lm is not None:
+                    _lib.call("hpx_lmmse_status", lm, int(clear), sp)
         finally:
             if self.model is not None:
                 self.model.status(clear, stream)

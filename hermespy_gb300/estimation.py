@@ -102,6 +102,32 @@ def ls_stream_tables(ref_mask: np.ndarray, comb: int, num_streams: int) -> tuple
             np.concatenate(wts).astype(np.float32))
 
 
+def robust_statistics(channel, sampling_rate: float, num_delays: int = 64, doppler_frequency: float = 1000.0,
+                      design_snr_db: float = 20.0):
+    """Design statistics of the robust tap-domain LMMSE estimator: a channel that
+    knows nothing of the true one but its expected energy, and the prior noise
+    variance that regularizes its tap estimates.
+
+    The robust LMMSE of Li, Cimini and Sollenberger (IEEE Trans. Commun. 46(7), 1998)
+    replaces the channel's power-delay profile and Doppler by a uniform profile over
+    an assumed delay window and a design Doppler bound. Here the window is
+    ``num_delays`` sample delays (64 at 30.72 MHz: 2.1 us, beyond the 4x4 workload's
+    1.1 us and within its 2.3 us cyclic prefix), the bound ``doppler_frequency``, the
+    uniform profile carries the channel's expected energy (gain times the sum of its
+    powers, which the receiver can measure as received power), and the prior noise is
+    that of ``design_snr_db`` (20 dB gave the lowest NMSE over 5-25 dB). Returns
+    (design channel, ridge noise variance) for ``hpx_lmmse_create_regularized``. No
+    counterpart in the reference."""
+
+    from .channel import MultipathFadingChannel
+
+    energy = float(channel.gain) * float(np.sum(channel.power_profile))
+    delays = np.arange(int(num_delays)) / float(sampling_rate)
+    design = MultipathFadingChannel(list(delays), [energy / num_delays] * int(num_delays), [0.0] * int(num_delays),
+                                    doppler_frequency=float(doppler_frequency))
+    return design, energy * 10.0 ** (-design_snr_db / 10.0)
+
+
 class OrthogonalLeastSquaresChannelEstimation(ChannelEstimation):
     """Least-squares estimation with linear interpolation (SISO)."""
 

@@ -275,6 +275,17 @@ hpx_status hpx_ls_estimate_streams(const hpx_ls* ls, const hpx_cf32* grid, int32
 typedef struct hpx_lmmse hpx_lmmse;
 hpx_status hpx_lmmse_create(const hpx_frame* frame, const hpx_fading* fading, int32_t num_columns,
                             hpx_lmmse** out);
+/* The same estimator with the statistics of `statistics` used as a prior in each
+ * pilot word's tap estimate: (A^H A + ridge_noise diag(1 / P_u))^-1 A^H y instead of
+ * the weighted LS, P_u the prior tap powers, and the per-tap noise of that estimate
+ * in the LMMSE over words. With design statistics (a uniform profile over a delay
+ * window, a design Doppler, the prior noise of a design SNR) this is the robust LMMSE
+ * of Li, Cimini and Sollenberger (IEEE Trans. Commun. 46(7), 1998), which needs no
+ * knowledge of the channel's taps; the plain LS step is ill-conditioned on such a
+ * dense delay grid when the band is partly occupied. No counterpart in the
+ * reference (engine extension); ridge_noise = 0 is hpx_lmmse_create. */
+hpx_status hpx_lmmse_create_regularized(const hpx_frame* frame, const hpx_fading* statistics, int32_t num_columns,
+                                        double ridge_noise, hpx_lmmse** out);
 hpx_status hpx_lmmse_destroy(hpx_lmmse* lmmse);
 /* grid[B][Nrx][num_words][grid_columns], noise_power[B] (per element) ->
  * H[B][Nrx][Ntx][num_words][num_columns]. */

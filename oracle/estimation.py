@@ -125,8 +125,14 @@ def tap_statistics(config: fading.FadingConfig, fs: float, N: int) -> tuple[np.n
 
 
 def tap_lmmse_estimate(layout: FrameLayout, grids: np.ndarray, config: fading.FadingConfig, fs: float,
-                       noise_variance: float, num_tx: int) -> np.ndarray:
-    """(Nrx, words, N) received grids -> (Nrx, Ntx, words, N) LMMSE channel estimate."""
+                       noise_variance: float, num_tx: int, ridge_noise: float = 0.0) -> np.ndarray:
+    """(Nrx, words, N) received grids -> (Nrx, Ntx, words, N) LMMSE channel estimate.
+
+    ``ridge_noise`` > 0 regularizes each pilot word's tap estimate with the profile of
+    ``config`` as prior, (A^H A + ridge_noise diag(1 / P_u))^-1 A^H y, and takes the
+    per-tap noise variance of that estimate as noise_variance diag(M^-1 A^H A M^-1):
+    the robust (design-statistics) estimator, whose dense delay grid makes A^H A
+    ill-conditioned on a partly occupied band."""
 
     N = layout.N
     delays, P, rho = tap_statistics(config, fs, N)
@@ -146,9 +152,14 @@ def tap_lmmse_estimate(layout: FrameLayout, grids: np.ndarray, config: fading.Fa
         for pi, w in enumerate(words):
             sel = rw == w
             A = pilots[sel][:, None] * F_all[rc[sel]]  # (n_p, U)
-            inv = np.linalg.inv(A.conj().T @ A)
-            G = inv @ A.conj().T  # weighted LS of the tap gains
-            e[pi] = noise_variance * np.real(np.diag(inv))
+            AhA = A.conj().T @ A
+            if ridge_noise > 0:
+                inv = np.linalg.inv(AhA + np.diag(ridge_noise / np.maximum(P, 1e-300)))
+                e[pi] = noise_variance * np.real(np.diag(inv @ AhA @ inv))
+            else:
+                inv = np.linalg.inv(AhA)
+                e[pi] = noise_variance * np.real(np.diag(inv))
+            G = inv @ A.conj().T  # (regularized) weighted LS of the tap gains
             for r in range(grids.shape[0]):
                 g_ls[r, pi] = G @ grids[r, w, rc[sel]]
         taps = np.zeros((grids.shape[0], W, U), dtype=np.complex128)

@@ -43,6 +43,8 @@ class LinkConfig:
     equalizer: str = "zf"        # "zf" | "lmmse"
     noise: str = "ebn0"          # "ebn0" | "snr"
     cnn_params: np.ndarray | None = None  # parameter vector of the learned estimator
+    estimation_channel: fading.FadingConfig | None = None  # statistics the LMMSE estimator assumes (default: true)
+    estimation_ridge: float = 0.0  # design noise variance regularizing the estimator's tap LS (0: plain LS)
 
 
 def noise_power(cfg: LinkConfig, layout: FrameLayout, level_db: float) -> float:
@@ -96,7 +98,8 @@ def simulate_drop(cfg: LinkConfig, seed: int, drop: int, level_db: float, keep: 
             U = layout.num_used
             H[..., :U] = cnn.refine(cfg.cnn_params, H[..., :U])
     elif cfg.estimator == "lmmse":
-        H = estimation.tap_lmmse_estimate(layout, grids, cfg.channel, fs, p, cfg.num_tx)
+        stats = cfg.estimation_channel if cfg.estimation_channel is not None else cfg.channel
+        H = estimation.tap_lmmse_estimate(layout, grids, stats, fs, p, cfg.num_tx, cfg.estimation_ridge)
     else:
         H = estimation.ideal_csi(layout, sample, fs)
     lap("estimate")

@@ -83,3 +83,16 @@ def mimo_channel(fs: float = 30.72e6) -> ofad.FadingConfig:
 
     k = np.arange(23)
     return ofad.FadingConfig(k * 50e-9, 10 ** (-0.04 * k), np.zeros(23), 20, 500.0)
+
+
+def robust_design(cfg: ofad.FadingConfig, fs: float, num_delays: int = 64, doppler: float = 1000.0,
+                  design_snr_db: float = 20.0) -> tuple[ofad.FadingConfig, float]:
+    """Statistics of the robust (non-genie) tap-domain LMMSE estimator: a uniform
+    profile over `num_delays` sample delays carrying the channel's expected energy,
+    design Doppler `doppler`, and the prior noise variance of `design_snr_db`
+    (hermespy_gb300.estimation.robust_statistics). Returns (design config, ridge)."""
+
+    energy = cfg.gain * float(np.sum(cfg.power_profile))
+    k = np.arange(num_delays)
+    design = ofad.FadingConfig(k / fs, np.full(num_delays, energy / num_delays), np.zeros(num_delays), 20, doppler)
+    return design, energy * 10.0 ** (-design_snr_db / 10.0)

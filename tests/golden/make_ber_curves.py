@@ -16,10 +16,13 @@ ber_mimo.npz    4x4 1024/600 data-only frame, 64-QAM, 23-tap Rayleigh (500 Hz, 3
                 MHz), ideal CSI, SNR U[0, 30] dB, 256 drops: the reference's drop with
                 ZF (its nearest equalizer) and the oracle's with ZF and with LMMSE.
 ber_pilot.npz   4x4 1024/600 pilot-comb frame (words 0 and 7, comb 4), 64-QAM, same
-                channel, SNR U[0, 30] dB, 512 drops, LMMSE detection after the three
-                estimators of the learned-vs-LMMSE comparison: tap-domain LMMSE,
-                per-stream LS, and LS refined by the shipped CNN weights (oracle drops;
-                the reference has none of the three). Records the weights' SHA-256.
+                channel, SNR U[0, 30] dB, 512 drops, LMMSE detection after the four
+                estimators of the learned-vs-LMMSE comparison: tap-domain LMMSE with the
+                channel's statistics, the same with the robust design statistics
+                (uniform profile over 64 delays, 1000 Hz, tap estimates regularized at a
+                20 dB design SNR), per-stream LS, and LS refined
+                by the shipped CNN weights (oracle drops; the reference has none of
+                them). Records the weights' SHA-256.
 uneven.npz      40 drops of the uneven-batch distribution (antennas {1,2,4,8}^2,
                 FFT 128..2048, 4/7/14 words, 4..256-QAM, 1-23 taps), including the
                 8x8 / 2048-point / 256-QAM and 1x1 / 128-point / 4-QAM corners, ideal
@@ -118,11 +121,13 @@ def work(task):
         cfg, _ = _mimo_cfg(name[5:])
         seed = MIMO_SEED
     elif name.startswith("pilot_"):
-        from configs import mimo_channel, pilot_frame
+        from configs import mimo_channel, pilot_frame, robust_design
 
         est = name[6:]
         params = np.load(WEIGHTS)["params"] if est == "learned" else None
-        cfg = LinkConfig(pilot_frame(), mimo_channel(30.72e6), 30.72e6, 4, 4, est, "lmmse", "snr", cnn_params=params)
+        design, ridge = robust_design(mimo_channel(30.72e6), 30.72e6) if est == "lmmse_robust" else (None, 0.0)
+        cfg = LinkConfig(pilot_frame(), mimo_channel(30.72e6), 30.72e6, 4, 4, "lmmse" if design else est, "lmmse",
+                         "snr", cnn_params=params, estimation_channel=design, estimation_ridge=ridge)
         seed = PILOT_SEED
     else:  # uneven
         from oracle.fading import FadingConfig
@@ -186,7 +191,7 @@ def make_pilot(pool):
     drops = np.arange(PILOT_DROPS)
     snr = snr_draws(PILOT_SEED + 1, PILOT_DROPS)
     out = {}
-    for est in ("lmmse", "ls", "learned"):
+    for est in ("lmmse", "lmmse_robust", "ls", "learned"):
         e, pw = run(pool, "oracle", "pilot_" + est, drops, snr, 8)
         out[f"{est}_errors"] = e.astype(np.uint32)
     with open(WEIGHTS, "rb") as f:

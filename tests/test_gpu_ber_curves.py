@@ -90,11 +90,12 @@ def test_config2_mimo_ideal_csi(golden, equalizer):
     check_interval(errs, cpu, errs.size * int(z["bits_per_drop"]), what=equalizer)
 
 
-@pytest.mark.parametrize("estimator", ["lmmse", "ls", "learned"])
+@pytest.mark.parametrize("estimator", ["lmmse", "lmmse_robust", "ls", "learned"])
 def test_headline_pilot_link_estimators(golden, estimator):
     """The learned-vs-LMMSE workload: 4x4 pilot-comb 1024/600, 64-QAM, SNR U[0, 30] dB,
-    512 drops; tap-domain LMMSE (the fused tensor-core receiver), per-stream LS and LS
-    + CNN, each with LMMSE detection, against the oracle's drops."""
+    512 drops; tap-domain LMMSE with the channel's statistics and with the robust design
+    statistics (both the fused tensor-core receiver), per-stream LS and LS + CNN, each
+    with LMMSE detection, against the oracle's drops."""
 
     z = golden("ber_pilot.npz")
     wpath = os.path.join(WEIGHTS_DIR, "cnn_4x4_1024.npz")

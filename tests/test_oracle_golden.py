@@ -189,8 +189,9 @@ def test_ber_fixtures_match_their_inputs(golden):
     with open(os.path.join(ROOT, "hermespy_gb300", "weights", "cnn_4x4_1024.npz"), "rb") as f:
         assert hashlib.sha256(f.read()).hexdigest() == str(p["weights_sha256"])
     n = 512 * 172800
-    ber = {k: p[f"{k}_errors"].astype(np.int64).sum() / n for k in ("lmmse", "ls", "learned")}
+    ber = {k: p[f"{k}_errors"].astype(np.int64).sum() / n for k in ("lmmse", "lmmse_robust", "ls", "learned")}
     assert ber["lmmse"] < ber["learned"] < ber["ls"]
+    assert ber["lmmse"] < ber["lmmse_robust"] < ber["ls"]  # design statistics cost accuracy, still beat LS
     u = golden("uneven.npz")
     fields = ("num_rx", "num_tx", "fft_size", "num_words", "modulation_order", "num_taps", "tap_decay_db",
               "doppler_frequency", "snr_db")
