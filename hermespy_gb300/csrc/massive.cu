@@ -7,12 +7,19 @@
 // Per resource element with H (NRX x 16) and y (NRX):
 //   P = [Re H; Im H] (2 NRX x 16), Q = [Im H; -Re H], Y = [[Re y, Im y]; [Im y, -Re y]]
 //   Re(H^H H) = P^T P,  Im(H^H H) = P^T Q,  H^H y = P^T Y   (K = 2 NRX real GEMMs)
-// Every operand is split X = X_hi + X_lo into two BF16 numbers and each product is
-// X_hi Y_hi + X_hi Y_lo + X_lo Y_hi with FP32 accumulation (mma.sync m16n8k16): the
-// dropped X_lo Y_lo term is below 2^-16 of the product.
+// Every operand is split X = X_hi + X_lo into two BF16 numbers and each Gram product
+// is X_hi Y_hi + X_hi Y_lo + X_lo Y_hi with FP32 accumulation (mma.sync m16n8k16): the
+// dropped X_lo Y_lo term is below 2^-16 of the product. The matched filter keeps all
+// four terms: Y_hi and Y_lo sit side by side in one 8-column B tile, so two MMAs per
+// k-step give them.
 // The warp computes the Gram of two elements, then each half-warp factors one of
-// them with its 16 rows in registers (lane i holds row i), solves, demaps its 16
-// streams and counts errors against the regenerated Philox bits.
+// them with its 16 rows in registers (lane i holds row i; packed FP32x2 updates),
+// solves (forward substitution on rows, backward on columns after a transpose through
+// shared memory), demaps its 16 streams and counts errors against the Philox bits,
+// regenerated per element.
+// The split operands are built per element from the channel h = g S (tap response g
+// of the element, spatial matrix S of the drop): each lane forms 8 columns of one row,
+// converts them two at a time (BF16x2 and its residual) and writes 16-byte chunks.
 #include <cuda_bf16.h>
 
 #include "fading_dev.cuh"
@@ -56,20 +63,6 @@ __device__ __forceinline__ uint32_t neg2(uint32_t v) { return v ^ 0x80008000u; }
 // halves swap on every other group of 4 rows (conflict-free 8-row ldmatrix).
 __device__ __forceinline__ int toff(int row, int col) {
   return row * 32 + ((((col >> 3) ^ (row >> 2)) & 1) << 4) + (col & 7) * 2;
-}
-
-__device__ __forceinline__ void split_bf16(float v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-  hi = __float2bfloat16_rn(v);
-  lo = __float2bfloat16_rn(v - __bfloat162float(hi));
-}
-
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
-  __nv_bfloat162 t;
-  t.x = a;
-  t.y = b;
-  uint32_t u;
-  memcpy(&u, &t, sizeof(u));
-  return u;
 }
 
 // Serial FP64 Cholesky solve of (G + reg I) x = b for one element whose FP32
@@ -119,22 +112,60 @@ __device__ bool solve_fp64(double2* L, const double2* b, double reg, float2* x) 
   return true;
 }
 
-// Per-warp shared memory: [P_hi | P_lo] (reused for the FP64 Gram and matched
-// filter of the two elements once the FP32 ones are formed), Y, G[2][16][17] (rows
-// padded: a half-warp reading one row per lane hits distinct banks), b[2][16],
-// x[2][16], Cholesky column broadcast [2][16], g[2], column[2].
+// Stream bits of one data element, MSB first (the layout extract_bits_msb reads from
+// staged words: stream bit p is bit p % 32 of word p / 32, four words per Philox
+// block), generated on demand: the lane keeps the last Philox block it made, which
+// serves the following elements of its stream until their bits move past it.
+struct BitCache {
+  int64_t blk = -1;
+  uint4 cur = make_uint4(0u, 0u, 0u, 0u);
+};
+
+__device__ __forceinline__ uint32_t element_bits(BitCache& bc, uint64_t seed, int64_t drop, uint32_t stream, int64_t pos,
+                                                 int m) {
+  const int64_t blk = pos >> 7;
+  if (blk != bc.blk) {
+    bc.cur = hpx_random_block(seed, drop, stream, HPX_DOMAIN_BITS, (uint32_t)blk);
+    bc.blk = blk;
+  }
+  const int off = (int)(pos & 127), wi = off >> 5, sh = off & 31;
+  const uint32_t w0 = wi == 0 ? bc.cur.x : (wi == 1 ? bc.cur.y : (wi == 2 ? bc.cur.z : bc.cur.w));
+  uint32_t w1 = wi == 0 ? bc.cur.y : (wi == 1 ? bc.cur.z : bc.cur.w);
+  if (wi == 3) w1 = sh + m > 32 ? hpx_random_block(seed, drop, stream, HPX_DOMAIN_BITS, (uint32_t)(blk + 1)).x : 0u;
+  const uint64_t win = (uint64_t)w0 | ((uint64_t)w1 << 32);
+  const uint32_t raw = (uint32_t)(win >> sh) & ((1u << m) - 1u);
+  return __brev(raw) >> (32 - m);
+}
+
+// Two floats as a BF16 pair (hi) and the pair of their rounding residuals (lo).
+__device__ __forceinline__ void split2_bf16(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+  memcpy(&hi, &h, sizeof(hi));
+  memcpy(&lo, &l, sizeof(lo));
+}
+
+// Per-warp shared memory: [P_hi | P_lo] (reused for the FP64 Gram of the two elements
+// once the FP32 ones are formed), Y [KR][8] (16-byte rows: columns 0-1 hi, 2-3 lo,
+// 4-7 zero), G[2][16][17] (rows padded: a half-warp reading one row per lane hits
+// distinct banks; reused to transpose L), b[2][16], x[2][16] (FP64-path results),
+// Cholesky column broadcast [2][16] as (re, re, im, im) (reused for the FP64 matched
+// filter), g[2], column[2].
 template <int NRX>
 struct MassiveSmem {
   static constexpr int KR = 2 * NRX;        // stacked real rows
   static constexpr int TILE = KR * 16 * 2;  // bytes of one [KR][16] bf16 tile
-  static constexpr int FP64 = 2 * MT * MT * 16 + 2 * MT * 16;
-  static constexpr int UNION = 2 * TILE > FP64 ? 2 * TILE : FP64;
-  static constexpr int WARP_BYTES = UNION + TILE + 2 * MT * (MT + 1) * 8 + 2 * MT * 8 + 2 * MT * 8 + 2 * MT * 8 + 2 * 8 + 2 * 8;
+  static constexpr int UNION = 2 * TILE > 2 * MT * MT * 16 ? 2 * TILE : 2 * MT * MT * 16;
+  static constexpr int YBYTES = KR * 16;
+  static constexpr int WARP_BYTES = UNION + YBYTES + 2 * MT * (MT + 1) * 8 + 2 * MT * 8 + 2 * MT * 8 + 2 * MT * 16 +
+                                    2 * 8 + 2 * 8;
 };
+constexpr int SMS = MT + 2;  // row stride of the spatial matrix in shared memory (144 bytes: conflict-free rows)
 
 // Fused ideal-CSI massive-MIMO receiver, one block (4 warps) per (word, drop).
 template <int NRX>
-__global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
+__global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
     FadingConst fc, FadingView v, int N, int W, int C, int m, const int32_t* __restrict__ window_start,
     const int32_t* __restrict__ data_offset, const int32_t* __restrict__ num_data_word,
     const int32_t* __restrict__ data_column, const int32_t* __restrict__ bins, const float2* __restrict__ tw,
@@ -145,59 +176,41 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
   constexpr int KR = SM::KR, KS = KR / 16;
   extern __shared__ float4 smem4[];
   const int w = blockIdx.x, b = blockIdx.y;
-  const int BW = staged_bit_words(C, m);
   unsigned char* base = reinterpret_cast<unsigned char*>(smem4);
-  unsigned char* wbase = base;  // per-warp areas first (16-byte aligned)
-  float2* hb = reinterpret_cast<float2*>(base + MWARPS * SM::WARP_BYTES);
+  // [NRX][SMS] spatial matrix (16-byte aligned rows), then taps
+  float2* Sm = reinterpret_cast<float2*>(base + MWARPS * SM::WARP_BYTES);
+  float2* hb = Sm + NRX * SMS;
   float2* scratch = hb + fc.L;
-  // [NRX][16], 16-byte aligned for the float4 loads of the fill
-  float2* Sm = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(scratch + fc.L * fc.S1) + 15) & ~uintptr_t(15));
-  int* ds = reinterpret_cast<int*>(Sm + NRX * MT);
-  uint32_t* bitsm = reinterpret_cast<uint32_t*>(ds + fc.L + 4);
+  int* ds = reinterpret_cast<int*>(scratch + fc.L * fc.S1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  unsigned char* my = wbase + warp * SM::WARP_BYTES;
+  unsigned char* my = base + warp * SM::WARP_BYTES;
   unsigned char* Phi = my;
   unsigned char* Plo = my + SM::TILE;
   unsigned char* Yt = my + SM::UNION;
-  constexpr int GS = MT + 1;                                  // padded Gram row
-  float2* Gs = reinterpret_cast<float2*>(my + SM::UNION + SM::TILE);  // [2][16][17]
-  float2* bs = Gs + 2 * MT * GS;                              // [2][16]
-  float2* xs = bs + 2 * MT;                                   // [2][16] FP64-path results
-  float2* colb = xs + 2 * MT;                                 // [2][16] column of L being broadcast
-  float2* gsave = colb + 2 * MT;                              // [2] tap response of each element
-  int* csave = reinterpret_cast<int*>(gsave + 2);             // [2] grid column of each element
+  constexpr int GS = MT + 1;                                               // padded Gram row
+  float2* Gs = reinterpret_cast<float2*>(Yt + SM::YBYTES);                 // [2][16][17]
+  float2* bs = Gs + 2 * MT * GS;                                           // [2][16]
+  float2* xs = bs + 2 * MT;                                                // [2][16] FP64-path results
+  float4* colb = reinterpret_cast<float4*>(xs + 2 * MT);                   // [2][16] (re, re, im, im)
+  float2* gsave = reinterpret_cast<float2*>(colb + 2 * MT);                // [2] tap response of each element
+  int* csave = reinterpret_cast<int*>(gsave + 2);                          // [2] grid column of each element
 
   const int64_t k0 = data_offset[w];
   const int nd = num_data_word[w];
   for (int l = threadIdx.x; l < fc.L; l += blockDim.x) ds[l] = fc.delay[l];
   const float2* Sg = v.spatial(b);
-  for (int i = threadIdx.x; i < NRX * MT; i += blockDim.x) Sm[i] = Sg[i];
-  // zero the Y tiles once: only columns 0, 1 (hi) and 8, 9 (lo) change per element
-  for (int i = lane; i < KR * 8; i += 32) reinterpret_cast<uint32_t*>(Yt)[i] = 0u;
-  // stage the Philox bits of the 16 streams
-  if (nd > 0) {
-    const int64_t blk0 = ((k0 * m) >> 5) >> 2, blk1 = (((k0 + nd) * m - 1) >> 5) >> 2;
-    const int nblk = (int)(blk1 - blk0 + 1);
-    for (int q = threadIdx.x; q < nblk * MT; q += blockDim.x) {
-      const int s = q / nblk;
-      const int64_t blk = blk0 + (q - s * nblk);
-      const uint4 r = hpx_random_block(seed, drop0 + b, (uint32_t)s, HPX_DOMAIN_BITS, (uint32_t)blk);
-      uint32_t* dst = bitsm + s * BW + (blk - blk0) * 4;
-      dst[0] = r.x;
-      dst[1] = r.y;
-      dst[2] = r.z;
-      dst[3] = r.w;
-    }
-  }
+  for (int i = threadIdx.x; i < NRX * MT; i += blockDim.x) Sm[(i / MT) * SMS + i % MT] = Sg[i];
+  // zero the Y tile once: only columns 0-3 change per element
+  for (int i = lane; i < KR * 4; i += 32) reinterpret_cast<uint32_t*>(Yt)[i] = 0u;
   tap_averages(fc, v.W(b), v.P0(b), window_start[w], N, hb, scratch);  // ends with __syncthreads
-  const int64_t wofs = (((k0 * m) >> 5) >> 2) * 4;
   const float s2 = nv ? nv[b] : 0.0f;
   const float reg = mode == HPX_EQ_LMMSE ? s2 : 0.0f;
   const uint32_t phi = smem_u32(Phi), plo = smem_u32(Plo), yt = smem_u32(Yt);
   const int j8 = lane >> 3, r8 = lane & 7;
   const int half = lane >> 4, row = lane & 15;
   unsigned int local = 0, n64 = 0;
+  BitCache bc;
   // a NaN / inf noise power, or an element whose solution (after the FP64 re-solve of
   // ill-conditioned elements) is not finite
   bool bad = !(fabsf(s2) < INFINITY);
@@ -230,6 +243,12 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
       for (int q = 0; q < YR; ++q) ycur[s][q] = ypf[s][q];
     }
     if (j0 + 2 * MWARPS < nd) prefetch(j0 + 2 * MWARPS);
+    // tap responses of both elements at once: lanes 0-15 the first, 16-31 the second
+    const float2 gh = tap_response(fc, hb, ds, tw, bins[half ? ccur[1] : ccur[0]], N);
+    if (row == 0) {
+      gsave[half] = gh;
+      csave[half] = half ? ccur[1] : ccur[0];
+    }
     // ---------------- Gram and matched filter of elements j0 and j0 + 1
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
@@ -242,41 +261,47 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
         __syncwarp();
         continue;
       }
-      const int c = ccur[s];
-      const float2 g = tap_response(fc, hb, ds, tw, bins[c], N);
-      if (lane == 0) {
-        gsave[s] = g;
-        csave[s] = c;
+      const float2 g = make_float2(__shfl_sync(0xffffffffu, gh.x, 16 * s), __shfl_sync(0xffffffffu, gh.y, 16 * s));
+      // P tiles: item = (row r, 8-column half cb); rows r (Re H) and NRX + r (Im H)
+#pragma unroll
+      for (int it = lane; it < 2 * NRX; it += 32) {
+        const int r = it >> 1, cb = it & 1;
+        const float4* sp = reinterpret_cast<const float4*>(Sm + r * SMS + cb * 8);
+        float hr[8], hi[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float4 v4 = sp[q];
+          const float2 h0 = cmul(make_float2(v4.x, v4.y), g), h1 = cmul(make_float2(v4.z, v4.w), g);
+          hr[2 * q] = h0.x;
+          hi[2 * q] = h0.y;
+          hr[2 * q + 1] = h1.x;
+          hi[2 * q + 1] = h1.y;
+        }
+        uint4 rh, rl, ih, il;
+        split2_bf16(hr[0], hr[1], rh.x, rl.x);
+        split2_bf16(hr[2], hr[3], rh.y, rl.y);
+        split2_bf16(hr[4], hr[5], rh.z, rl.z);
+        split2_bf16(hr[6], hr[7], rh.w, rl.w);
+        split2_bf16(hi[0], hi[1], ih.x, il.x);
+        split2_bf16(hi[2], hi[3], ih.y, il.y);
+        split2_bf16(hi[4], hi[5], ih.z, il.z);
+        split2_bf16(hi[6], hi[7], ih.w, il.w);
+        *reinterpret_cast<uint4*>(Phi + toff(r, cb * 8)) = rh;
+        *reinterpret_cast<uint4*>(Plo + toff(r, cb * 8)) = rl;
+        *reinterpret_cast<uint4*>(Phi + toff(NRX + r, cb * 8)) = ih;
+        *reinterpret_cast<uint4*>(Plo + toff(NRX + r, cb * 8)) = il;
       }
-      // P tiles: rows r (Re H) and NRX + r (Im H), two columns per lane and step
-      for (int e = lane; e < NRX * MT / 2; e += 32) {
-        const int r = e >> 3, t = (e & 7) * 2;
-        const float4 sp = *reinterpret_cast<const float4*>(Sm + r * MT + t);  // one 16-byte load, no bank conflicts
-        const float2 h0 = cmul(make_float2(sp.x, sp.y), g), h1 = cmul(make_float2(sp.z, sp.w), g);
-        __nv_bfloat16 a0, a1, b0, b1, c0, c1, d0, d1;
-        split_bf16(h0.x, a0, a1);
-        split_bf16(h1.x, b0, b1);
-        split_bf16(h0.y, c0, c1);
-        split_bf16(h1.y, d0, d1);
-        *reinterpret_cast<uint32_t*>(Phi + toff(r, t)) = pack2(a0, b0);
-        *reinterpret_cast<uint32_t*>(Plo + toff(r, t)) = pack2(a1, b1);
-        *reinterpret_cast<uint32_t*>(Phi + toff(NRX + r, t)) = pack2(c0, d0);
-        *reinterpret_cast<uint32_t*>(Plo + toff(NRX + r, t)) = pack2(c1, d1);
-      }
-      // Y tile: column 0 = [Re y; Im y], column 1 = [Im y; -Re y] (hi in 0-1, lo in 8-9)
+      // Y tile: row r = [Re y, Im y], row NRX + r = [Im y, -Re y]; hi in columns 0-1, lo in 2-3
 #pragma unroll
       for (int q = 0; q < YR; ++q) {
         const int r = lane + 32 * q;
         if (r >= NRX) continue;
         const float2 yv = ycur[s][q];
-        __nv_bfloat16 xr0, xr1, xi0, xi1, nr0, nr1;
-        split_bf16(yv.x, xr0, xr1);
-        split_bf16(yv.y, xi0, xi1);
-        split_bf16(-yv.x, nr0, nr1);
-        *reinterpret_cast<uint32_t*>(Yt + toff(r, 0)) = pack2(xr0, xi0);
-        *reinterpret_cast<uint32_t*>(Yt + toff(r, 8)) = pack2(xr1, xi1);
-        *reinterpret_cast<uint32_t*>(Yt + toff(NRX + r, 0)) = pack2(xi0, nr0);
-        *reinterpret_cast<uint32_t*>(Yt + toff(NRX + r, 8)) = pack2(xi1, nr1);
+        uint32_t h0, l0, h1, l1;
+        split2_bf16(yv.x, yv.y, h0, l0);
+        split2_bf16(yv.y, -yv.x, h1, l1);
+        *reinterpret_cast<uint2*>(Yt + r * 16) = make_uint2(h0, l0);
+        *reinterpret_cast<uint2*>(Yt + (NRX + r) * 16) = make_uint2(h1, l1);
       }
       __syncwarp();
       float gr[2][4] = {}, gi[2][4] = {}, by[4] = {};
@@ -292,14 +317,9 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
           ldsm_x4_t(phi + toff(rr, cc), ah[p][0], ah[p][1], ah[p][2], ah[p][3]);
           ldsm_x4_t(plo + toff(rr, cc), al[p][0], al[p][1], al[p][2], al[p][3]);
         }
-        // Y fragments: matrices (hi, k lo), (hi, k hi), (lo, k lo), (lo, k hi)
-        uint32_t yf[2][4];
-#pragma unroll
-        for (int p = 0; p < 2; ++p) {
-          const int kk = p == 0 ? ks : ks2;
-          const int rr = kk * 16 + (j8 & 1) * 8 + r8, cc = (j8 >> 1) * 8;
-          ldsm_x4_t(yt + toff(rr, cc), yf[p][0], yf[p][1], yf[p][2], yf[p][3]);
-        }
+        // Y fragments of both k-steps: matrices (ks, k 0-7), (ks, k 8-15), (ks2, k 0-7), (ks2, k 8-15)
+        uint32_t yf[4];
+        ldsm_x4_t(yt + ((j8 >> 1 ? ks2 : ks) * 16 + (j8 & 1) * 8 + r8) * 16, yf[0], yf[1], yf[2], yf[3]);
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
           // B = P fragments of the same k-step are the A fragments reordered:
@@ -317,7 +337,9 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
             }
             mma3(gi[nt], ah[p], al[p], qh0, qh1, ql0, ql1);
           }
-          mma3(by, ah[p], al[p], yf[p][0], yf[p][1], yf[p][2], yf[p][3]);
+          // matched filter: (P_hi + P_lo)^T [Y_hi | Y_lo], the lo half summed in below
+          mma16816(by, ah[p][0], ah[p][1], ah[p][2], ah[p][3], yf[2 * p], yf[2 * p + 1]);
+          mma16816(by, al[p][0], al[p][1], al[p][2], al[p][3], yf[2 * p], yf[2 * p + 1]);
         }
       }
       // C fragments: rows lane/4 (+8), columns 2 (lane % 4) (+1) of each 8-column tile
@@ -331,6 +353,9 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
             const int i = gm + hr * 8, jj = nt * 8 + gn + e;
             G[i * GS + jj] = make_float2(gr[nt][hr * 2 + e], gi[nt][hr * 2 + e]);
           }
+      // H^H y: columns 0-1 (Y_hi) of lanes 4i plus columns 2-3 (Y_lo) of lanes 4i + 1
+#pragma unroll
+      for (int e = 0; e < 4; ++e) by[e] += __shfl_down_sync(0xffffffffu, by[e], 1);
       if ((lane & 3) == 0) {
         bv[gm] = make_float2(by[0], by[1]);
         bv[gm + 8] = make_float2(by[2], by[3]);
@@ -341,8 +366,8 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
     // ---------------- FP32 Cholesky solve, one element per half-warp (lane i: row i)
     const int jme = j0 + half;
     const bool valid = jme < nd;
-    const float2* G = Gs + half * MT * GS;
-    float2* col = colb + half * MT;
+    float2* G = Gs + half * MT * GS;
+    float4* col = colb + half * MT;
     float2 a[MT];
 #pragma unroll
     for (int jj = 0; jj < MT; ++jj) {
@@ -352,8 +377,9 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
     float2 bi = bs[half * MT + row];
     float pmin = INFINITY, pmax = 0.f, inv_i = 0.f;
     bool ok = true;
-    // right-looking Cholesky; column k of L goes through shared memory, every loop has
-    // a fixed trip count so that a[] stays in registers
+    // right-looking Cholesky; column k of L goes through shared memory as (re, re, im, im)
+    // so that each update a[jj] -= l_ik conj(l_jk) is two packed FMAs; every loop has a
+    // fixed trip count so that a[] stays in registers
 #pragma unroll
     for (int k = 0; k < MT; ++k) {
       const float dkk = __shfl_sync(0xffffffffu, a[k].x, k, 16);
@@ -365,20 +391,21 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
       if (row == k) inv_i = ik;
       const float2 lik = row > k ? cscale(a[k], ik) : (row == k ? make_float2(pk, 0.f) : make_float2(0.f, 0.f));
       a[k] = lik;
-      col[row] = lik;
+      col[row] = make_float4(lik.x, lik.x, lik.y, lik.y);
       __syncwarp();
+      const float2 n0 = make_float2(-lik.x, -lik.y), n1 = make_float2(-lik.y, lik.x);
 #pragma unroll
       for (int jj = 0; jj < MT; ++jj) {
         if (jj <= k) continue;
-        const float2 ljk = col[jj];
-        if (row >= jj) {  // a[jj] -= lik conj(ljk)
-          a[jj].x -= lik.x * ljk.x + lik.y * ljk.y;
-          a[jj].y -= lik.y * ljk.x - lik.x * ljk.y;
+        const float4 c = col[jj];
+        if (row >= jj) {
+          a[jj] = __ffma2_rn(n0, make_float2(c.x, c.y), a[jj]);
+          a[jj] = __ffma2_rn(n1, make_float2(c.z, c.w), a[jj]);
         }
       }
       __syncwarp();
     }
-    // forward: L z = b
+    // forward: L z = b (lane i holds row i of L)
     float2 zi = make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < MT; ++k) {
@@ -387,18 +414,22 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
       if (row == k) zi = zk;
       if (row > k) bi = csub(bi, cmul(a[k], zk));
     }
-    // backward: L^H x = z
-    float2 xi = make_float2(0.f, 0.f);
+    // backward: L^H x = z with lane i holding column i of L (transposed through G):
+    // once x_p is known every lane i < p subtracts conj(L[p][i]) x_p from its sum
 #pragma unroll
-    for (int k = MT - 1; k >= 0; --k) {
-      float2 t = row > k ? cmulc(a[k], xi) : make_float2(0.f, 0.f);  // conj(L[row][k]) x_row
+    for (int p = 0; p < MT; ++p) G[row * GS + p] = a[p];
+    __syncwarp();
 #pragma unroll
-      for (int o = 8; o > 0; o >>= 1) {
-        t.x += __shfl_xor_sync(0xffffffffu, t.x, o, 16);
-        t.y += __shfl_xor_sync(0xffffffffu, t.y, o, 16);
-      }
-      if (row == k) xi = cscale(csub(zi, t), inv_i);
+    for (int p = 0; p < MT; ++p) a[p] = G[p * GS + row];
+    float2 acc = make_float2(0.f, 0.f), xi = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int p = MT - 1; p >= 0; --p) {
+      const float2 xl = cscale(csub(zi, acc), inv_i);
+      const float2 xp = make_float2(__shfl_sync(0xffffffffu, xl.x, p, 16), __shfl_sync(0xffffffffu, xl.y, p, 16));
+      if (row == p) xi = xp;
+      if (row < p) acc = cadd(acc, cmulc(a[p], xp));
     }
+    __syncwarp();  // G reads done before the next element pair's Gram
     const bool cond_bad = !ok || pmax * pmax > kCondLimit * pmin * pmin;  // (pmax / pmin)^2 > 1e6
     const unsigned need = __ballot_sync(0xffffffffu, valid && cond_bad && row == 0);
     if (need) {
@@ -406,26 +437,26 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
       // (lane i: row i), then a serial FP64 Cholesky solve on the half's first lane
       const bool mine = (need >> (16 * half)) & 1u;
       double2* G64 = reinterpret_cast<double2*>(Phi) + half * MT * MT;  // P tiles are free now
-      double2* b64 = reinterpret_cast<double2*>(Phi) + 2 * MT * MT + half * MT;
+      double2* b64 = reinterpret_cast<double2*>(colb) + half * MT;      // so is the column broadcast
       if (mine) {
         const float2 gg = gsave[half];
         const int cc = csave[half];
         double2 bacc = make_double2(0.0, 0.0);
         for (int r = 0; r < NRX; ++r) {
-          const float2 hi = cmul(Sm[r * MT + row], gg);
+          const float2 hi = cmul(Sm[r * SMS + row], gg);
           const float2 yv = grid[(((int64_t)b * NRX + r) * W + w) * gcols + cc];
           bacc.x += (double)hi.x * yv.x + (double)hi.y * yv.y;  // conj(h) y
           bacc.y += (double)hi.x * yv.y - (double)hi.y * yv.x;
         }
         b64[row] = bacc;
         for (int jj = 0; jj <= row; ++jj) {
-          double2 acc = make_double2(0.0, 0.0);
+          double2 acc64 = make_double2(0.0, 0.0);
           for (int r = 0; r < NRX; ++r) {
-            const float2 hi = cmul(Sm[r * MT + row], gg), hj = cmul(Sm[r * MT + jj], gg);
-            acc.x += (double)hi.x * hj.x + (double)hi.y * hj.y;  // conj(h_i) h_j
-            acc.y += (double)hi.x * hj.y - (double)hi.y * hj.x;
+            const float2 hi = cmul(Sm[r * SMS + row], gg), hj = cmul(Sm[r * SMS + jj], gg);
+            acc64.x += (double)hi.x * hj.x + (double)hi.y * hj.y;  // conj(h_i) h_j
+            acc64.y += (double)hi.x * hj.y - (double)hi.y * hj.x;
           }
-          G64[row * MT + jj] = acc;
+          G64[row * MT + jj] = acc64;
         }
       }
       __syncwarp();
@@ -443,7 +474,7 @@ __global__ void __launch_bounds__(MWARPS * 32, 1) k_detect_massive(
       bad = bad || !(fabsf(xi.x) < INFINITY && fabsf(xi.y) < INFINITY);
       const int64_t k = k0 + jme;
       const uint32_t rx_v = qam_decide(qt, xi);
-      const uint32_t tx_v = extract_bits_msb(bitsm + row * BW - wofs, k * m, m);
+      const uint32_t tx_v = element_bits(bc, seed, drop0 + b, (uint32_t)row, k * m, m);
       local += __popc(rx_v ^ tx_v);
       if (equalized) equalized[((int64_t)b * MT + row) * num_data + k] = xi;
     }
@@ -470,9 +501,8 @@ hpx_status launch_massive(const hpx_fading* f, const void* state, const hpx_fram
   HPX_TRY(qam_demap_table(fr->info.modulation_order, &qt));
   const FadingConst fc = fading_const(f);
   const int C = fr->info.num_columns, m = fr->info.bits_per_symbol;
-  const size_t smem = (size_t)MWARPS * MassiveSmem<NRX>::WARP_BYTES + (size_t)fc.L * sizeof(float2) * (1 + fc.S1) +
-                      (size_t)NRX * MT * sizeof(float2) + 16 + (fc.L + 4) * sizeof(int) +
-                      (size_t)MT * staged_bit_words(C, m) * 4 + 16;
+  const size_t smem = (size_t)MWARPS * MassiveSmem<NRX>::WARP_BYTES + (size_t)NRX * SMS * sizeof(float2) +
+                      (size_t)fc.L * sizeof(float2) * (1 + fc.S1) + (size_t)fc.L * sizeof(int);
   if (smem > 220 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_massive: frame needs %zu bytes of shared memory", smem);
   auto kern = k_detect_massive<NRX>;
   HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
