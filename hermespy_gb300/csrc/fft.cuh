@@ -29,12 +29,14 @@ __host__ __device__ constexpr float cos32_base(int t) {
        : t == 7 ? 0.19509032368659973f
        : 0.0f;
 }
-__host__ __device__ constexpr float cos32(int t) {
-  return (t & 31) >= 16 ? -cos32((t & 31) - 16) : ((t & 31) > 8 ? -cos32_base(16 - (t & 31)) : cos32_base(t & 31));
+// Not recursive, so that every call inlines and folds: cos of the quarter-turn
+// reduction u -> r in [0, 8] with the sign of the half-turn, sin(x) = cos(x - pi / 2).
+__host__ __device__ __forceinline__ constexpr float cos32(int t) {
+  const int u = t & 31;
+  const int r = u <= 8 ? u : (u < 16 ? 16 - u : (u <= 24 ? u - 16 : 32 - u));
+  return (u > 8 && u < 24) ? -cos32_base(r) : cos32_base(r);
 }
-__host__ __device__ constexpr float sin32(int t) {
-  return (t & 31) >= 16 ? -sin32((t & 31) - 16) : ((t & 31) <= 8 ? cos32_base(8 - (t & 31)) : cos32_base((t & 31) - 8));
-}
+__host__ __device__ __forceinline__ constexpr float sin32(int t) { return cos32(t - 8); }
 
 // v * exp(-+2 pi i t / 32) with the sign of the exponent set by INV.
 template <bool INV>

@@ -40,7 +40,8 @@ static void release(hpx_frame* f) {
   if (!f) return;
   void* ptrs[] = {f->d_prefix, f->d_zero_prefix, f->d_word_start, f->d_window_start, f->d_data_offset,
                   f->d_num_data_word, f->d_kind, f->d_index, f->d_bins, f->d_data_column, f->d_data_word,
-                  f->d_twiddle, f->d_stage_twiddle, f->d_pilots, f->d_bin_code, f->d_constellation};
+                  f->d_twiddle, f->d_stage_twiddle, f->d_pilots, f->d_bin_code, f->d_constellation,
+                  f->d_tx_src, f->d_tx_regular, f->d_tx_bitoff, f->d_constellation_lsb};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete f;
@@ -193,6 +194,40 @@ hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out) {
       else if (k == HPX_RE_REFERENCE) bin_code[(size_t)w * N + f->h_bins[c]] = ~idx;
     }
 
+  // Transmitter descriptors (see hpx_frame): the staged bits of word w start at Philox
+  // block (k0 m) / 128, so data element k sits at bit (k - k0) m + (k0 m) mod 128.
+  if (nr >= (1 << 24)) {
+    release(f);
+    return hpx_fail(HPX_ERR_ARG, "frame: too many reference elements");
+  }
+  std::vector<int32_t> tx_src((size_t)W * N, -1), tx_regular(W, 0), tx_bitoff(W, 0);
+  const int comb = desc->pilot_comb;
+  for (int w = 0; w < W; ++w) {
+    const int64_t k0 = f->h_data_offset[w];
+    const int32_t off0 = (int32_t)((k0 * m) & 127);
+    bool regular = true;
+    for (int c = 0; c < C; ++c) {
+      const int8_t k = f->h_kind[(size_t)w * C + c];
+      const int32_t idx = f->h_index[(size_t)w * C + c];
+      int32_t& dst = tx_src[(size_t)w * N + f->h_bins[c]];
+      if (k == HPX_RE_DATA) {
+        dst = (int32_t)((idx - k0) * m) + off0;
+        regular = regular && idx == k0 + c;
+      } else {
+        regular = false;
+        if (k == HPX_RE_REFERENCE) dst = -2 - ((idx << 6) | (comb > 1 ? c % comb : 0));
+      }
+    }
+    tx_regular[w] = regular ? 1 : 0;
+    tx_bitoff[w] = off0;
+  }
+  std::vector<float2> constellation_lsb(desc->modulation_order);
+  for (int raw = 0; raw < desc->modulation_order; ++raw) {
+    uint32_t v = 0;
+    for (int i = 0; i < m; ++i) v |= (((uint32_t)raw >> i) & 1u) << (m - 1 - i);
+    constellation_lsb[raw] = constellation[v];
+  }
+
   hpx_status s = HPX_OK;
   if ((s = upload(&f->d_prefix, f->h_prefix)) != HPX_OK ||
       (s = upload(&f->d_zero_prefix, f->h_zero_prefix)) != HPX_OK ||
@@ -204,7 +239,9 @@ hpx_status hpx_frame_create(const hpx_frame_desc* desc, hpx_frame** out) {
       (s = upload(&f->d_bins, f->h_bins)) != HPX_OK || (s = upload(&f->d_data_column, data_column)) != HPX_OK ||
       (s = upload(&f->d_data_word, data_word)) != HPX_OK || (s = upload(&f->d_twiddle, tw)) != HPX_OK || (s = upload(&f->d_stage_twiddle, stw)) != HPX_OK ||
       (s = upload(&f->d_pilots, pilots)) != HPX_OK || (s = upload(&f->d_bin_code, bin_code)) != HPX_OK ||
-      (s = upload(&f->d_constellation, constellation)) != HPX_OK) {
+      (s = upload(&f->d_constellation, constellation)) != HPX_OK || (s = upload(&f->d_tx_src, tx_src)) != HPX_OK ||
+      (s = upload(&f->d_tx_regular, tx_regular)) != HPX_OK || (s = upload(&f->d_tx_bitoff, tx_bitoff)) != HPX_OK ||
+      (s = upload(&f->d_constellation_lsb, constellation_lsb)) != HPX_OK) {
     release(f);
     return s;
   }

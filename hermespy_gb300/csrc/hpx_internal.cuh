@@ -165,6 +165,14 @@ struct hpx_frame {
   float2* d_pilots = nullptr;          // [num_refs]
   int32_t* d_bin_code = nullptr;       // [W * N] per (word, FFT bin): data index, ~pilot index, or INT32_MIN (null)
   float2* d_constellation = nullptr;   // [M] symbols in MSB-first bit-value order
+  // transmitter from Philox bits (k_ofdm_tx): per (word, bin) the bit offset of a data
+  // element within the word's staged words, -2 - (reference index * 64 + comb phase) for
+  // a reference element, -1 for nothing; per word 1 if its columns are data elements in
+  // column order (then the offset is column * m + word bit offset) and that bit offset
+  int32_t* d_tx_src = nullptr;         // [W * N]
+  int32_t* d_tx_regular = nullptr;     // [W]
+  int32_t* d_tx_bitoff = nullptr;      // [W] (first data index * m) mod 128
+  float2* d_constellation_lsb = nullptr;  // [M] symbols by LSB-first bit value (bit-reversed index)
 };
 
 // ------------------------------------------------------------ fading state

@@ -137,11 +137,12 @@ __device__ __forceinline__ uint32_t element_bits(BitCache& bc, uint64_t seed, in
   return __brev(raw) >> (32 - m);
 }
 
-// Two floats as a BF16 pair (hi) and the pair of their rounding residuals (lo).
-__device__ __forceinline__ void split2_bf16(float a, float b, uint32_t& hi, uint32_t& lo) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-  const float2 hf = __bfloat1622float2(h);
-  const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+// Two floats as a BF16 pair (hi) and the pair of their rounding residuals (lo); the
+// residual v - hi is exact in FP32 and formed by one packed FMA.
+__device__ __forceinline__ void split2_bf16(float2 v, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __float22bfloat162_rn(v);
+  const float2 r = __ffma2_rn(__bfloat1622float2(h), make_float2(-1.f, -1.f), v);
+  const __nv_bfloat162 l = __float22bfloat162_rn(r);
   memcpy(&hi, &h, sizeof(hi));
   memcpy(&lo, &l, sizeof(lo));
 }
@@ -161,7 +162,9 @@ struct MassiveSmem {
   static constexpr int WARP_BYTES = UNION + YBYTES + 2 * MT * (MT + 1) * 8 + 2 * MT * 8 + 2 * MT * 8 + 2 * MT * 16 +
                                     2 * 8 + 2 * 8;
 };
-constexpr int SMS = MT + 2;  // row stride of the spatial matrix in shared memory (144 bytes: conflict-free rows)
+// Spatial matrix in shared memory as planes per row: 16 real parts, 16 imaginary parts,
+// 4 floats of padding (144-byte rows: conflict-free 16-byte loads by rows)
+constexpr int SMF = 2 * MT + 4;
 
 // Fused ideal-CSI massive-MIMO receiver, one block (4 warps) per (word, drop).
 template <int NRX>
@@ -177,9 +180,9 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
   extern __shared__ float4 smem4[];
   const int w = blockIdx.x, b = blockIdx.y;
   unsigned char* base = reinterpret_cast<unsigned char*>(smem4);
-  // [NRX][SMS] spatial matrix (16-byte aligned rows), then taps
-  float2* Sm = reinterpret_cast<float2*>(base + MWARPS * SM::WARP_BYTES);
-  float2* hb = Sm + NRX * SMS;
+  // [NRX][SMF] spatial matrix (16-byte aligned rows), then taps
+  float* Sm = reinterpret_cast<float*>(base + MWARPS * SM::WARP_BYTES);
+  float2* hb = reinterpret_cast<float2*>(Sm + NRX * SMF);
   float2* scratch = hb + fc.L;
   int* ds = reinterpret_cast<int*>(scratch + fc.L * fc.S1);
 
@@ -200,7 +203,11 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
   const int nd = num_data_word[w];
   for (int l = threadIdx.x; l < fc.L; l += blockDim.x) ds[l] = fc.delay[l];
   const float2* Sg = v.spatial(b);
-  for (int i = threadIdx.x; i < NRX * MT; i += blockDim.x) Sm[(i / MT) * SMS + i % MT] = Sg[i];
+  for (int i = threadIdx.x; i < NRX * MT; i += blockDim.x) {
+    const float2 sv = Sg[i];
+    Sm[(i / MT) * SMF + i % MT] = sv.x;
+    Sm[(i / MT) * SMF + MT + i % MT] = sv.y;
+  }
   // zero the Y tile once: only columns 0-3 change per element
   for (int i = lane; i < KR * 4; i += 32) reinterpret_cast<uint32_t*>(Yt)[i] = 0u;
   tap_averages(fc, v.W(b), v.P0(b), window_start[w], N, hb, scratch);  // ends with __syncthreads
@@ -261,31 +268,35 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
         __syncwarp();
         continue;
       }
-      const float2 g = make_float2(__shfl_sync(0xffffffffu, gh.x, 16 * s), __shfl_sync(0xffffffffu, gh.y, 16 * s));
-      // P tiles: item = (row r, 8-column half cb); rows r (Re H) and NRX + r (Im H)
+      const float gx = __shfl_sync(0xffffffffu, gh.x, 16 * s), gy = __shfl_sync(0xffffffffu, gh.y, 16 * s);
+      const float2 gx2 = make_float2(gx, gx), gy2 = make_float2(gy, gy), ngy2 = make_float2(-gy, -gy);
+      // P tiles: item = (row r, 8-column half cb); rows r (Re H) and NRX + r (Im H). Two
+      // columns per packed FMA: Re h = Re s gx - Im s gy, Im h = Re s gy + Im s gx.
 #pragma unroll
       for (int it = lane; it < 2 * NRX; it += 32) {
         const int r = it >> 1, cb = it & 1;
-        const float4* sp = reinterpret_cast<const float4*>(Sm + r * SMS + cb * 8);
-        float hr[8], hi[8];
+        const float4* rp = reinterpret_cast<const float4*>(Sm + r * SMF + cb * 8);
+        const float4* ip = reinterpret_cast<const float4*>(Sm + r * SMF + MT + cb * 8);
+        float2 hr[4], hi[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const float4 v4 = sp[q];
-          const float2 h0 = cmul(make_float2(v4.x, v4.y), g), h1 = cmul(make_float2(v4.z, v4.w), g);
-          hr[2 * q] = h0.x;
-          hi[2 * q] = h0.y;
-          hr[2 * q + 1] = h1.x;
-          hi[2 * q + 1] = h1.y;
+        for (int q = 0; q < 2; ++q) {
+          const float4 sr = rp[q], si = ip[q];
+          const float2 sr0 = make_float2(sr.x, sr.y), sr1 = make_float2(sr.z, sr.w);
+          const float2 si0 = make_float2(si.x, si.y), si1 = make_float2(si.z, si.w);
+          hr[2 * q] = __ffma2_rn(si0, ngy2, __fmul2_rn(sr0, gx2));
+          hr[2 * q + 1] = __ffma2_rn(si1, ngy2, __fmul2_rn(sr1, gx2));
+          hi[2 * q] = __ffma2_rn(si0, gx2, __fmul2_rn(sr0, gy2));
+          hi[2 * q + 1] = __ffma2_rn(si1, gx2, __fmul2_rn(sr1, gy2));
         }
         uint4 rh, rl, ih, il;
-        split2_bf16(hr[0], hr[1], rh.x, rl.x);
-        split2_bf16(hr[2], hr[3], rh.y, rl.y);
-        split2_bf16(hr[4], hr[5], rh.z, rl.z);
-        split2_bf16(hr[6], hr[7], rh.w, rl.w);
-        split2_bf16(hi[0], hi[1], ih.x, il.x);
-        split2_bf16(hi[2], hi[3], ih.y, il.y);
-        split2_bf16(hi[4], hi[5], ih.z, il.z);
-        split2_bf16(hi[6], hi[7], ih.w, il.w);
+        split2_bf16(hr[0], rh.x, rl.x);
+        split2_bf16(hr[1], rh.y, rl.y);
+        split2_bf16(hr[2], rh.z, rl.z);
+        split2_bf16(hr[3], rh.w, rl.w);
+        split2_bf16(hi[0], ih.x, il.x);
+        split2_bf16(hi[1], ih.y, il.y);
+        split2_bf16(hi[2], ih.z, il.z);
+        split2_bf16(hi[3], ih.w, il.w);
         *reinterpret_cast<uint4*>(Phi + toff(r, cb * 8)) = rh;
         *reinterpret_cast<uint4*>(Plo + toff(r, cb * 8)) = rl;
         *reinterpret_cast<uint4*>(Phi + toff(NRX + r, cb * 8)) = ih;
@@ -298,8 +309,8 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
         if (r >= NRX) continue;
         const float2 yv = ycur[s][q];
         uint32_t h0, l0, h1, l1;
-        split2_bf16(yv.x, yv.y, h0, l0);
-        split2_bf16(yv.y, -yv.x, h1, l1);
+        split2_bf16(yv, h0, l0);
+        split2_bf16(make_float2(yv.y, -yv.x), h1, l1);
         *reinterpret_cast<uint2*>(Yt + r * 16) = make_uint2(h0, l0);
         *reinterpret_cast<uint2*>(Yt + (NRX + r) * 16) = make_uint2(h1, l1);
       }
@@ -309,37 +320,44 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
       for (int ks = 0; ks < KS / 2; ++ks) {
         const int ks2 = ks + KS / 2;
         // A = P^T fragments of k-steps ks (rows of Re H) and ks2 (rows of Im H)
-        uint32_t ah[2][4], al[2][4];
+        // and the same matrices in B order (a0, a2, a1, a3): the B pair of n-tile nt is
+        // registers 2 nt, 2 nt + 1 of it, consecutive as the MMA wants them
+        uint32_t bh[2][4], bl[2][4];
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
           const int kk = p == 0 ? ks : ks2;
-          const int rr = kk * 16 + (j8 >> 1) * 8 + r8, cc = (j8 & 1) * 8;
-          ldsm_x4_t(phi + toff(rr, cc), ah[p][0], ah[p][1], ah[p][2], ah[p][3]);
-          ldsm_x4_t(plo + toff(rr, cc), al[p][0], al[p][1], al[p][2], al[p][3]);
+          const int rb = kk * 16 + (j8 & 1) * 8 + r8, cb2 = (j8 >> 1) * 8;
+          ldsm_x4_t(phi + toff(rb, cb2), bh[p][0], bh[p][1], bh[p][2], bh[p][3]);
+          ldsm_x4_t(plo + toff(rb, cb2), bl[p][0], bl[p][1], bl[p][2], bl[p][3]);
         }
         // Y fragments of both k-steps: matrices (ks, k 0-7), (ks, k 8-15), (ks2, k 0-7), (ks2, k 8-15)
         uint32_t yf[4];
         ldsm_x4_t(yt + ((j8 >> 1 ? ks2 : ks) * 16 + (j8 & 1) * 8 + r8) * 16, yf[0], yf[1], yf[2], yf[3]);
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
-          // B = P fragments of the same k-step are the A fragments reordered:
-          // n-tile nt, k-half kb <- A register (m-block nt, k-half kb) = index nt + 2 kb
+          uint32_t ah[4], al[4];  // A order, loaded per k-step to keep registers down
+          {
+            const int rr = (p == 0 ? ks : ks2) * 16 + (j8 >> 1) * 8 + r8, cc = (j8 & 1) * 8;
+            ldsm_x4_t(phi + toff(rr, cc), ah[0], ah[1], ah[2], ah[3]);
+            ldsm_x4_t(plo + toff(rr, cc), al[0], al[1], al[2], al[3]);
+          }
+          // B = P fragments of the same k-step (B order), Q those of the partner k-step
           const int q = 1 - p;  // Q = [Im H; -Re H]: the partner k-step, negated in the lower half
 #pragma unroll
           for (int nt = 0; nt < 2; ++nt) {
-            mma3(gr[nt], ah[p], al[p], ah[p][nt], ah[p][nt + 2], al[p][nt], al[p][nt + 2]);
-            uint32_t qh0 = ah[q][nt], qh1 = ah[q][nt + 2], ql0 = al[q][nt], ql1 = al[q][nt + 2];
+            mma3(gr[nt], ah, al, bh[p][2 * nt], bh[p][2 * nt + 1], bl[p][2 * nt], bl[p][2 * nt + 1]);
+            uint32_t qh0 = bh[q][2 * nt], qh1 = bh[q][2 * nt + 1], ql0 = bl[q][2 * nt], ql1 = bl[q][2 * nt + 1];
             if (p == 1) {
               qh0 = neg2(qh0);
               qh1 = neg2(qh1);
               ql0 = neg2(ql0);
               ql1 = neg2(ql1);
             }
-            mma3(gi[nt], ah[p], al[p], qh0, qh1, ql0, ql1);
+            mma3(gi[nt], ah, al, qh0, qh1, ql0, ql1);
           }
           // matched filter: (P_hi + P_lo)^T [Y_hi | Y_lo], the lo half summed in below
-          mma16816(by, ah[p][0], ah[p][1], ah[p][2], ah[p][3], yf[2 * p], yf[2 * p + 1]);
-          mma16816(by, al[p][0], al[p][1], al[p][2], al[p][3], yf[2 * p], yf[2 * p + 1]);
+          mma16816(by, ah[0], ah[1], ah[2], ah[3], yf[2 * p], yf[2 * p + 1]);
+          mma16816(by, al[0], al[1], al[2], al[3], yf[2 * p], yf[2 * p + 1]);
         }
       }
       // C fragments: rows lane/4 (+8), columns 2 (lane % 4) (+1) of each 8-column tile
@@ -393,6 +411,8 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
       a[k] = lik;
       col[row] = make_float4(lik.x, lik.x, lik.y, lik.y);
       __syncwarp();
+      // (the predicate keeps the scheduler from hoisting every column load of the step:
+      // without it the factorization spills)
       const float2 n0 = make_float2(-lik.x, -lik.y), n1 = make_float2(-lik.y, lik.x);
 #pragma unroll
       for (int jj = 0; jj < MT; ++jj) {
@@ -405,14 +425,15 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
       }
       __syncwarp();
     }
-    // forward: L z = b (lane i holds row i of L)
+    // forward: L z = b (lane i holds row i of L). Every lane updates: L[i][k] = 0 for
+    // i < k, and lane k's own value is not read after step k.
     float2 zi = make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < MT; ++k) {
       const float2 zl = cscale(bi, inv_i);
       const float2 zk = make_float2(__shfl_sync(0xffffffffu, zl.x, k, 16), __shfl_sync(0xffffffffu, zl.y, k, 16));
       if (row == k) zi = zk;
-      if (row > k) bi = csub(bi, cmul(a[k], zk));
+      bi = csub(bi, cmul(a[k], zk));
     }
     // backward: L^H x = z with lane i holding column i of L (transposed through G):
     // once x_p is known every lane i < p subtracts conj(L[p][i]) x_p from its sum
@@ -427,7 +448,7 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
       const float2 xl = cscale(csub(zi, acc), inv_i);
       const float2 xp = make_float2(__shfl_sync(0xffffffffu, xl.x, p, 16), __shfl_sync(0xffffffffu, xl.y, p, 16));
       if (row == p) xi = xp;
-      if (row < p) acc = cadd(acc, cmulc(a[p], xp));
+      acc = cadd(acc, cmulc(a[p], xp));  // L[p][i] = 0 for i > p; lane p's sum is not read after step p
     }
     __syncwarp();  // G reads done before the next element pair's Gram
     const bool cond_bad = !ok || pmax * pmax > kCondLimit * pmin * pmin;  // (pmax / pmin)^2 > 1e6
@@ -443,7 +464,7 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
         const int cc = csave[half];
         double2 bacc = make_double2(0.0, 0.0);
         for (int r = 0; r < NRX; ++r) {
-          const float2 hi = cmul(Sm[r * SMS + row], gg);
+          const float2 hi = cmul(make_float2(Sm[r * SMF + row], Sm[r * SMF + MT + row]), gg);
           const float2 yv = grid[(((int64_t)b * NRX + r) * W + w) * gcols + cc];
           bacc.x += (double)hi.x * yv.x + (double)hi.y * yv.y;  // conj(h) y
           bacc.y += (double)hi.x * yv.y - (double)hi.y * yv.x;
@@ -452,7 +473,8 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
         for (int jj = 0; jj <= row; ++jj) {
           double2 acc64 = make_double2(0.0, 0.0);
           for (int r = 0; r < NRX; ++r) {
-            const float2 hi = cmul(Sm[r * SMS + row], gg), hj = cmul(Sm[r * SMS + jj], gg);
+            const float2 hi = cmul(make_float2(Sm[r * SMF + row], Sm[r * SMF + MT + row]), gg);
+            const float2 hj = cmul(make_float2(Sm[r * SMF + jj], Sm[r * SMF + MT + jj]), gg);
             acc64.x += (double)hi.x * hj.x + (double)hi.y * hj.y;  // conj(h_i) h_j
             acc64.y += (double)hi.x * hj.y - (double)hi.y * hj.x;
           }
@@ -501,7 +523,7 @@ hpx_status launch_massive(const hpx_fading* f, const void* state, const hpx_fram
   HPX_TRY(qam_demap_table(fr->info.modulation_order, &qt));
   const FadingConst fc = fading_const(f);
   const int C = fr->info.num_columns, m = fr->info.bits_per_symbol;
-  const size_t smem = (size_t)MWARPS * MassiveSmem<NRX>::WARP_BYTES + (size_t)NRX * SMS * sizeof(float2) +
+  const size_t smem = (size_t)MWARPS * MassiveSmem<NRX>::WARP_BYTES + (size_t)NRX * SMF * sizeof(float) +
                       (size_t)fc.L * sizeof(float2) * (1 + fc.S1) + (size_t)fc.L * sizeof(int);
   if (smem > 220 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_massive: frame needs %zu bytes of shared memory", smem);
   auto kern = k_detect_massive<NRX>;

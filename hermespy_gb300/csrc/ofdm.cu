@@ -28,6 +28,10 @@ struct FrameDev {
   const float2* pilots;
   const int32_t* bin_code;
   const float2* constellation;
+  const int32_t* tx_src;
+  const int32_t* tx_regular;
+  const int32_t* tx_bitoff;
+  const float2* constellation_lsb;
 };
 
 FrameDev frame_dev(const hpx_frame* f) {
@@ -57,6 +61,10 @@ FrameDev frame_dev(const hpx_frame* f) {
   d.pilots = f->d_pilots;
   d.bin_code = f->d_bin_code;
   d.constellation = f->d_constellation;
+  d.tx_src = f->d_tx_src;
+  d.tx_regular = f->d_tx_regular;
+  d.tx_bitoff = f->d_tx_bitoff;
+  d.constellation_lsb = f->d_constellation_lsb;
   return d;
 }
 
@@ -77,12 +85,13 @@ constexpr int groups_per_block() {
 // item / num_streams, stream item % num_streams; MODE 2: a placed grid `data`
 // [items][W][G] with G = num_streams columns.
 // Resident CTAs per SM the FFT kernels are compiled for: the transforms are latency
-// bound, so the 128-thread CTAs of N <= 2048 take a register cap (72 transmit / 80
-// receive) at a few bytes of spill; the 256-thread CTAs of N = 4096 keep 85 registers.
+// bound, so the 128-thread CTAs of N <= 2048 take a 64-register cap (8 CTAs per SM),
+// without spills: for 8 192 drops of the 1024-point 4x4 link that measured 2 % (transmit)
+// and 5 % (receive) faster than 7 and 6 CTAs; the 256-thread CTAs of N = 4096 keep 85.
 template <int N>
-constexpr int tx_min_blocks() { return fft::Plan<N>::TP * groups_per_block<N>() >= 256 ? 3 : 7; }
+constexpr int tx_min_blocks() { return fft::Plan<N>::TP * groups_per_block<N>() >= 256 ? 3 : 8; }
 template <int N>
-constexpr int rx_min_blocks() { return fft::Plan<N>::TP * groups_per_block<N>() >= 256 ? 3 : 6; }
+constexpr int rx_min_blocks() { return fft::Plan<N>::TP * groups_per_block<N>() >= 256 ? 3 : 8; }
 
 template <int N, int MODE>
 __global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), tx_min_blocks<N>())
@@ -102,7 +111,6 @@ __global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), tx_m
   const int item = valid ? p / fr.W : 0, w = valid ? p - item * fr.W : 0;
   const bool dc = fr.dc != 0;
   const float scale = rsqrtf((float)N);
-  int64_t wofs = 0;
   if (MODE == 1 && valid) {
     const int drop = item / num_streams, s = item - drop * num_streams;
     const int64_t k0 = fr.data_offset[w];
@@ -117,31 +125,51 @@ __global__ void __launch_bounds__(fft::Plan<N>::TP * groups_per_block<N>(), tx_m
         dst[2] = r.z;
         dst[3] = r.w;
       }
-      wofs = blk0 * 4;
     }
   }
+  // MODE 1: the constellation by LSB-first bit value, scaled, in shared memory
   if (MODE == 1) {
-    for (int i = threadIdx.x; i < fr.order; i += blockDim.x) cons[i] = fr.constellation[i];
+    for (int i = threadIdx.x; i < fr.order; i += blockDim.x) cons[i] = cscale(fr.constellation_lsb[i], scale);
     __syncthreads();
   }
-  const uint32_t* words = bits - wofs;
   const int32_t* codes = fr.bin_code + (int64_t)w * N;
+  const int32_t* srcs = fr.tx_src + (int64_t)w * N;
   // stream of this item (MODE 1: items are (drop, stream); MODE 0: stream 0)
   const int stream = MODE == 1 ? item % num_streams : 0;
+  const int phase = fr.comb > 1 ? stream % fr.comb : 0;
+  const bool regular = MODE == 1 && valid && fr.tx_regular[w] != 0;
+  const int bitoff = MODE == 1 && valid ? fr.tx_bitoff[w] : 0;
+  const uint32_t mask = (1u << fr.m) - 1u;
+  // symbol of the m staged bits at bit offset d (LSB-first window, so no bit reversal)
+  auto symbol = [&](int d) -> float2 {
+    const int wi = d >> 5;
+    return cons[__funnelshift_r(bits[wi], bits[wi + 1], d & 31) & mask];
+  };
   auto load = [&](int b) -> float2 {
     if (!valid) return make_float2(0.f, 0.f);
     float2 v = make_float2(0.f, 0.f);
     if (MODE == 2) {
       const int c = column_of_bin(b, N, dc);
       if (c < num_streams) v = data[(int64_t)p * num_streams + c];
-    } else {
-      const int32_t code = __ldg(codes + b);
-      if (code >= 0) {
-        if (MODE == 0) v = data[(int64_t)item * fr.num_data + code];
-        else v = cons[extract_bits_msb(words, (int64_t)code * fr.m, fr.m)];
-      } else if (code != INT32_MIN) {
-        if (fr.comb <= 1 || column_of_bin(b, N, dc) % fr.comb == stream % fr.comb) v = fr.pilots[~code];
+      return cscale(v, scale);
+    }
+    if (MODE == 1) {
+      if (regular) {  // every column a data element in column order: no table lookup
+        const int c = column_of_bin(b, N, dc);
+        return c < fr.C ? symbol(c * fr.m + bitoff) : v;
       }
+      const int32_t d = __ldg(srcs + b);
+      if (d >= 0) return symbol(d);
+      if (d != -1) {
+        const int q = -2 - d;  // reference index * 64 + comb phase of its column
+        if (fr.comb <= 1 || (q & 63) == phase) v = cscale(fr.pilots[q >> 6], scale);
+      }
+      return v;
+    }
+    const int32_t code = __ldg(codes + b);
+    if (code >= 0) v = data[(int64_t)item * fr.num_data + code];
+    else if (code != INT32_MIN) {
+      if (fr.comb <= 1 || column_of_bin(b, N, dc) % fr.comb == stream % fr.comb) v = fr.pilots[~code];
     }
     return cscale(v, scale);
   };

@@ -35,7 +35,8 @@ struct UFrame {  // device view of one frame configuration
   const float2* stage_twiddle;
   const float2* twiddle;
   const int32_t* bins;
-  const float2* constellation;
+  const float2* constellation;      // MSB-first bit value order
+  const float2* constellation_lsb;  // LSB-first bit value order (bit-reversed index)
 };
 
 struct UDrop {  // one drop of the batch
@@ -127,12 +128,16 @@ __device__ void u_tx(const UFrame& fr, int ntx, uint64_t seed, int64_t drop, flo
         dst[3] = r.w;
       }
     __syncthreads();
-    const uint32_t* words = bits - blk0 * 4;
+    // data element k0 + c sits at bit c m + (k0 m) mod 128 of the staged words; the
+    // LSB-first window indexes the bit-reversed constellation directly
+    const int off0 = (int)((k0 * fr.m) & 127);
+    const uint32_t mask = (1u << fr.m) - 1u;
     auto load = [&](int b) -> float2 {
       if (!valid) return make_float2(0.f, 0.f);
       const int c = column_of_bin_u(b, N);
       if (c >= fr.C) return make_float2(0.f, 0.f);
-      const float2 v = __ldg(fr.constellation + extract_bits_msb(words, (k0 + c) * fr.m, fr.m));
+      const int d = c * fr.m + off0, wi = d >> 5;
+      const float2 v = __ldg(fr.constellation_lsb + (__funnelshift_r(bits[wi], bits[wi + 1], d & 31) & mask));
       return cscale(v, scale);
     };
     float2* dst = x + (int64_t)s * fr.T + (int64_t)w * (N + fr.cp);
@@ -646,6 +651,7 @@ hpx_status hpx_uneven_create(const hpx_uneven_drop* drops, int32_t num_drops, do
       v.twiddle = f->d_twiddle;
       v.bins = f->d_bins;
       v.constellation = f->d_constellation;
+      v.constellation_lsb = f->d_constellation_lsb;
       hf.push_back(v);
       if (!u->qts.t[m].order) {
         const hpx_status s2 = qam_demap_table(q.modulation_order, &u->qts.t[m]);
