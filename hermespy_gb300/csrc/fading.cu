@@ -214,7 +214,7 @@ template <int NTX, int K, bool DIRECT, int XS = 0, int PPT = 2, int BT = tile_le
           int PTHREADS = tile_len<NTX>() / (2 * PPT)>
 __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(FadingConst fc, FadingView v, int T, const float2* __restrict__ x,
                                                         float2* __restrict__ y, const float* __restrict__ noise_power,
-                                                        uint64_t seed, int64_t drop0) {
+                                                        const __grid_constant__ PhiloxKeys nk, int64_t drop0) {
   extern __shared__ float4 smem4[];
   const int b = blockIdx.y;
   const int m0 = blockIdx.x * BT;
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(PTHREADS, PPT == 1 ? 2 : 3) k_propagate(Fading
       const int m = m0 + jp[pr];
       if (noise_power && np > 0.0f) {
         // complex sample k of antenna rx: block k/2, words (0,1) for even k, (2,3) for odd k
-        const uint4 w = hpx_random_block(seed, drop0 + b, (uint32_t)rx, HPX_DOMAIN_NOISE, (uint32_t)(m >> 1));
+        const uint4 w = hpx_random_block_k(nk, drop0 + b, (uint32_t)rx, HPX_DOMAIN_NOISE, (uint32_t)(m >> 1));
         const float2 n0 = box_muller(w.x, w.y);
         const float2 n1 = box_muller(w.z, w.w);
         ore = __ffma2_rn(make_float2(sigma, sigma), make_float2(n0.x, n1.x), ore);
@@ -494,7 +494,7 @@ hpx_status launch_propagate(const hpx_fading* f, const void* state, int B, const
   const int TD = T + fc.D;
   dim3 grid((TD + BT - 1) / BT, B);
   kern<<<grid, BT / (2 * PPT), smem, s>>>(fc, v, T, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(y),
-                                          np, seed, drop0);
+                                          np, philox_keys(seed), drop0);
   HPX_LAUNCHED("propagate");
   return HPX_OK;
 }

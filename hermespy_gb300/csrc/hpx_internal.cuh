@@ -95,6 +95,40 @@ __host__ __device__ __forceinline__ uint4 hpx_random_block(uint64_t seed, int64_
   return philox4x32_10(c, make_uint2((uint32_t)(seed & 0xFFFFFFFFu), (uint32_t)(seed >> 32)));
 }
 
+// Round keys of one seed (k0 + r W0, k1 + r W1 for the ten rounds), computed on the
+// host and passed by value, so that a kernel drawing many blocks with one seed reads
+// them as constant operands instead of re-deriving the key schedule in every block.
+struct PhiloxKeys {
+  uint32_t k[20];
+};
+
+static inline PhiloxKeys philox_keys(uint64_t seed) {
+  PhiloxKeys r;
+  uint32_t k0 = (uint32_t)(seed & 0xFFFFFFFFu), k1 = (uint32_t)(seed >> 32);
+  for (int i = 0; i < 10; ++i) {
+    r.k[2 * i] = k0;
+    r.k[2 * i + 1] = k1;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return r;
+}
+
+// hpx_random_block with the seed's round keys (same values).
+__device__ __forceinline__ uint4 hpx_random_block_k(const PhiloxKeys& rk, int64_t drop, uint32_t stream_id,
+                                                   uint32_t domain, uint32_t block) {
+  const uint64_t d = (uint64_t)drop;
+  uint4 c = make_uint4(block, stream_id, (uint32_t)(d & 0xFFFFFFFFu),
+                       (domain & 0xFFu) | ((uint32_t)((d >> 32) & 0xFFFFFFu) << 8));
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), hi1 = __umulhi(0xCD9E8D57u, c.z);
+    const uint32_t lo0 = 0xD2511F53u * c.x, lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ rk.k[2 * i], lo1, hi0 ^ c.w ^ rk.k[2 * i + 1], lo0);
+  }
+  return c;
+}
+
 __host__ __device__ __forceinline__ uint32_t uint4_get(const uint4& v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
