@@ -13,16 +13,20 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 // ---------------------------------------------------------------- parameters
 // One block per drop. MODE 0: draws from the Philox stream (domain 2);
 // MODE 1: explicit angles / phases / spatial response from device arrays.
-// MODE 0 with `staged`: the drop's uniforms (nrx ntx + 2 L + 2 L S of them) are drawn
-// once into shared memory, one Philox block per four, instead of one block per draw.
+// MODE 0 with `staged`: the drop's drawn words (nrx ntx + 2 L + 2 L S of them) are
+// drawn once into shared memory, one Philox block per four, instead of one block per
+// draw. MODE 0 forms the initial phases exactly from the drawn words and, with
+// `fp32_rates` (rates within kFp32RateLimit), the rates in FP32 (cospif; see
+// rate_to_fixed), so its FP64 work is the spatial response alone; MODE 1 (explicit
+// angles) and faster channels stay in FP64.
 template <int MODE>
 __global__ void k_fading_params(FadingConst fc, double nlos_rate, double los_rate, uint64_t seed, int64_t drop0,
                                 const double* __restrict__ la, const double* __restrict__ na,
                                 const double* __restrict__ lp, const double* __restrict__ np_,
                                 const double* __restrict__ sp_in, const double* __restrict__ rxc,
                                 const double* __restrict__ txc, unsigned char* state, size_t stride, size_t off_w,
-                                size_t off_p0, size_t off_sp, int staged) {
-  extern __shared__ double2 sps[];  // [nrx*ntx] spatial, then [nrx*ntx] temp, then the staged uniforms
+                                size_t off_p0, size_t off_sp, int staged, int fp32_rates) {
+  extern __shared__ double2 sps[];  // [nrx*ntx] spatial, then [nrx*ntx] temp, then the staged words
   const int b = blockIdx.x;
   const int64_t drop = drop0 + b;
   const int L = fc.L, S = fc.S, S1 = fc.S1, nrx = fc.nrx, ntx = fc.ntx;
@@ -31,7 +35,7 @@ __global__ void k_fading_params(FadingConst fc, double nlos_rate, double los_rat
   int64_t* Wout = reinterpret_cast<int64_t*>(base + off_w);
   int64_t* Pout = reinterpret_cast<int64_t*>(base + off_p0);
   float2* Sout = reinterpret_cast<float2*>(base + off_sp);
-  double* ud = reinterpret_cast<double*>(sps + 2 * nsp);
+  uint32_t* uw = reinterpret_cast<uint32_t*>(sps + 2 * nsp);
   if (MODE == 0 && staged) {
     const int num = nsp + 2 * L + 2 * L * S;
     for (int blk = threadIdx.x; blk < (num + 3) >> 2; blk += blockDim.x) {
@@ -39,46 +43,51 @@ __global__ void k_fading_params(FadingConst fc, double nlos_rate, double los_rat
       const uint32_t wv[4] = {r.x, r.y, r.z, r.w};
 #pragma unroll
       for (int i = 0; i < 4; ++i)
-        if (4 * blk + i < num) ud[4 * blk + i] = u01_f64(wv[i]);
+        if (4 * blk + i < num) uw[4 * blk + i] = wv[i];
     }
     __syncthreads();
   }
 
-  auto uniform = [&](int idx) -> double {
-    if (staged) return ud[idx];
+  auto word = [&](int idx) -> uint32_t {
+    if (staged) return uw[idx];
     const uint4 r = hpx_random_block(seed, drop, 0u, HPX_DOMAIN_FADING, (uint32_t)(idx >> 2));
-    return u01_f64(uint4_get(r, idx & 3));
+    return uint4_get(r, idx & 3);
   };
+  auto uniform = [&](int idx) -> double { return u01_f64(word(idx)); };
 
   // Drawn angles enter as turns: theta = -pi + 2 pi u gives (2 pi (n + 1) + theta) / S
-  // = pi (2 n + 1 + 2 u) / S and phi / (2 pi) = u - 1/2, so the FP64 work per sinusoid
-  // is one cospi and no division.
-  const double inv_s = 1.0 / (double)(S > 0 ? S : 1);
+  // = pi (2 n + 1 + 2 u) / S and phi / (2 pi) = u - 1/2: one cospif per sinusoid for its
+  // rate, the phase straight from the drawn word.
   constexpr double kInv2Pi = 0.15915494309189535;
+  const double inv_s = 1.0 / (double)(S > 0 ? S : 1);
+  const float inv_sf = 1.0f / (float)(S > 0 ? S : 1);
+  const float rate_n = (float)(nlos_rate * kInv2Pi), rate_l = (float)(los_rate * kInv2Pi);
+  // (w + 1/2) 2^-32 in FP32
+  auto u01 = [](uint32_t w) { return fmaf(__uint2float_rn(w), 2.3283064365386963e-10f, 1.1641532182693481e-10f); };
   for (int q = threadIdx.x; q < L * S1; q += blockDim.x) {
     const int l = q / S1, n = q - l * S1;
-    double omega, turns;
-    if (n < S) {
-      if (MODE == 0) {
-        const double ut = uniform(nsp + L + l * S + n);
-        omega = nlos_rate * cospi((2.0 * n + 1.0 + 2.0 * ut) * inv_s);
-        turns = uniform(nsp + 2 * L + L * S + l * S + n) - 0.5;
-      } else {
+    if (MODE == 0) {
+      const uint32_t wu = n < S ? word(nsp + L + l * S + n) : word(nsp + l);
+      if (fp32_rates)
+        Wout[q] = n < S ? rate_to_fixed(rate_n * cospif(((float)(2 * n + 1) + 2.0f * u01(wu)) * inv_sf))
+                        : rate_to_fixed(rate_l * cospif(2.0f * u01(wu)));
+      else
+        Wout[q] = turns_to_fixed(kInv2Pi * (n < S ? nlos_rate * cospi((2.0 * n + 1.0 + 2.0 * u01_f64(wu)) * inv_s)
+                                                  : los_rate * cospi(2.0 * u01_f64(wu))));
+      Pout[q] = phase_from_word(n < S ? word(nsp + 2 * L + L * S + l * S + n) : word(nsp + L + L * S + l));
+    } else {
+      double omega, turns;
+      if (n < S) {
         const double theta = na[((int64_t)b * L + l) * S + n];
         omega = nlos_rate * cos((2.0 * kPi * (n + 1) + theta) / (double)S);
         turns = np_[((int64_t)b * L + l) * S + n] * kInv2Pi;
-      }
-    } else {
-      if (MODE == 0) {
-        omega = los_rate * cospi(2.0 * uniform(nsp + l));
-        turns = uniform(nsp + L + L * S + l) - 0.5;
       } else {
         omega = los_rate * cos(la[(int64_t)b * L + l]);
         turns = lp[(int64_t)b * L + l] * kInv2Pi;
       }
+      Wout[q] = turns_to_fixed(omega * kInv2Pi);
+      Pout[q] = turns_to_fixed(turns);
     }
-    Wout[q] = turns_to_fixed(omega * kInv2Pi);
-    Pout[q] = turns_to_fixed(turns);
   }
   for (int j = threadIdx.x; j < nsp; j += blockDim.x) {
     if (MODE == 0) {
@@ -666,14 +675,15 @@ static hpx_status launch_params(const hpx_fading* f, int mode, uint64_t seed, in
   const double nlos_rate = f->doppler / f->fs, los_rate = f->los_doppler / f->fs;
   if (mode == 0) {
     const size_t draws = (size_t)f->nrx * f->ntx + 2 * (size_t)f->L + 2 * (size_t)f->L * f->S;
-    const int staged = smem0 + draws * sizeof(double) <= 32 * 1024 ? 1 : 0;
-    const size_t smem = smem0 + (staged ? draws * sizeof(double) : 0);
+    const int staged = smem0 + draws * sizeof(uint32_t) <= 32 * 1024 ? 1 : 0;
+    const size_t smem = smem0 + (staged ? draws * sizeof(uint32_t) : 0);
     if (smem > 48 * 1024)
       HPX_CUDA(cudaFuncSetAttribute(k_fading_params<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_fading_params<0><<<B, 128, smem, as_stream(stream)>>>(fc, nlos_rate, los_rate, seed, drop0, nullptr, nullptr,
                                                             nullptr, nullptr, nullptr, f->d_rx_corr, f->d_tx_corr,
                                                             static_cast<unsigned char*>(state), f->stride, f->off_w,
-                                                            f->off_p0, f->off_spatial, staged);
+                                                            f->off_p0, f->off_spatial, staged,
+                                                            std::fmax(std::fabs(nlos_rate), std::fabs(los_rate)) * 0.15915494309189535 <= kFp32RateLimit);
   } else {
     const size_t smem = smem0;
     if ((!la || !lp) || (f->S > 0 && (!na || !np_)) || !sp) return hpx_fail(HPX_ERR_ARG, "fading_load: null array");
@@ -682,7 +692,7 @@ static hpx_status launch_params(const hpx_fading* f, int mode, uint64_t seed, in
     // explicit spatial responses are used as given (the caller applied any correlation)
     k_fading_params<1><<<B, 128, smem, as_stream(stream)>>>(fc, nlos_rate, los_rate, 0, 0, la, na, lp, np_, sp, nullptr,
                                                             nullptr, static_cast<unsigned char*>(state), f->stride,
-                                                            f->off_w, f->off_p0, f->off_spatial, 0);
+                                                            f->off_w, f->off_p0, f->off_spatial, 0, 0);
   }
   HPX_LAUNCHED("fading_params");
   return HPX_OK;

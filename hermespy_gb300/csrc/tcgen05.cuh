@@ -67,7 +67,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 // Wait for the phase with parity `parity` to complete; gives up after `max_cycles`
-// SM clock cycles and returns false.
+// SM clock cycles and returns false. Each try_wait may suspend the thread for up to
+// 100 us (it resumes as soon as the phase completes), so a wait costs one or two
+// polls instead of a spin of several.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long max_cycles) {
   const uint32_t a = smem_u32(bar);
   const long long t0 = clock64();
@@ -75,10 +77,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(done)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "r"(100000u)
         : "memory");
     if (done) return true;
   }

@@ -74,25 +74,27 @@ __device__ __forceinline__ int column_of_bin_u(int b, int N) {  // DC suppressio
 // Fading realization of drop `drop` (the homogeneous k_fading_params, no correlation).
 __device__ void u_realize(const UDrop& d, int S, uint64_t seed, int64_t drop, int64_t* Wp, int64_t* P0, float2* Sm) {
   const int L = d.L, S1 = S + 1, nsp = d.nrx * d.ntx;
-  auto uniform = [&](int idx) -> double {
+  auto word = [&](int idx) -> uint32_t {
     const uint4 r = hpx_random_block(seed, drop, 0u, HPX_DOMAIN_FADING, (uint32_t)(idx >> 2));
-    return u01_f64(uint4_get(r, idx & 3));
+    return uint4_get(r, idx & 3);
   };
-  const double inv_s = 1.0 / (double)(S > 0 ? S : 1);
+  auto uniform = [&](int idx) -> double { return u01_f64(word(idx)); };
+  auto u01 = [](uint32_t w) { return fmaf(__uint2float_rn(w), 2.3283064365386963e-10f, 1.1641532182693481e-10f); };
   constexpr double kInv2Pi = 0.15915494309189535;
+  const double inv_s = 1.0 / (double)(S > 0 ? S : 1);
+  const float inv_sf = 1.0f / (float)(S > 0 ? S : 1);
+  const float rate_n = (float)(d.nlos_rate * kInv2Pi), rate_l = (float)(d.los_rate * kInv2Pi);
+  const bool fp32_rates = fmax(fabs(d.nlos_rate), fabs(d.los_rate)) * kInv2Pi <= kFp32RateLimit;
   for (int q = threadIdx.x; q < L * S1; q += blockDim.x) {  // the same arithmetic as k_fading_params<0>
     const int l = q / S1, n = q - l * S1;
-    double omega, turns;
-    if (n < S) {
-      const double ut = uniform(nsp + L + l * S + n);
-      omega = d.nlos_rate * cospi((2.0 * n + 1.0 + 2.0 * ut) * inv_s);
-      turns = uniform(nsp + 2 * L + L * S + l * S + n) - 0.5;
-    } else {
-      omega = d.los_rate * cospi(2.0 * uniform(nsp + l));
-      turns = uniform(nsp + L + L * S + l) - 0.5;
-    }
-    Wp[q] = turns_to_fixed(omega * kInv2Pi);
-    P0[q] = turns_to_fixed(turns);
+    const uint32_t wu = n < S ? word(nsp + L + l * S + n) : word(nsp + l);
+    if (fp32_rates)
+      Wp[q] = n < S ? rate_to_fixed(rate_n * cospif(((float)(2 * n + 1) + 2.0f * u01(wu)) * inv_sf))
+                    : rate_to_fixed(rate_l * cospif(2.0f * u01(wu)));
+    else
+      Wp[q] = turns_to_fixed(kInv2Pi * (n < S ? d.nlos_rate * cospi((2.0 * n + 1.0 + 2.0 * u01_f64(wu)) * inv_s)
+                                              : d.los_rate * cospi(2.0 * u01_f64(wu))));
+    P0[q] = phase_from_word(n < S ? word(nsp + 2 * L + L * S + l * S + n) : word(nsp + L + L * S + l));
   }
   for (int j = threadIdx.x; j < nsp; j += blockDim.x) {
     double s, c;
