@@ -180,7 +180,8 @@ __device__ void u_rx(const UFrame& fr, int nrx, int TD, const float2* y, float2*
 }
 
 // Propagation with AWGN (k_propagate: the same tiles, Taylor terms, FMA order and
-// noise streams; any transmit count up to 8, every thread a set of sample pairs).
+// noise streams; any transmit count up to MAXA, every thread a set of sample pairs).
+template <int MAXA>
 __device__ void u_propagate(const UDrop& d, const FadingConst& fc, int T, const int64_t* Wp, const int64_t* P0,
                             const float2* Sm, const int* dl, const float2* x, float2* y, float np, uint64_t seed,
                             int64_t drop, unsigned char* sm) {
@@ -244,9 +245,9 @@ __device__ void u_propagate(const UDrop& d, const FadingConst& fc, int T, const 
       const int jp = 2 * pi;
       const int m = m0 + jp;
       if (m >= TD) continue;
-      float2 zr[8], zi[8];
+      float2 zr[MAXA], zi[MAXA];
 #pragma unroll
-      for (int tx = 0; tx < 8; ++tx) zr[tx] = zi[tx] = make_float2(0.f, 0.f);
+      for (int tx = 0; tx < MAXA; ++tx) zr[tx] = zi[tx] = make_float2(0.f, 0.f);
       float2 up[9];
       const float u0 = ((float)jp - 0.5f * BT) / (0.5f * BT);
       const float u1 = ((float)(jp + 1) - 0.5f * BT) / (0.5f * BT);
@@ -287,7 +288,9 @@ __device__ void u_propagate(const UDrop& d, const FadingConst& fc, int T, const 
         } else {
           const float2* cl = coef + l * (KK + 1);
           float2 ax = make_float2(cl[0].x, cl[0].x), ay = make_float2(cl[0].y, cl[0].y);
-          for (int k = 1; k <= KK; ++k) {
+#pragma unroll
+          for (int k = 1; k <= 8; ++k) {  // static indices keep up[] in registers
+            if (k > KK) break;
             const float2 ck = cl[k];
             ax = __ffma2_rn(make_float2(ck.x, ck.x), up[k], ax);
             ay = __ffma2_rn(make_float2(ck.y, ck.y), up[k], ay);
@@ -300,7 +303,7 @@ __device__ void u_propagate(const UDrop& d, const FadingConst& fc, int T, const 
         const int s0 = jp - dd + D;
         const float2 nhy = make_float2(-hy.x, -hy.y);
 #pragma unroll
-        for (int tx = 0; tx < 8; ++tx) {
+        for (int tx = 0; tx < MAXA; ++tx) {
           if (tx >= ntx) break;
           const float* pl = src + tx * 4 * XW + s0;
           const float2 re = *reinterpret_cast<const float2*>(pl);
@@ -314,7 +317,7 @@ __device__ void u_propagate(const UDrop& d, const FadingConst& fc, int T, const 
       for (int rx = 0; rx < nrx; ++rx) {
         float2 ore = make_float2(0.f, 0.f), oim = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int tx = 0; tx < 8; ++tx) {
+        for (int tx = 0; tx < MAXA; ++tx) {
           if (tx >= ntx) break;
           const float2 sv = Sm[rx * ntx + tx];
           const float2 sr = make_float2(sv.x, sv.x), si = make_float2(sv.y, sv.y), nsi = make_float2(-sv.y, -sv.y);
@@ -365,7 +368,7 @@ __device__ __forceinline__ unsigned int u_element(int mode, float2 g, const floa
   return e;
 }
 
-template <int NRX>
+template <int NRX, int MAXA>
 __device__ __forceinline__ unsigned int u_element_tx(int ntx, int mode, float2 g, const float2* Sm,
                                                      const float2* grid, int W, int C, int w, int c, float s2,
                                                      const QamDemapTable& qt, const uint32_t* bitsm, int BW,
@@ -373,13 +376,18 @@ __device__ __forceinline__ unsigned int u_element_tx(int ntx, int mode, float2 g
   switch (ntx) {
     case 1: return u_element<NRX, 1>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
     case 2: return u_element<NRX, 2>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
-    case 4: return u_element<NRX, 4>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
-    default: return u_element<NRX, 8>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
+    case 4:
+      if constexpr (MAXA >= 4) return u_element<NRX, 4>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
+      else return 0u;
+    default:
+      if constexpr (MAXA >= 8) return u_element<NRX, 8>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
+      else return 0u;  // not reached: the batch's kernel covers its largest antenna count
   }
 }
 
 // The thread's share of the drop's bit errors; `fin` turns false if one of its
 // elements had a non-finite equalizer pivot.
+template <int MAXA>
 __device__ unsigned int u_detect(const UDrop& d, const UFrame& fr, const FadingConst& fc, const int64_t* Wp,
                                  const int64_t* P0, const float2* Sm, const int* dl, const float2* grid, float s2,
                                  const QamDemapTable& qt, uint64_t seed, int64_t drop, unsigned char* sm, bool& fin) {
@@ -409,10 +417,14 @@ __device__ unsigned int u_detect(const UDrop& d, const UFrame& fr, const FadingC
       const float2 g = tap_response(fc, hb, dl, fr.twiddle, fr.bins[j], fr.N);
       const int64_t k = k0 + j;
       switch (d.nrx) {
-        case 1: local += u_element_tx<1>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
-        case 2: local += u_element_tx<2>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
-        case 4: local += u_element_tx<4>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
-        default: local += u_element_tx<8>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
+        case 1: local += u_element_tx<1, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
+        case 2: local += u_element_tx<2, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
+        case 4:
+          if constexpr (MAXA >= 4) local += u_element_tx<4, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin);
+          break;
+        default:
+          if constexpr (MAXA >= 8) local += u_element_tx<8, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin);
+          break;
       }
     }
     __syncthreads();
@@ -423,7 +435,7 @@ __device__ unsigned int u_detect(const UDrop& d, const UFrame& fr, const FadingC
 // ---------------------------------------------------------- persistent kernel
 // MINB = 1: registers as the largest stage needs; MINB = 2: capped so that two CTAs of
 // 256 threads share an SM (the autotuner measures both).
-template <int MINB>
+template <int MINB, int MAXA>
 __global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __grid_constant__ QamTables qts) {
   extern __shared__ float4 smem4[];
   __shared__ int s_drop;
@@ -472,7 +484,7 @@ __global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __
       default: u_tx<2048>(fr, d.ntx, a.seed, drop, x, work); break;
     }
     const float np = a.noise_power[b];
-    u_propagate(d, fc, fr.T, Wp, P0, Sm, dl, x, y, np, a.seed, drop, work);
+    u_propagate<MAXA>(d, fc, fr.T, Wp, P0, Sm, dl, x, y, np, a.seed, drop, work);
     switch (fr.N) {
       case 128: u_rx<128>(fr, d.nrx, fr.T + d.D, y, grid, work); break;
       case 256: u_rx<256>(fr, d.nrx, fr.T + d.D, y, grid, work); break;
@@ -481,7 +493,7 @@ __global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __
       default: u_rx<2048>(fr, d.nrx, fr.T + d.D, y, grid, work); break;
     }
     bool fin = finite_f(np);  // a NaN / inf noise power is an invalid drop too
-    const unsigned int e = u_detect(d, fr, fc, Wp, P0, Sm, dl, grid, np, qts.t[fr.m], a.seed, drop, work, fin);
+    const unsigned int e = u_detect<MAXA>(d, fr, fc, Wp, P0, Sm, dl, grid, np, qts.t[fr.m], a.seed, drop, work, fin);
     // drop total
     unsigned int v = e;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -529,6 +541,7 @@ struct hpx_uneven {
   size_t slot_bytes = 0, off_x = 0, off_y = 0, off_grid = 0, smem = 0;
   int max_slots = 0;
   int threads = 256, blocks_per_sm = 1, num_sms = 1, variant = 0;
+  int maxa = 8;  // largest antenna count of the batch (2, 4 or 8): selects the kernel instantiation
   QamTables qts;
   cudaGraphExec_t graph = nullptr;
   cudaGraph_t graph_def = nullptr;
@@ -545,6 +558,16 @@ void uneven_release(hpx_uneven* u) {
   for (void* q : p)
     if (q) cudaFree(q);
   delete u;
+}
+
+// The persistent kernel for a register variant (0: registers as needed, 1: capped for two
+// CTAs of 256 threads per SM) and the batch's largest antenna count: a batch without
+// 8-antenna drops runs an instantiation without the 8 x 8 stages and their registers.
+using UnevenKernel = void (*)(UArgs, QamTables);
+UnevenKernel uneven_kernel(int variant, int maxa) {
+  if (maxa <= 2) return variant ? k_uneven<2, 2> : k_uneven<1, 2>;
+  if (maxa <= 4) return variant ? k_uneven<2, 4> : k_uneven<1, 4>;
+  return variant ? k_uneven<2, 8> : k_uneven<1, 8>;
 }
 
 hpx_status uneven_launch(hpx_uneven* u, uint64_t seed, int64_t drop0, const float* noise, uint32_t* errors,
@@ -568,7 +591,7 @@ hpx_status uneven_launch(hpx_uneven* u, uint64_t seed, int64_t drop0, const floa
   a.drop0 = drop0;
   a.errors = errors;
   const int grid = std::min(u->num_sms * u->blocks_per_sm, u->max_slots);
-  auto kern = u->variant ? k_uneven<2> : k_uneven<1>;
+  auto kern = uneven_kernel(u->variant, u->maxa);
   if (u->smem > 48 * 1024)  // the attribute is per kernel: set it for this batch's size
     HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem));
   HPX_CUDA(cudaMemsetAsync(u->d_counter, 0, sizeof(unsigned int), s));
@@ -705,6 +728,8 @@ hpx_status hpx_uneven_create(const hpx_uneven_drop* drops, int32_t num_drops, do
     const size_t det_smem = (size_t)d.L * (1 + S1) * sizeof(float2) + (size_t)d.ntx * staged_bit_words(fr.C, m) * 4;
     max_smem = std::max({max_smem, fft_smem, prop_smem, det_smem});
     // schedule weight: samples x transmit antennas x taps + elements x Nrx x Ntx^2
+    u->maxa = i == 0 ? 2 : u->maxa;
+    u->maxa = std::max({u->maxa, q.num_rx, q.num_tx});
     u->cost.push_back((double)T * d.ntx * (d.L + d.nrx) + (double)fr.W * fr.C * d.nrx * d.ntx * d.ntx);
     u->bits.push_back((int64_t)fr.W * fr.C * m * d.ntx);
   }
@@ -739,16 +764,16 @@ hpx_status hpx_uneven_create(const hpx_uneven_drop* drops, int32_t num_drops, do
     return hpx_cuda_status(e, "uneven tables");
   }
   if (u->smem > 48 * 1024) {
-    if ((e = cudaFuncSetAttribute(k_uneven<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem)) !=
-            cudaSuccess ||
-        (e = cudaFuncSetAttribute(k_uneven<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem)) !=
-            cudaSuccess) {
+    if ((e = cudaFuncSetAttribute(uneven_kernel(0, u->maxa), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)u->smem)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(uneven_kernel(1, u->maxa), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)u->smem)) != cudaSuccess) {
       uneven_release(u);
       return hpx_cuda_status(e, "uneven shared memory");
     }
   }
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_uneven<1>, u->threads, u->smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, uneven_kernel(0, u->maxa), u->threads, u->smem);
   u->blocks_per_sm = std::max(1, occ);
   *out = u;
   return HPX_OK;
@@ -770,7 +795,7 @@ hpx_status hpx_uneven_config(hpx_uneven* u, int32_t threads, int32_t blocks_per_
   if (threads != 128 && threads != 256) return hpx_fail(HPX_ERR_ARG, "uneven_config: 128 or 256 threads");
   if (variant != 0 && variant != 1) return hpx_fail(HPX_ERR_ARG, "uneven_config: variant 0 or 1");
   int occ = 0;
-  HPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, variant ? k_uneven<2> : k_uneven<1>, threads, u->smem));
+  HPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, uneven_kernel(variant, u->maxa), threads, u->smem));
   if (occ < 1) return hpx_fail(HPX_ERR_UNSUPPORTED, "uneven_config: %d threads do not fit one SM", threads);
   if (blocks_per_sm < 1 || blocks_per_sm > occ)
     return hpx_fail(HPX_ERR_ARG, "uneven_config: %d CTAs per SM (1..%d fit)", blocks_per_sm, occ);
@@ -795,7 +820,7 @@ hpx_status hpx_uneven_get_config(const hpx_uneven* u, int32_t threads, int32_t v
   if (max_fit) {
     int occ = 0;
     if (threads == 128 || threads == 256)
-      HPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, variant ? k_uneven<2> : k_uneven<1>, threads,
+      HPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, uneven_kernel(variant, u->maxa), threads,
                                                              u->smem));
     *max_fit = occ;
   }
