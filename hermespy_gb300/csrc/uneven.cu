@@ -433,8 +433,9 @@ __device__ unsigned int u_detect(const UDrop& d, const UFrame& fr, const FadingC
 }
 
 // ---------------------------------------------------------- persistent kernel
-// MINB = 1: registers as the largest stage needs; MINB = 2: capped so that two CTAs of
-// 256 threads share an SM (the autotuner measures both).
+// MINB = 1: registers as the largest stage needs; MINB = 2 / 3: capped so that two / three
+// CTAs of 256 threads share an SM (three only without the 8 x 8 stages: 80 registers
+// without spills; the autotuner measures every variant the batch can use).
 template <int MINB, int MAXA>
 __global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __grid_constant__ QamTables qts) {
   extern __shared__ float4 smem4[];
@@ -565,6 +566,7 @@ void uneven_release(hpx_uneven* u) {
 // 8-antenna drops runs an instantiation without the 8 x 8 stages and their registers.
 using UnevenKernel = void (*)(UArgs, QamTables);
 UnevenKernel uneven_kernel(int variant, int maxa) {
+  if (variant == 2) return maxa <= 2 ? k_uneven<3, 2> : (maxa <= 4 ? k_uneven<3, 4> : nullptr);
   if (maxa <= 2) return variant ? k_uneven<2, 2> : k_uneven<1, 2>;
   if (maxa <= 4) return variant ? k_uneven<2, 4> : k_uneven<1, 4>;
   return variant ? k_uneven<2, 8> : k_uneven<1, 8>;
@@ -767,7 +769,10 @@ hpx_status hpx_uneven_create(const hpx_uneven_drop* drops, int32_t num_drops, do
     if ((e = cudaFuncSetAttribute(uneven_kernel(0, u->maxa), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)u->smem)) != cudaSuccess ||
         (e = cudaFuncSetAttribute(uneven_kernel(1, u->maxa), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)u->smem)) != cudaSuccess) {
+                                  (int)u->smem)) != cudaSuccess ||
+        (uneven_kernel(2, u->maxa) &&
+         (e = cudaFuncSetAttribute(uneven_kernel(2, u->maxa), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)u->smem)) != cudaSuccess)) {
       uneven_release(u);
       return hpx_cuda_status(e, "uneven shared memory");
     }
@@ -793,7 +798,9 @@ hpx_status hpx_uneven_bits(const hpx_uneven* u, int64_t* bits_per_drop) {
 hpx_status hpx_uneven_config(hpx_uneven* u, int32_t threads, int32_t blocks_per_sm, int32_t variant) {
   if (!u) return hpx_fail(HPX_ERR_ARG, "uneven_config: null argument");
   if (threads != 128 && threads != 256) return hpx_fail(HPX_ERR_ARG, "uneven_config: 128 or 256 threads");
-  if (variant != 0 && variant != 1) return hpx_fail(HPX_ERR_ARG, "uneven_config: variant 0 or 1");
+  if (variant < 0 || variant > 2) return hpx_fail(HPX_ERR_ARG, "uneven_config: variant 0, 1 or 2");
+  if (!uneven_kernel(variant, u->maxa))
+    return hpx_fail(HPX_ERR_UNSUPPORTED, "uneven_config: variant 2 needs drops of at most 4 antennas a side");
   int occ = 0;
   HPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, uneven_kernel(variant, u->maxa), threads, u->smem));
   if (occ < 1) return hpx_fail(HPX_ERR_UNSUPPORTED, "uneven_config: %d threads do not fit one SM", threads);
@@ -819,7 +826,7 @@ hpx_status hpx_uneven_get_config(const hpx_uneven* u, int32_t threads, int32_t v
   if (cur_variant) *cur_variant = u->variant;
   if (max_fit) {
     int occ = 0;
-    if (threads == 128 || threads == 256)
+    if ((threads == 128 || threads == 256) && variant >= 0 && variant <= 2 && uneven_kernel(variant, u->maxa))
       HPX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, uneven_kernel(variant, u->maxa), threads,
                                                              u->smem));
     *max_fit = occ;

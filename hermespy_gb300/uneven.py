@@ -121,7 +121,7 @@ class UnevenBatch:
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         best = None
         self.tuning = []
-        for variant in (0, 1):
+        for variant in (0, 1, 2):  # 2 exists only for batches of at most 4 antennas (fit 0 otherwise)
             for threads in (128, 256):
                 fit = min(self.fit(threads, variant), max(1, self.max_slots // sms))
                 for bps in range(1, fit + 1):

@@ -530,9 +530,10 @@ hpx_status hpx_uneven_destroy(hpx_uneven* batch);
 /* Data bits of every drop (host array [num_drops]). */
 hpx_status hpx_uneven_bits(const hpx_uneven* batch, int64_t* bits_per_drop);
 /* Launch shape: threads per CTA (128 or 256), CTAs per SM and kernel variant (0:
- * registers as needed, 1: capped for two 256-thread CTAs per SM), picked by the
- * caller's autotuner. hpx_uneven_get_config reports the current shape and how many
- * CTAs of (threads, variant) fit one SM. */
+ * registers as needed, 1: capped for two 256-thread CTAs per SM, 2: capped for three,
+ * only for batches whose drops have at most 4 antennas a side), picked by the caller's
+ * autotuner. hpx_uneven_get_config reports the current shape and how many CTAs of
+ * (threads, variant) fit one SM (0 for a variant the batch cannot use). */
 hpx_status hpx_uneven_config(hpx_uneven* batch, int32_t threads, int32_t blocks_per_sm, int32_t variant);
 hpx_status hpx_uneven_get_config(const hpx_uneven* batch, int32_t threads, int32_t variant, int32_t* cur_threads,
                                  int32_t* cur_blocks_per_sm, int32_t* cur_variant, int32_t* max_blocks_per_sm);

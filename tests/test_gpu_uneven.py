@@ -70,6 +70,25 @@ def test_uneven_tune_graph_and_bits():
     batch.errors.zero_()
     batch.replay()
     assert torch.equal(batch.errors, first)
-    assert batch.config()["variant"] in (0, 1)
+    assert batch.config()["variant"] in (0, 1, 2)
     with pytest.raises(ValueError):
         batch.set_config(96, 1)
+
+
+def test_three_cta_variant_for_small_antenna_batches():
+    """Batches whose drops have at most 4 antennas a side also run the 80-register
+    instantiation at three CTAs of 256 threads per SM, with the same counts; a batch
+    with 8-antenna drops cannot select it."""
+
+    small = [DropConfig(4, 4, 1024, 14, 64, 23, 0.4, 500.0, 20.0), DropConfig(2, 4, 512, 7, 16, 9, 2.0, 300.0, 12.0),
+             DropConfig(4, 1, 256, 14, 64, 17, 1.0, 1000.0, 30.0), DropConfig(1, 1, 128, 4, 4, 1, 3.0, 0.0, 5.0)] * 3
+    batch = UnevenBatch(small, SCS, TAP, 20, max_slots=4 * 152)
+    batch.set_config(256, 2, 1)
+    ref = batch.run(SEED, 0).clone()
+    assert batch.fit(256, 2) >= 3
+    batch.set_config(256, 3, 2)
+    assert torch.equal(batch.run(SEED, 0), ref)
+    big = UnevenBatch([DropConfig(8, 8, 1024, 14, 64, 23, 0.4, 500.0, 20.0)], SCS, TAP, 20, max_slots=152)
+    assert big.fit(256, 2) == 0
+    with pytest.raises(NotImplementedError):
+        big.set_config(256, 1, 2)
