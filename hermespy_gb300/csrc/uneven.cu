@@ -61,6 +61,7 @@ struct UArgs {
   size_t slot_bytes, off_x, off_y, off_grid;  // per-slot layout (state at 0)
   const float* noise_power;
   uint64_t seed;
+  PhiloxKeys noise_keys;  // the seed's round keys, for the AWGN of propagation
   int64_t drop0;
   uint32_t* errors;
 };
@@ -183,8 +184,8 @@ __device__ void u_rx(const UFrame& fr, int nrx, int TD, const float2* y, float2*
 // noise streams; any transmit count up to MAXA, every thread a set of sample pairs).
 template <int MAXA>
 __device__ void u_propagate(const UDrop& d, const FadingConst& fc, int T, const int64_t* Wp, const int64_t* P0,
-                            const float2* Sm, const int* dl, const float2* x, float2* y, float np, uint64_t seed,
-                            int64_t drop, unsigned char* sm) {
+                            const float2* Sm, const int* dl, const float2* x, float2* y, float np,
+                            const PhiloxKeys& nk, int64_t drop, unsigned char* sm) {
   const int L = d.L, S1 = fc.S1, D = d.D, nrx = d.nrx, ntx = d.ntx, K = d.K, BT = d.BT;
   const int XW = (BT + D + 2) & ~1;
   const int TD = T + D;
@@ -301,7 +302,7 @@ __device__ void u_propagate(const UDrop& d, const FadingConst& fc, int T, const 
         const int odd = (D - dd) & 1;
         const float* src = xp + 2 * odd * XW - odd;
         const int s0 = jp - dd + D;
-        const float2 nhy = make_float2(-hy.x, -hy.y);
+        const float2 nhy = __fmul2_rn(hy, make_float2(-1.f, -1.f));
 #pragma unroll
         for (int tx = 0; tx < MAXA; ++tx) {
           if (tx >= ntx) break;
@@ -327,7 +328,7 @@ __device__ void u_propagate(const UDrop& d, const FadingConst& fc, int T, const 
           oim = __ffma2_rn(si, zr[tx], oim);
         }
         if (np > 0.0f) {
-          const uint4 w = hpx_random_block(seed, drop, (uint32_t)rx, HPX_DOMAIN_NOISE, (uint32_t)(m >> 1));
+          const uint4 w = hpx_random_block_k(nk, drop, (uint32_t)rx, HPX_DOMAIN_NOISE, (uint32_t)(m >> 1));
           const float2 n0 = box_muller(w.x, w.y);
           const float2 n1 = box_muller(w.z, w.w);
           ore = __ffma2_rn(make_float2(sigma, sigma), make_float2(n0.x, n1.x), ore);
@@ -485,7 +486,7 @@ __global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __
       default: u_tx<2048>(fr, d.ntx, a.seed, drop, x, work); break;
     }
     const float np = a.noise_power[b];
-    u_propagate<MAXA>(d, fc, fr.T, Wp, P0, Sm, dl, x, y, np, a.seed, drop, work);
+    u_propagate<MAXA>(d, fc, fr.T, Wp, P0, Sm, dl, x, y, np, a.noise_keys, drop, work);
     switch (fr.N) {
       case 128: u_rx<128>(fr, d.nrx, fr.T + d.D, y, grid, work); break;
       case 256: u_rx<256>(fr, d.nrx, fr.T + d.D, y, grid, work); break;
@@ -590,6 +591,7 @@ hpx_status uneven_launch(hpx_uneven* u, uint64_t seed, int64_t drop0, const floa
   a.off_grid = u->off_grid;
   a.noise_power = noise;
   a.seed = seed;
+  a.noise_keys = philox_keys(seed);
   a.drop0 = drop0;
   a.errors = errors;
   const int grid = std::min(u->num_sms * u->blocks_per_sm, u->max_slots);
