@@ -32,6 +32,28 @@ def test_draws_match_oracle():
         np.testing.assert_array_equal(got[d], streams.fading_uniforms(SEED, 4 + d, h.num_draws))
 
 
+@pytest.mark.parametrize("doppler, expect_fp32", [(40.0, True), (400.0, False)])
+def test_taps_either_rate_path_with_los(doppler, expect_fp32):
+    """Realization takes FP32 rates while the largest rate is at most 2^-16 turns per
+    sample (40 Hz and 20 Hz LOS at 1 MHz: 6.4e-6), FP64 above (400 Hz: 6.4e-5); both
+    match the float64 oracle over 30 000 samples, LOS and NLOS taps alike."""
+
+    from oracle import fading as ofad
+
+    fs, T = 1e6, 30000
+    cfg = ofad.FadingConfig(np.array([0.0, 2.0, 5.0]) / fs, np.array([1.0, 0.4, 0.2]), np.array([np.inf, 2.0, 0.0]),
+                            9, doppler, doppler / 2, 1.0)
+    assert (doppler / fs / (2 * np.pi) <= 2.0 ** -16) == expect_fp32
+    h = fading_handle(cfg, 2, 2, fs)
+    st = _realize(h, 2, 3)
+    out = torch.empty((2, cfg.num_taps, T), dtype=torch.complex64, device="cuda")
+    _lib.call("hpx_fading_taps", h.handle, _lib.ptr(st), 2, T, _lib.ptr(out), stream())
+    got = host(out)
+    for d in range(2):
+        smp = fading.realize(cfg, SEED, 3 + d, 2, 2)
+        assert rel_rms(got[d], fading.path_impulses(smp, T, fs)) < TOL
+
+
 @pytest.mark.parametrize("name", list(FADING_CASES))
 def test_taps(name):
     cfg, nrx, ntx, T, fs = fading_case(name)
