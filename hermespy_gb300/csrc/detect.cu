@@ -1,5 +1,7 @@
 // Channel estimation (LS), per-element equalization (ZF / LMMSE) and the fused
 // receivers that end in bit-error counts.
+#include <algorithm>
+
 #include "fading_dev.cuh"
 #include "lmmse_dev.cuh"
 #include "equalize_dev.cuh"
@@ -16,6 +18,13 @@ struct hpx_ls {
   int32_t* d_ref_column = nullptr;  // [num_refs]
   int32_t* d_pos = nullptr;         // [nnz] word << 16 | column of the entry's reference element
   float2* d_coef = nullptr;         // [nnz] weight * conj(x_ref) / |x_ref|^2 (the LS division folded in)
+  // staged form (k_ls_staged): per block of LS_BLOCK_ROWS rows the distinct reference
+  // positions its entries read (d_bpos[d_bstart[b] .. d_bstart[b + 1])), and per entry the
+  // index of its position in that list; empty if a block's list is too long to stage
+  int32_t* d_bstart = nullptr;      // [blocks + 1]
+  int32_t* d_bpos = nullptr;        // [sum of the lists] word << 16 | column
+  int32_t* d_loc = nullptr;         // [nnz]
+  int max_block_refs = 0;
 };
 
 // True if the LS table's grid (words x columns) is the frame's: the receivers lay
@@ -308,6 +317,51 @@ __global__ void __launch_bounds__(DTHREADS) k_detect_ls(int W, int C, int m, con
   block_count(local, !fin, errors + b);
 }
 
+// Staged LS + interpolation: one block per LS_BLOCK_ROWS table rows and LS_ITEMS
+// received grids (drop, rx). The block first copies, for each of its grids, the
+// reference positions its rows read (one list per row block, built with the table)
+// into shared memory, then every thread walks its row's entries in table order on
+// those copies: the same products and sums as k_ls_estimate, with one read of each
+// reference element per grid instead of one per entry (the entries gather from L2).
+constexpr int LS_BLOCK_ROWS = 256;
+constexpr int LS_STAGE_ITEMS = 16;
+__global__ void __launch_bounds__(LS_BLOCK_ROWS) k_ls_staged(int W, int rows, int items,
+                                                              const int32_t* __restrict__ indptr,
+                                                              const int32_t* __restrict__ loc,
+                                                              const float2* __restrict__ coef,
+                                                              const int32_t* __restrict__ bstart,
+                                                              const int32_t* __restrict__ bpos,
+                                                              const float2* __restrict__ grid, int gcols,
+                                                              float2* __restrict__ est) {
+  extern __shared__ float2 stg[];  // [LS_STAGE_ITEMS][np]
+  const int blk = blockIdx.x, i0 = blockIdx.y * LS_STAGE_ITEMS;
+  const int n = min(LS_STAGE_ITEMS, items - i0);
+  const int p0 = bstart[blk], np = bstart[blk + 1] - p0;
+  for (int q = threadIdx.x; q < np * LS_STAGE_ITEMS; q += LS_BLOCK_ROWS) {
+    const int i = q / np, j = q - i * np;
+    const int ps = bpos[p0 + j];
+    stg[q] = i < n ? grid[(int64_t)(i0 + i) * W * gcols + (int64_t)(ps >> 16) * gcols + (ps & 0xFFFF)]
+                   : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int row = blk * LS_BLOCK_ROWS + threadIdx.x;
+  if (row >= rows) return;
+  float2 h[LS_STAGE_ITEMS];
+#pragma unroll
+  for (int i = 0; i < LS_STAGE_ITEMS; ++i) h[i] = make_float2(0.f, 0.f);
+  for (int e = indptr[row]; e < indptr[row + 1]; ++e) {
+    const int l = loc[e];
+    const float2 cf = coef[e];
+#pragma unroll
+    for (int i = 0; i < LS_STAGE_ITEMS; ++i) cfma(h[i], cf, stg[i * np + l]);
+  }
+#pragma unroll
+  for (int i = 0; i < LS_STAGE_ITEMS; ++i) {
+    if (i >= n) break;
+    est[(int64_t)(i0 + i) * rows + row] = h[i];
+  }
+}
+
 // rows = streams * W * C (the stacked tables); blockIdx.y covers LS_ITEMS received
 // grids (drop, rx), which share every table row a thread loads. Each table entry is
 // (position, weight conj(x) / |x|^2): the LS value y / x of a reference element and
@@ -427,6 +481,24 @@ hpx_status detect_ideal_tx(int ntx, const hpx_fading* f, const void* state, cons
   }
 }
 
+// The staged kernel when the table has its block lists, else the gathering one.
+hpx_status launch_ls(const hpx_ls* ls, int W, int rows, int items, const float2* grid, int gcols, float2* est,
+                     cudaStream_t s) {
+  if (ls->max_block_refs > 0) {
+    const size_t smem = (size_t)LS_STAGE_ITEMS * ls->max_block_refs * sizeof(float2);
+    if (smem > 48 * 1024)
+      HPX_CUDA(cudaFuncSetAttribute(k_ls_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 g((rows + LS_BLOCK_ROWS - 1) / LS_BLOCK_ROWS, (items + LS_STAGE_ITEMS - 1) / LS_STAGE_ITEMS);
+    k_ls_staged<<<g, LS_BLOCK_ROWS, smem, s>>>(W, rows, items, ls->d_indptr, ls->d_loc, ls->d_coef, ls->d_bstart,
+                                               ls->d_bpos, grid, gcols, est);
+  } else {
+    dim3 g((rows + 255) / 256, (items + LS_ITEMS - 1) / LS_ITEMS);
+    k_ls_estimate<<<g, 256, 0, s>>>(W, rows, items, ls->d_indptr, ls->d_pos, ls->d_coef, grid, gcols, est);
+  }
+  HPX_LAUNCHED("ls_estimate");
+  return HPX_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -490,7 +562,26 @@ hpx_status hpx_ls_create_streams(const hpx_frame* frame, int32_t C, int32_t num_
     coef[q] = den > 0 ? make_float2((float)(weights[q] * xr / den), (float)(-weights[q] * xi / den))
                       : make_float2(NAN, NAN);  // y / 0, as the division it replaces
   }
+  // staged form: the distinct positions read by each block of LS_BLOCK_ROWS rows
+  const int nblk = (rows + LS_BLOCK_ROWS - 1) / LS_BLOCK_ROWS;
+  std::vector<int32_t> bstart(nblk + 1, 0), bpos, loc(nnz);
+  for (int b = 0; b < nblk; ++b) {
+    const int e0 = indptr[b * LS_BLOCK_ROWS], e1 = indptr[std::min(rows, (b + 1) * LS_BLOCK_ROWS)];
+    std::vector<int32_t> u(pos.begin() + e0, pos.begin() + e1);
+    std::sort(u.begin(), u.end());
+    u.erase(std::unique(u.begin(), u.end()), u.end());
+    for (int q = e0; q < e1; ++q) loc[q] = (int32_t)(std::lower_bound(u.begin(), u.end(), pos[q]) - u.begin());
+    bstart[b] = (int32_t)bpos.size();
+    bpos.insert(bpos.end(), u.begin(), u.end());
+    ls->max_block_refs = std::max(ls->max_block_refs, (int)u.size());
+  }
+  bstart[nblk] = (int32_t)bpos.size();
+  const bool staged = (size_t)LS_STAGE_ITEMS * ls->max_block_refs * sizeof(float2) <= 96 * 1024 && nnz > 0;
+  if (!staged) ls->max_block_refs = 0;
   if ((e = up((void**)&ls->d_indptr, indptr, (rows + 1) * sizeof(int32_t))) != cudaSuccess ||
+      (staged && (e = up((void**)&ls->d_bstart, bstart.data(), bstart.size() * sizeof(int32_t))) != cudaSuccess) ||
+      (staged && (e = up((void**)&ls->d_bpos, bpos.data(), bpos.size() * sizeof(int32_t))) != cudaSuccess) ||
+      (staged && (e = up((void**)&ls->d_loc, loc.data(), loc.size() * sizeof(int32_t))) != cudaSuccess) ||
       (e = up((void**)&ls->d_indices, indices, nnz * sizeof(int32_t))) != cudaSuccess ||
       (e = up((void**)&ls->d_weights, weights, nnz * sizeof(float))) != cudaSuccess ||
       (e = up((void**)&ls->d_ref_word, rw.data(), rw.size() * sizeof(int32_t))) != cudaSuccess ||
@@ -511,7 +602,8 @@ hpx_status hpx_ls_create(const hpx_frame* frame, int32_t C, const int32_t* indpt
 
 hpx_status hpx_ls_destroy(hpx_ls* ls) {
   if (!ls) return HPX_OK;
-  void* p[] = {ls->d_indptr, ls->d_indices, ls->d_weights, ls->d_ref_word, ls->d_ref_column, ls->d_pos, ls->d_coef};
+  void* p[] = {ls->d_indptr, ls->d_indices, ls->d_weights, ls->d_ref_word, ls->d_ref_column, ls->d_pos, ls->d_coef,
+               ls->d_bstart, ls->d_bpos, ls->d_loc};
   for (void* q : p)
     if (q) cudaFree(q);
   delete ls;
@@ -527,12 +619,8 @@ hpx_status hpx_ls_estimate(const hpx_ls* ls, const hpx_cf32* grid, int32_t gcols
   if (B > 65535) return hpx_fail(HPX_ERR_ARG, "ls_estimate: batch too large");
   if (ls->ntx != 1) return hpx_fail(HPX_ERR_ARG, "ls_estimate: table of %d streams (use hpx_ls_estimate_streams)", ls->ntx);
   const int W = ls->frame->info.num_words;
-  dim3 grid_dim((W * ls->C + 255) / 256, (B + LS_ITEMS - 1) / LS_ITEMS);
-  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, W * ls->C, B, ls->d_indptr, ls->d_pos, ls->d_coef,
-                                                         reinterpret_cast<const float2*>(grid), gcols,
-                                                         reinterpret_cast<float2*>(est));
-  HPX_LAUNCHED("ls_estimate");
-  return HPX_OK;
+  return launch_ls(ls, W, W * ls->C, B, reinterpret_cast<const float2*>(grid), gcols, reinterpret_cast<float2*>(est),
+                   as_stream(stream));
 }
 
 hpx_status hpx_ls_estimate_streams(const hpx_ls* ls, const hpx_cf32* grid, int32_t gcols, int32_t nrx, int32_t B,
@@ -544,12 +632,8 @@ hpx_status hpx_ls_estimate_streams(const hpx_ls* ls, const hpx_cf32* grid, int32
   if ((int64_t)B * nrx > 65535) return hpx_fail(HPX_ERR_ARG, "ls_estimate: batch too large");
   const int W = ls->frame->info.num_words;
   const int rows = ls->ntx * W * ls->C;
-  dim3 grid_dim((rows + 255) / 256, (B * nrx + LS_ITEMS - 1) / LS_ITEMS);
-  k_ls_estimate<<<grid_dim, 256, 0, as_stream(stream)>>>(W, rows, B * nrx, ls->d_indptr, ls->d_pos, ls->d_coef,
-                                                         reinterpret_cast<const float2*>(grid), gcols,
-                                                         reinterpret_cast<float2*>(est));
-  HPX_LAUNCHED("ls_estimate");
-  return HPX_OK;
+  return launch_ls(ls, W, rows, B * nrx, reinterpret_cast<const float2*>(grid), gcols, reinterpret_cast<float2*>(est),
+                   as_stream(stream));
 }
 
 hpx_status hpx_equalize(int32_t mode, int32_t nrx, int32_t ntx, int64_t K, int32_t B, const hpx_cf32* H,
