@@ -491,10 +491,10 @@ def bench_estimators(ctx, spec, args):
                             "ber": r["ber"], "nmse_db": nm[name],
                             "stages_ms": {k: round(v / args.steps, 4) for k, v in r["stage_ms"].items()}}
     sel = results[selected]
-    # lmmse: realize, transmit, propagate, receive, then gains + tensor-core receiver per
-    # chunk of 8 192 drops
+    # lmmse: realize, transmit, propagate, receive, then pilot LS + gains + tensor-core
+    # receiver per chunk of 8 192 drops
     launches = {"learned": 4 + 1 + 8 * ((drops + chunk - 1) // chunk) + 1,
-                "lmmse": 4 + 2 * ((drops + 8191) // 8192), "ls": 6}[selected]
+                "lmmse": 4 + 3 * ((drops + 8191) // 8192), "ls": 6}[selected]
     extra = {"synchronization": sync_report(ctx, args), "fec": fec_report(ctx, args), "comparison": comparison,
              "estimator_policy": {
         "selected": selected, "rule": "learned if its validation NMSE <= LMMSE NMSE + 0.5 dB, else LMMSE",

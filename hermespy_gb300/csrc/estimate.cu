@@ -422,7 +422,7 @@ hpx_status hpx_lmmse_create_regularized(const hpx_frame* frame, const hpx_fading
     return hpx_cuda_status(err, "lmmse tables");
   }
   if (ntx == 4 && 2 * U <= 128) {  // the 4 x 4 receiver's tensor-core path
-    const hpx_status st = lmmse_tc_prepare(e, delays);
+    const hpx_status st = lmmse_tc_prepare(e, delays, G, pw_count, pw_off, pcol);
     if (st != HPX_OK) {
       release(e);
       return st;

@@ -268,9 +268,19 @@ struct hpx_lmmse {
   float* d_tc_scale = nullptr;     // [tc_ws_drops]
   int* d_tc_fail = nullptr;        // set if a tensor-core wait timed out (later CTAs skip)
   int32_t* d_tc_etab = nullptr;    // [W][FC] data element index, -1 for other elements
+  int tc_cnt_max = 0;              // most pilots of one stream in one word
+  int tc_ls_tu = 0;                // taps per thread of the batched pilot LS (rows padded to 8 of them)
+  int tc_ls_stages = 0;            // its cp.async pipeline depth (0: the frame does not fit)
+  int tc_ls_nch_max = 0, tc_ls_kcm = 0;  // column chunks per pilot word, most pilots of a stream in one
+  int32_t* d_tc_ls_cspan = nullptr;      // [np][2] first pilot column of the word, columns spanned
+  int2* d_tc_ls_krange = nullptr;        // [np][nch_max][4] pilots of stream t in chunk c: [kb, ke)
+  float4* d_tc_gt = nullptr;       // [total pilots][8 tc_ls_tu] weighted-LS rows transposed, (gr, gr, gi, gi)
+  float2* d_tc_gls = nullptr;      // [tc_ws_drops][16 pairs][np][U] pilot LS gains
 };
 constexpr int kLmmseTcChunk = 8192;  // drops per gains/GEMM launch pair (workspace 72 KB per drop)
-hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays);
+hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays, const std::vector<float2>& G,
+                            const std::vector<int32_t>& pw_count, const std::vector<int32_t>& pw_off,
+                            const std::vector<int32_t>& pcol);
 void lmmse_tc_release(hpx_lmmse* e);
 hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int gcols, const float* nv,
                            uint64_t seed, int64_t drop0, int B, uint32_t* errors, cudaStream_t s);

@@ -91,6 +91,72 @@ __device__ __forceinline__ void lmmse_word_weights(const LmmseView& e, float s2,
   }
 }
 
+// The weights of lmmse_word_weights for the words wlist[0 .. nwl) only (-1 entries
+// skipped), one thread per (stream, tap, word) system: each thread factors its own
+// np x np matrix (np == NPW) and solves for its word, with the same operations as
+// lmmse_word_weights, so the weights are identical. cw layout as there.
+template <int NPW>
+__device__ __forceinline__ void lmmse_listed_word_weights(const LmmseView& e, float s2, const int32_t* __restrict__ wlist,
+                                                          int nwl, float* cw) {
+  const int W = e.W, U = e.U, P = e.P;
+  for (int q = threadIdx.x; q < e.ntx * U * nwl; q += blockDim.x) {
+    const int tu = q / nwl, wi = q - tu * nwl, t = tu / U, u = tu - t * U;
+    const int w = wlist[wi];
+    if (w < 0) continue;
+    float m[NPW][NPW];
+#pragma unroll
+    for (int i = 0; i < NPW; ++i)
+#pragma unroll
+      for (int j = 0; j < NPW; ++j)
+        m[i][j] = e.R[((size_t)u * P + i) * P + j] + (i == j ? s2 * e.E[(t * P + i) * U + u] : 0.f);
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < NPW; ++j) {
+      float d = m[j][j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) d -= m[j][k] * m[j][k];
+      if (!(d > 0.f)) ok = false;  // no signal power on this tap: its gains stay zero
+      const float inv = ok ? rsqrtf(d) : 0.f;
+      m[j][j] = inv;
+#pragma unroll
+      for (int i = j + 1; i < NPW; ++i) {
+        float sm = m[i][j];
+#pragma unroll
+        for (int k = 0; k < j; ++k) sm -= m[i][k] * m[j][k];
+        m[i][j] = sm * inv;
+      }
+    }
+    float z[NPW];
+#pragma unroll
+    for (int i = 0; i < NPW; ++i) {
+      float sm = ok ? e.rw[((size_t)u * W + w) * P + i] : 0.f;
+#pragma unroll
+      for (int k = 0; k < i; ++k) sm -= m[i][k] * z[k];
+      z[i] = ok ? sm * m[i][i] : 0.f;
+    }
+#pragma unroll
+    for (int i = NPW - 1; i >= 0; --i) {
+      float sm = z[i];
+#pragma unroll
+      for (int k = i + 1; k < NPW; ++k) sm -= m[k][i] * z[k];
+      z[i] = ok ? sm * m[i][i] : 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < NPW; ++i) cw[(((size_t)t * U + u) * W + w) * NPW + i] = z[i];
+  }
+}
+
+// lmmse_word_weights with register-resident systems for the usual pilot-word counts.
+__device__ __forceinline__ void lmmse_word_weights_np(const LmmseView& e, float s2, float* cw) {
+  switch (e.np) {
+    case 1: lmmse_word_weights<1>(e, s2, cw); break;
+    case 2: lmmse_word_weights<2>(e, s2, cw); break;
+    case 3: lmmse_word_weights<3>(e, s2, cw); break;
+    case 4: lmmse_word_weights<4>(e, s2, cw); break;
+    default: lmmse_word_weights<kMaxPilotWords>(e, s2, cw, e.np); break;
+  }
+}
+
 // Tap gains of every antenna pair and word of drop b into gt (pair = rx * ntx + tx),
 // stored as planes: for word w and tap u, NP real parts then NP imaginary parts
 // (float index (w U + u) 2 NP + {0, NP} + pair), so two pairs share each packed
@@ -158,13 +224,7 @@ __device__ __forceinline__ void lmmse_drop_taps(const LmmseView& e, int b, int n
       }
     }
   }
-  switch (np) {  // register-resident systems for the usual pilot-word counts
-    case 1: lmmse_word_weights<1>(e, s2, cw); break;
-    case 2: lmmse_word_weights<2>(e, s2, cw); break;
-    case 3: lmmse_word_weights<3>(e, s2, cw); break;
-    case 4: lmmse_word_weights<4>(e, s2, cw); break;
-    default: lmmse_word_weights<kMaxPilotWords>(e, s2, cw, np); break;
-  }
+  lmmse_word_weights_np(e, s2, cw);
   __syncthreads();
   float* gtf = reinterpret_cast<float*>(gt);
   for (int q = threadIdx.x; q < W * U * NP; q += blockDim.x) {

@@ -4,10 +4,13 @@
 // The per-element channel of every antenna pair is a tap DFT,
 //   H[w][c][pair] = sum_u g[w][u][pair] exp(-2 pi i bin(c) d_u / N),
 // i.e. for one drop a GEMM of (subcarriers x 2U) twiddles by (2U x words*pairs*{re,im})
-// gains: [Re H | Im H] = [F_re | F_im] [[G_re, G_im], [-G_im, G_re]]. It runs in two
+// gains: [Re H | Im H] = [F_re | F_im] [[G_re, G_im], [-G_im, G_re]]. It runs in three
 // kernels per chunk of drops:
-//   k_lmmse_gains  (one CTA per drop): pilot LS, per-tap LMMSE over the words and
-//                  the gains of every word and pair (lmmse_drop_taps), written to a
+//   k_lmmse_ls     (one CTA per pilot word of a stream and 32 drops): the pilot LS of
+//                  the tap gains, as a complex GEMM over drops with the weighted-LS
+//                  operator held in shared memory;
+//   k_lmmse_gains  (one CTA per drop): per-tap LMMSE weights over the pilot words
+//                  and the gains of every data word and pair, written to a
 //                  workspace as the GEMM's FP16 (hi, lo) operand in its shared-memory
 //                  layout, scaled by a power of two bounding them by 1;
 //   k_lmmse_tc     (one CTA per drop and 128 subcarriers): the GEMM as FP16 MMAs
@@ -50,35 +53,230 @@ struct TcView {
   const float* scale;     // [drops]
 };
 
+// ------------------------------------------------------- kernel 0: pilot LS
+// The weighted LS of every tap gain on every pilot word (step 1 of lmmse_drop_taps),
+// batched over drops as a complex GEMM: CTA (pilot word p, DROPS drops) computes
+// gls[b][r ntx + t][p][u] = sum_k G_tp[u][k] y(b, r, word_p, pcol_tp[k]) for all four
+// streams t, its drops and the 4 receive antennas. The received rows of the word pass
+// through shared memory in chunks of LS_CC columns (whole 32-byte sectors: every
+// pilot of every stream in them is used), with the weighted-LS rows of the pilots
+// that fall in the chunk, by cp.async S stages deep. Rows are stored as (gr, gr, gi,
+// gi) and pilots as received, so that P += (yr, yi) (gr, gr) and Q += (yr, yi) (gi, gi)
+// are packed FP32x2 FMAs and the gain is (P.x - Q.y, Q.x + P.y). Thread (t, g, d)
+// accumulates taps g, g + 8, ... of stream t for drop d's four antennas.
+// A chunk column holds (drop d, antenna r) at 8-byte slot 4 d + r, columns ROWS + 2
+// slots apart: a staging copy instruction writes 32 columns of one row (one 256-byte
+// run in global memory, 4-way bank aliasing in shared memory), and the FMA loop reads
+// a drop's antennas (0, 1) and (2, 3) as 16-byte pairs, the warp's 4 drops without
+// conflicts.
+constexpr int LS_CC = 32;  // columns per chunk
+
+template <int TU>
+struct LsShape {
+  static constexpr int DROPS = TU <= 4 ? 16 : 8;  // accumulator registers: 16 TU per thread
+  static constexpr int THREADS = 4 * 8 * DROPS;   // 4 streams x 8 tap groups x DROPS
+  static constexpr int ROWS = 4 * DROPS;          // received rows (drop, antenna) of a chunk
+  static constexpr int CS = ROWS + 2;             // slots per staged column
+};
+
+struct LsView {
+  const int32_t* cspan;  // [np][2] first pilot column of the word, columns spanned
+  const int2* krange;    // [np][nch_max][4]: stream t's pilots in chunk c, [kb, ke)
+  int nch_max, kcm, cnt_max;
+};
+
+size_t lmmse_ls_smem(int tu, int stages, int kcm, int cnt_max, int nch_max) {
+  const int cs = (tu <= 4 ? 64 : 32) + 2;
+  return (size_t)stages * LS_CC * cs * sizeof(float2) + (size_t)stages * 4 * kcm * 8 * tu * sizeof(float4) +
+         (size_t)4 * cnt_max * 4 + (size_t)nch_max * 4 * sizeof(int2);
+}
+
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, bool fill) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(src), "r"(fill ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool fill) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(src), "r"(fill ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <int TU, int S>  // taps per thread (U <= 8 TU), pipeline stages
+__global__ void __launch_bounds__(LsShape<TU>::THREADS, 1)
+    k_lmmse_ls(LmmseView e, LsView lv, const float4* __restrict__ gtab, const float2* __restrict__ grid, int gcols,
+               int nb, float2* __restrict__ gls_out) {
+  using SH = LsShape<TU>;
+  constexpr int UP = 8 * TU;
+  extern __shared__ float4 smem4[];
+  const int kcm = lv.kcm, cmax = lv.cnt_max;
+  float2* ys = reinterpret_cast<float2*>(smem4);               // [S][LS_CC][CS]
+  float4* gs = reinterpret_cast<float4*>(ys + S * LS_CC * SH::CS);  // [S][4][kcm][UP]
+  int* pcs = reinterpret_cast<int*>(gs + S * 4 * kcm * UP);    // [4][cnt_max] column - first column
+  int2* kr = reinterpret_cast<int2*>(pcs + 4 * cmax);          // [nch][4]
+  const int W = e.W, U = e.U, np = e.np, P = e.P;
+  const int p = blockIdx.x, b0 = blockIdx.y * SH::DROPS;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int word = e.pw_word[p];  // every stream carries pilots in the same words
+  const int c_first = lv.cspan[2 * p], span = lv.cspan[2 * p + 1];
+  const int nch = (span + LS_CC - 1) / LS_CC;
+  __shared__ int offt[4];  // first pilot of each stream's word p in the pilot tables
+  if (tid < 4) offt[tid] = e.pw_off[tid * P + p];
+  for (int i = tid; i < 4 * cmax; i += SH::THREADS) {
+    const int t = i / cmax, k = i - t * cmax;
+    if (k < e.pw_count[t * P + p]) pcs[i] = e.pcol[e.pw_off[t * P + p] + k] - c_first;
+  }
+  for (int i = tid; i < nch * 4; i += SH::THREADS) kr[i] = lv.krange[(size_t)p * lv.nch_max * 4 + i];
+  __syncthreads();
+  // staging: copy m of this thread is row warp + (THREADS / 32) m, column lane of the chunk
+  constexpr int NM = SH::ROWS * LS_CC / SH::THREADS;
+  static_assert(NM * SH::THREADS == SH::ROWS * LS_CC && SH::THREADS / 32 * NM == SH::ROWS, "staging rounds");
+  const float2* rp[NM];
+  int ys_off[NM];
+#pragma unroll
+  for (int m = 0; m < NM; ++m) {
+    const int row = warp + (SH::THREADS / 32) * m, dd = row >> 2, r = row & 3;
+    rp[m] = grid + (((int64_t)min(b0 + dd, nb - 1) * 4 + r) * W + word) * gcols + c_first;
+    ys_off[m] = lane * SH::CS + 4 * dd + r;
+  }
+  const int g = tid & 7, d = (tid >> 3) % SH::DROPS;
+  const int ts = tid / (8 * SH::DROPS);  // this thread's stream
+  auto stage = [&](int c, int st) {
+    const int col = c * LS_CC + lane;
+    const bool ok = col < span;
+    float2* yd = ys + st * LS_CC * SH::CS;
+#pragma unroll
+    for (int m = 0; m < NM; ++m) cp_async8(yd + ys_off[m], rp[m] + (ok ? col : 0), ok);
+    // the operator rows of this thread's stream: its 8 DROPS threads copy kcm x UP rows
+    float4* gd = gs + (st * 4 + ts) * kcm * UP;
+    const int2 k = kr[c * 4 + ts];
+    const float4* gsrc = gtab + (int64_t)(offt[ts] + k.x) * UP;
+    for (int j = tid - ts * 8 * SH::DROPS; j < kcm * UP; j += 8 * SH::DROPS) {
+      const bool v = j < (k.y - k.x) * UP;
+      cp_async16(gd + j, v ? gsrc + j : gtab, v);
+    }
+  };
+  float2 Pa[TU][4], Qa[TU][4];
+#pragma unroll
+  for (int i = 0; i < TU; ++i)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) Pa[i][r] = Qa[i][r] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int s = 0; s < S - 1; ++s) {
+    if (s < nch) stage(s, s);
+    cp_async_commit();
+  }
+  const int* pct = pcs + ts * cmax;
+  for (int c = 0; c < nch; ++c) {
+    cp_async_wait<S - 2>();
+    __syncthreads();  // chunk c landed everywhere; chunk c - 1's stage is free
+    if (c + S - 1 < nch) stage(c + S - 1, (c + S - 1) % S);
+    cp_async_commit();
+    const int st = c % S;
+    const float2* yst = ys + st * LS_CC * SH::CS + 4 * d;
+    const float4* gst = gs + (st * 4 + ts) * kcm * UP + g;
+    const int2 k = kr[c * 4 + ts];
+#pragma unroll 2
+    for (int kk = k.x; kk < k.y; ++kk) {
+      const float2* yc = yst + (pct[kk] - c * LS_CC) * SH::CS;
+      const float4 y01 = *reinterpret_cast<const float4*>(yc);
+      const float4 y23 = *reinterpret_cast<const float4*>(yc + 2);
+      const float2 y[4] = {make_float2(y01.x, y01.y), make_float2(y01.z, y01.w), make_float2(y23.x, y23.y),
+                           make_float2(y23.z, y23.w)};
+      const float4* gk = gst + (kk - k.x) * UP;
+#pragma unroll
+      for (int i = 0; i < TU; ++i) {
+        const float4 gv = gk[8 * i];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          Pa[i][r] = __ffma2_rn(y[r], make_float2(gv.x, gv.y), Pa[i][r]);
+          Qa[i][r] = __ffma2_rn(y[r], make_float2(gv.z, gv.w), Qa[i][r]);
+        }
+      }
+    }
+  }
+  const int b = b0 + d;
+  if (b >= nb) return;
+  float2* dst = gls_out + (int64_t)b * 16 * np * U;
+#pragma unroll
+  for (int i = 0; i < TU; ++i) {
+    const int u = 8 * i + g;
+    if (u < U)
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        dst[((r * 4 + ts) * np + p) * U + u] = make_float2(Pa[i][r].x - Qa[i][r].y, Qa[i][r].x + Pa[i][r].y);
+  }
+}
+
 // ------------------------------------------------------------ kernel 1: gains
-// Writes, per pass of four data words, the FP16 (hi, lo) gains operand of the
-// GEMM in its K-major shared-memory layout: row n = slot * 32 + q (q < 16: Re H of
-// pair q, else Im H of pair q - 16), k < U: the coefficient of Re F (G_re or G_im),
-// U <= k < 2U: of Im F (-G_im or G_re), scaled by a power of two bounding the
-// drop's gains by 1.
-__global__ void __launch_bounds__(512, 2) k_lmmse_gains(LmmseView e, const float2* __restrict__ grid, int gcols,
-                                                         const float* __restrict__ nv, const int32_t* __restrict__ wlist,
-                                                         int nwl, int KP, uint16_t* __restrict__ bop,
-                                                         float* __restrict__ scale_ws) {
+// Per drop: the per-tap LMMSE weights over the pilot words (lmmse_word_weights), the
+// gains g[w][u][pair] = sum_p weight * LS gain of every data word, and from them,
+// per pass of four data words, the FP16 (hi, lo) gains operand of the GEMM in its
+// K-major shared-memory layout: row n = slot * 32 + q (q < 16: Re H of pair q, else
+// Im H of pair q - 16), k < U: the coefficient of Re F (G_re or G_im), U <= k < 2U:
+// of Im F (-G_im or G_re), scaled by a power of two bounding the drop's gains by 1.
+// The gains are kept as gx[i][row][q] (row < U: tap, U <= row < KP - U: zero) for
+// data word i of the pass list, q < 16: Re of pair q, else Im of pair q - 16; operand
+// column k reads row k (column q) for k < U and row k - U (column q ^ 16, negated for
+// q < 16) above, so k >= 2U meets the zero rows. Lane q of a warp writes row n.
+__global__ void __launch_bounds__(512, 2) k_lmmse_gains(LmmseView e, const float* __restrict__ nv,
+                                                         const int32_t* __restrict__ wlist, int nwl, int KP,
+                                                         uint16_t* __restrict__ bop, float* __restrict__ scale_ws,
+                                                         const float2* __restrict__ gls_ws) {
   extern __shared__ float4 smem4[];
   __shared__ float red[16];
   __shared__ float sscale;
-  const int b = blockIdx.x;
-  const int W = e.W, U = e.U;
-  float2* gt = reinterpret_cast<float2*>(smem4);
-  float2* gls = gt + (size_t)W * U * TC_NP;
-  float* cw = reinterpret_cast<float*>(gls + TC_NP * e.np * U);
-  int* ds = reinterpret_cast<int*>(cw + (size_t)e.ntx * U * W * e.np);
+  const int b = blockIdx.x, tid = threadIdx.x;
+  const int W = e.W, U = e.U, np = e.np, ntx = e.ntx, R = KP - U;
+  float* gx = reinterpret_cast<float*>(smem4);   // [nwl][R][32]
+  float* cw = gx + (size_t)nwl * R * 32;         // [ntx][U][W][np]
+  for (int i = tid; i < nwl * (R - U) * 32; i += blockDim.x) {
+    const int wi = i / ((R - U) * 32), rest = i - wi * (R - U) * 32;
+    gx[((size_t)wi * R + U) * 32 + rest] = 0.0f;
+  }
   const float s2 = nv ? nv[b] : 0.0f;
-  lmmse_drop_taps<TC_NP>(e, b, 4, grid, gcols, s2, gt, gls, cw, ds);  // ends with __syncthreads
-  const float* g = reinterpret_cast<const float*>(gt);  // [W][U][32]
+  switch (np) {  // the data words' systems in parallel for the usual pilot-word counts
+    case 1: lmmse_listed_word_weights<1>(e, s2, wlist, nwl, cw); break;
+    case 2: lmmse_listed_word_weights<2>(e, s2, wlist, nwl, cw); break;
+    case 3: lmmse_listed_word_weights<3>(e, s2, wlist, nwl, cw); break;
+    case 4: lmmse_listed_word_weights<4>(e, s2, wlist, nwl, cw); break;
+    default: lmmse_word_weights<kMaxPilotWords>(e, s2, cw, np); break;
+  }
+  __syncthreads();
+  const float2* gsrc = gls_ws + (int64_t)b * TC_NP * np * U;
   float mx = 0.0f;
-  for (int i = threadIdx.x; i < W * U * 2 * TC_NP; i += blockDim.x) mx = fmaxf(mx, fabsf(g[i]));
+  for (int q = tid; q < U * TC_NP; q += blockDim.x) {
+    const int u = q >> 4, pair = q & 15, t = pair % ntx;
+    float2 gl[kMaxPilotWords];
+#pragma unroll
+    for (int p = 0; p < kMaxPilotWords; ++p) gl[p] = p < np ? gsrc[(pair * np + p) * U + u] : make_float2(0.f, 0.f);
+    const float* cu = cw + ((size_t)t * U + u) * W * np;
+    for (int i = 0; i < nwl; ++i) {
+      const int w = wlist[i];
+      float2 acc = make_float2(0.f, 0.f);
+      if (w >= 0) {
+#pragma unroll
+        for (int p = 0; p < kMaxPilotWords; ++p)
+          if (p < np) {
+            const float c = cu[w * np + p];
+            acc.x = fmaf(c, gl[p].x, acc.x);
+            acc.y = fmaf(c, gl[p].y, acc.y);
+          }
+      }
+      float* row = gx + ((size_t)i * R + u) * 32;
+      row[pair] = acc.x;
+      row[16 + pair] = acc.y;
+      mx = fmaxf(mx, fmaxf(fabsf(acc.x), fabsf(acc.y)));
+    }
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  if ((tid & 31) == 0) red[tid >> 5] = mx;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     float m = 0.0f;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
     int ex = 0;
@@ -88,38 +286,27 @@ __global__ void __launch_bounds__(512, 2) k_lmmse_gains(LmmseView e, const float
   }
   __syncthreads();
   const float inv = 1.0f / sscale;
+  const int q = tid & 31;
+  const float inv_hi = q < 16 ? -inv : inv;          // k >= U: -G_im for Re rows, G_re for Im rows
+  const int step_hi = ((q ^ 16) - q) - U * 32;       // from (row k, column q) to (row k - U, column q ^ 16)
   const int kg = KP / 8;
   const size_t opel = (size_t)TC_M * KP;  // halves per operand
   uint16_t* dst = bop + (size_t)b * (nwl / TC_WORDS) * 2 * opel;
-  for (int it = threadIdx.x; it < nwl * 32 * kg; it += blockDim.x) {
-    const int row = it / kg, gk = it - row * kg;  // row over all words: pass = row / 128
-    const int pass = row / TC_N, n = row - pass * TC_N;
-    const int s = n >> 5, q = n & 31;
-    const int w = wlist[pass * TC_WORDS + s];
+  for (int it = tid >> 5; it < nwl * kg; it += blockDim.x >> 5) {
+    const int i = it / kg, gk = it - i * kg;
+    const int pass = i / TC_WORDS, n = (i - pass * TC_WORDS) * 32 + q;
+    const float* src = gx + (size_t)i * R * 32 + q;
     uint32_t hw[4], lw[4];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int k = gk * 8 + j;
-      float val = 0.0f;
-      if (w >= 0) {
-        if (k < U) {
-          val = g[((size_t)w * U + k) * 32 + q];
-        } else if (k < 2 * U) {
-          const float* rw = g + ((size_t)w * U + (k - U)) * 32;
-          val = q < 16 ? -rw[q + 16] : rw[q - 16];
-        }
-      }
-      val *= inv;
-      const __half h = __float2half_rn(val);
-      const __half l = __float2half_rn(val - __half2float(h));
-      const uint32_t hb = __half_as_ushort(h), lb = __half_as_ushort(l);
-      if (j & 1) {
-        hw[j >> 1] |= hb << 16;
-        lw[j >> 1] |= lb << 16;
-      } else {
-        hw[j >> 1] = hb;
-        lw[j >> 1] = lb;
-      }
+    for (int j = 0; j < 8; j += 2) {
+      const int k0 = gk * 8 + j, k1 = k0 + 1;
+      const float v0 = src[k0 * 32 + (k0 >= U ? step_hi : 0)] * (k0 >= U ? inv_hi : inv);
+      const float v1 = src[k1 * 32 + (k1 >= U ? step_hi : 0)] * (k1 >= U ? inv_hi : inv);
+      const __half2 h = __floats2half2_rn(v0, v1);
+      const float2 hf = __half22float2(h);
+      const __half2 l = __floats2half2_rn(v0 - hf.x, v1 - hf.y);
+      hw[j >> 1] = *reinterpret_cast<const uint32_t*>(&h);
+      lw[j >> 1] = *reinterpret_cast<const uint32_t*>(&l);
     }
     uint16_t* base = dst + (size_t)pass * 2 * opel;
     const uint32_t off = tc::kmajor_offset(n, gk * 8, KP) / 2;
@@ -312,7 +499,9 @@ void upload_raw(void** dst, const void* src, size_t bytes, cudaError_t* err) {
 }  // namespace
 
 // Host tables of the tensor-core receiver (called by hpx_lmmse_create for 4 x 4).
-hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays) {
+hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays, const std::vector<float2>& G,
+                            const std::vector<int32_t>& pw_count, const std::vector<int32_t>& pw_off,
+                            const std::vector<int32_t>& pcol) {
   const hpx_frame* fr = e->frame;
   const int N = e->N, W = e->W, FC = fr->info.num_columns, U = e->U;
   const int KP = ((2 * U + 15) / 16) * 16;
@@ -358,6 +547,54 @@ hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays) {
         int32_t& kf = kfirst[(size_t)w * mtiles + c / TC_M];
         if (kf < 0) kf = fr->h_index[(size_t)w * FC + c];
       }
+  // weighted-LS rows transposed to [pilot][tap] for the batched LS, (gr, gr, gi, gi),
+  // taps padded with zeros to 8 per thread
+  e->tc_ls_tu = U <= 24 ? 3 : 8;
+  const int up = 8 * e->tc_ls_tu;
+  std::vector<float4> gt(G.size() / U * up, make_float4(0.f, 0.f, 0.f, 0.f));
+  for (int q = 0; q < e->ntx * kMaxPilotWords; ++q) {
+    const int cnt = pw_count[q];
+    const size_t off = (size_t)pw_off[q];  // pilot word q's rows: G[off U ..], [U][cnt]
+    e->tc_cnt_max = std::max(e->tc_cnt_max, cnt);
+    for (int u = 0; u < U; ++u)
+      for (int k = 0; k < cnt; ++k) {
+        const float2 g = G[off * U + (size_t)u * cnt + k];
+        gt[(off + k) * up + u] = make_float4(g.x, g.x, g.y, g.y);
+      }
+  }
+  // column chunks of each pilot word for the batched LS: span, and per chunk and stream
+  // the range of the stream's pilots (columns increase with the pilot index)
+  std::vector<int32_t> cspan(2 * e->np);
+  for (int p = 0; p < e->np; ++p) {
+    int lo = 1 << 30, hi = -1;
+    for (int t = 0; t < e->ntx; ++t) {
+      const int q = t * kMaxPilotWords + p;
+      for (int k = 0; k < pw_count[q]; ++k) {
+        lo = std::min(lo, pcol[pw_off[q] + k]);
+        hi = std::max(hi, pcol[pw_off[q] + k]);
+      }
+    }
+    cspan[2 * p] = lo;
+    cspan[2 * p + 1] = hi - lo + 1;
+    e->tc_ls_nch_max = std::max(e->tc_ls_nch_max, (hi - lo + LS_CC) / LS_CC);
+  }
+  std::vector<int2> krange((size_t)e->np * e->tc_ls_nch_max * 4, make_int2(0, 0));
+  for (int p = 0; p < e->np; ++p)
+    for (int t = 0; t < e->ntx; ++t) {
+      const int q = t * kMaxPilotWords + p;
+      for (int k = 0; k < pw_count[q]; ++k) {
+        const int c = (pcol[pw_off[q] + k] - cspan[2 * p]) / LS_CC;
+        int2& r = krange[((size_t)p * e->tc_ls_nch_max + c) * 4 + t];
+        if (r.y == r.x) r.x = r.y = k;  // first pilot of the chunk
+        r.y = k + 1;
+      }
+    }
+  for (const int2& r : krange) e->tc_ls_kcm = std::max(e->tc_ls_kcm, r.y - r.x);
+  e->tc_ls_stages = 0;
+  for (const int st : {6, 3, 2})  // deepest pipeline that fits
+    if (!e->tc_ls_stages &&
+        lmmse_ls_smem(e->tc_ls_tu, st, e->tc_ls_kcm, e->tc_cnt_max, e->tc_ls_nch_max) <= 220 * 1024)
+      e->tc_ls_stages = st;
   e->tc_KP = KP;
   e->tc_mtiles = mtiles;
   e->tc_nwl = (int)wl.size();
@@ -371,13 +608,20 @@ hpx_status lmmse_tc_prepare(hpx_lmmse* e, const std::vector<int>& delays) {
              (size_t)kLmmseTcChunk * (wl.size() / TC_WORDS) * 2 * TC_M * KP * 2, &err);
   upload_raw(reinterpret_cast<void**>(&e->d_tc_scale), nullptr, (size_t)kLmmseTcChunk * 4, &err);
   upload_raw(reinterpret_cast<void**>(&e->d_tc_fail), nullptr, sizeof(int), &err);
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_gt), gt.data(), gt.size() * sizeof(float4), &err);
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_ls_cspan), cspan.data(), cspan.size() * 4, &err);
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_ls_krange), krange.data(), krange.size() * sizeof(int2), &err);
+  upload_raw(reinterpret_cast<void**>(&e->d_tc_gls), nullptr,
+             (size_t)kLmmseTcChunk * TC_NP * e->np * U * sizeof(float2), &err);
   if (err == cudaSuccess) err = cudaMemset(e->d_tc_fail, 0, sizeof(int));
   if (err != cudaSuccess) return hpx_cuda_status(err, "lmmse tensor-core tables");
   return HPX_OK;
 }
 
 void lmmse_tc_release(hpx_lmmse* e) {
-  void* p[] = {e->d_tc_ftab, e->d_tc_wlist, e->d_tc_kfirst, e->d_tc_bop, e->d_tc_scale, e->d_tc_fail, e->d_tc_etab};
+  void* p[] = {e->d_tc_ftab, e->d_tc_wlist, e->d_tc_kfirst, e->d_tc_bop,  e->d_tc_scale,
+               e->d_tc_fail, e->d_tc_etab,  e->d_tc_gt,     e->d_tc_gls,
+               e->d_tc_ls_cspan, e->d_tc_ls_krange};
   for (void* q : p)
     if (q) cudaFree(q);
 }
@@ -395,10 +639,20 @@ hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int
   const hpx_frame* fr = e->frame;
   QamDemapTable qt;
   HPX_TRY(qam_demap_table(fr->info.modulation_order, &qt));
-  const size_t smem_g = lmmse_taps_smem(e->W, e->U, e->np, e->ntx, TC_NP);
+  const size_t smem_g = ((size_t)e->tc_nwl * (e->tc_KP - e->U) * 32 + (size_t)e->ntx * e->U * e->W * e->np) * 4;
   const size_t smem_t = lmmse_tc_smem(e);
   if (smem_g > 220 * 1024 || smem_t > 220 * 1024)
     return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_lmmse: frame needs too much shared memory");
+  if (!e->tc_ls_stages)
+    return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_lmmse: pilot layout needs too much shared memory");
+  const int ls_st = e->tc_ls_stages, ls_tu = e->tc_ls_tu;
+  const size_t smem_ls = lmmse_ls_smem(ls_tu, ls_st, e->tc_ls_kcm, e->tc_cnt_max, e->tc_ls_nch_max);
+  auto* kls = ls_tu == 3 ? (ls_st == 6 ? k_lmmse_ls<3, 6> : ls_st == 3 ? k_lmmse_ls<3, 3> : k_lmmse_ls<3, 2>)
+                         : (ls_st == 6 ? k_lmmse_ls<8, 6> : ls_st == 3 ? k_lmmse_ls<8, 3> : k_lmmse_ls<8, 2>);
+  const int ls_drops = ls_tu == 3 ? LsShape<3>::DROPS : LsShape<8>::DROPS;
+  const int ls_threads = ls_tu == 3 ? LsShape<3>::THREADS : LsShape<8>::THREADS;
+  const LsView lsv{e->d_tc_ls_cspan, e->d_tc_ls_krange, e->tc_ls_nch_max, e->tc_ls_kcm, e->tc_cnt_max};
+  HPX_CUDA(cudaFuncSetAttribute(kls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ls));
   HPX_CUDA(cudaFuncSetAttribute(k_lmmse_gains, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g));
   HPX_CUDA(cudaFuncSetAttribute(k_lmmse_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
   const LmmseView lv = lmmse_view(e);
@@ -412,8 +666,11 @@ hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int
     const int nb = std::min(e->tc_ws_drops, B - d);
     const float2* g = grid + (int64_t)d * per_drop;
     const float* n = nv ? nv + d : nullptr;
-    k_lmmse_gains<<<nb, 512, smem_g, s>>>(lv, g, gcols, n, e->d_tc_wlist, e->tc_nwl, e->tc_KP, e->d_tc_bop,
-                                          e->d_tc_scale);
+    kls<<<dim3(e->np, (nb + ls_drops - 1) / ls_drops), ls_threads, smem_ls, s>>>(lv, lsv, e->d_tc_gt, g, gcols, nb,
+                                                                                 e->d_tc_gls);
+    HPX_LAUNCHED("lmmse_ls");
+    k_lmmse_gains<<<nb, 512, smem_g, s>>>(lv, n, e->d_tc_wlist, e->tc_nwl, e->tc_KP, e->d_tc_bop,
+                                          e->d_tc_scale, e->d_tc_gls);
     HPX_LAUNCHED("lmmse_gains");
     k_lmmse_tc<<<dim3(e->tc_mtiles, nb), TC_THREADS, smem_t, s>>>(tv, e->W, g, gcols, bulk_y, n, qt, mode, seed,
                                                                   drop0 + d, errors + d, e->d_tc_fail);
