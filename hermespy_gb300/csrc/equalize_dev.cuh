@@ -22,7 +22,10 @@ __device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], fl
   for (int j = 0; j < n; ++j) {
     float d = A[j][j].x;
 #pragma unroll
-    for (int k = 0; k < j; ++k) d -= A[j][k].x * A[j][k].x + A[j][k].y * A[j][k].y;
+    for (int k = 0; k < j; ++k) {  // d -= |A[j][k]|^2, as two fused steps
+      d = fmaf(-A[j][k].x, A[j][k].x, d);
+      d = fmaf(-A[j][k].y, A[j][k].y, d);
+    }
     ok = ok && (d > 0.0f);
     fin = fin && finite_f(d);
     inv[j] = rsqrtf(d);
@@ -32,8 +35,10 @@ __device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], fl
 #pragma unroll
       for (int k = 0; k < j; ++k) {
         // s -= A[i][k] * conj(A[j][k])
-        s.x -= A[i][k].x * A[j][k].x + A[i][k].y * A[j][k].y;
-        s.y -= A[i][k].y * A[j][k].x - A[i][k].x * A[j][k].y;
+        s.x = fmaf(-A[i][k].x, A[j][k].x, s.x);
+        s.x = fmaf(-A[i][k].y, A[j][k].y, s.x);
+        s.y = fmaf(-A[i][k].y, A[j][k].x, s.y);
+        s.y = fmaf(A[i][k].x, A[j][k].y, s.y);
       }
       A[i][j] = cscale(s, inv[j]);
     }
@@ -43,14 +48,24 @@ __device__ __forceinline__ bool chol_solve(float2 (&A)[n][n], float2 (&b)[n], fl
   for (int i = 0; i < n; ++i) {
     float2 s = b[i];
 #pragma unroll
-    for (int k = 0; k < i; ++k) s = csub(s, cmul(A[i][k], z[k]));
+    for (int k = 0; k < i; ++k) {  // s -= A[i][k] z[k]
+      s.x = fmaf(-A[i][k].x, z[k].x, s.x);
+      s.x = fmaf(A[i][k].y, z[k].y, s.x);
+      s.y = fmaf(-A[i][k].x, z[k].y, s.y);
+      s.y = fmaf(-A[i][k].y, z[k].x, s.y);
+    }
     z[i] = cscale(s, inv[i]);
   }
 #pragma unroll
   for (int i = n - 1; i >= 0; --i) {
     float2 s = z[i];
 #pragma unroll
-    for (int k = i + 1; k < n; ++k) s = csub(s, cmulc(A[k][i], x[k]));
+    for (int k = i + 1; k < n; ++k) {  // s -= conj(A[k][i]) x[k]
+      s.x = fmaf(-A[k][i].x, x[k].x, s.x);
+      s.x = fmaf(-A[k][i].y, x[k].y, s.x);
+      s.y = fmaf(-A[k][i].x, x[k].y, s.y);
+      s.y = fmaf(A[k][i].y, x[k].x, s.y);
+    }
     x[i] = cscale(s, inv[i]);
   }
   return ok;
@@ -112,14 +127,19 @@ __device__ __forceinline__ bool equalize_one(int mode, const float2 (&H)[NRX][NT
     for (int r = 0; r < NRX; ++r) cfmac(mf, H[r][i], y[r]);
     b[i] = mf;
 #pragma unroll
-    for (int j = 0; j <= i; ++j) {
+    for (int j = 0; j < i; ++j) {
       float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
       for (int r = 0; r < NRX; ++r) cfmac(acc, H[r][i], H[r][j]);  // (H^H H)[i][j] = sum_r conj(H[r][i]) H[r][j]
       A[i][j] = acc;
     }
-    A[i][i].x += reg;
-    A[i][i].y = 0.0f;
+    float d = 0.0f;  // the diagonal's real part, summed as cfmac sums it
+#pragma unroll
+    for (int r = 0; r < NRX; ++r) {
+      d = fmaf(H[r][i].x, H[r][i].x, d);
+      d = fmaf(H[r][i].y, H[r][i].y, d);
+    }
+    A[i][i] = make_float2(d + reg, 0.0f);
   }
   if (!chol_solve<NTX>(A, b, x, fin)) {
 #pragma unroll

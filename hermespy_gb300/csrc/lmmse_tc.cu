@@ -401,6 +401,16 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS) k_lmmse_tc(TcView v, int 
       }
       ++issued;
     }
+    // this thread's two word slots: word, data element index (-1: none), first
+    // element of the word in the tile, loaded ahead of the bits and the waits
+    int wsl[2], ksl[2], kfsl[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int w = v.wlist[p * TC_WORDS + (warp >> 2) + 2 * j];
+      ksl[j] = (w >= 0 && c < v.FC) ? v.etab[w * v.FC + c] : -1;
+      kfsl[j] = w >= 0 ? v.kfirst[w * v.mtiles + mt] : 0;
+      wsl[j] = w;
+    }
     // ---- Philox bits of the elements of the pass's rows in this tile
     for (int it = tid; it < TC_WORDS * 4 * TC_BITBLK; it += TC_THREADS) {
       const int s = it / (4 * TC_BITBLK), r = it - s * 4 * TC_BITBLK;
@@ -437,9 +447,9 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS) k_lmmse_tc(TcView v, int 
     // ---- epilogue: thread = subcarrier (TMEM lane), two word slots per warp
 #pragma unroll 1
     for (int s = warp >> 2; s < TC_WORDS; s += 2) {
-      const int w = v.wlist[p * TC_WORDS + s];
-      const bool mine = ok && w >= 0 && c < v.FC;
-      const int k = mine ? v.etab[w * v.FC + c] : -1;  // data element index, -1: not a data element
+      const bool second = s >= 2;
+      const int w = second ? wsl[1] : wsl[0];
+      const int k = ok ? (second ? ksl[1] : ksl[0]) : -1;  // data element index, -1: not a data element
       float2 y[4];
 #pragma unroll
       for (int r = 0; r < 4; ++r)
@@ -454,7 +464,7 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS) k_lmmse_tc(TcView v, int 
 #pragma unroll
         for (int t = 0; t < 4; ++t) A[r][t] = make_float2(acc[r * 4 + t], acc[16 + r * 4 + t]);
       fin &= equalize_one<4, 4>(mode, A, y, s2a, x);
-      const int kf = v.kfirst[w * v.mtiles + mt];
+      const int kf = second ? kfsl[1] : kfsl[0];
       const int64_t pos = (int64_t)k * m - ((((int64_t)kf * m) >> 7) << 7);
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
