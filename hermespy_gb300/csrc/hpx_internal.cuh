@@ -375,12 +375,12 @@ __host__ __device__ __forceinline__ float2 qam_symbol(int order, uint32_t v) {
 template <int PB>
 __device__ __forceinline__ uint32_t pam_decide(const QamDemapTable& t, float x) {
   const float ax = fabsf(x);
-  uint32_t v = (x < 0.0f && ax < INFINITY) ? 1u : 0u;
+  uint32_t v = ((x < 0.0f) & (ax < INFINITY)) ? 1u : 0u;  // plain compares, no short circuits
 #pragma unroll
   for (int i = 1; i < PB; ++i) {
     bool in = false;
 #pragma unroll
-    for (int k = 0; k < i; ++k) in = in || (ax > t.lo[i][k] && ax < t.hi[i][k]);
+    for (int k = 0; k < i; ++k) in |= (ax > t.lo[i][k]) & (ax < t.hi[i][k]);
     v = (v << 1) | (in ? 1u : 0u);
   }
   return v;
@@ -394,6 +394,16 @@ __device__ __forceinline__ uint32_t qam_decide_pb(const QamDemapTable& t, float2
 #pragma unroll
   for (int i = PB - 1; i >= 0; --i) v = (v << 2) | (((re >> i) & 1u) << 1) | ((im >> i) & 1u);
   return v;
+}
+
+// qam_decide for a modulation order known at compile time.
+template <int ORDER>
+__device__ __forceinline__ uint32_t qam_decide_t(const QamDemapTable& t, float2 y) {
+  if constexpr (ORDER == 2) return (y.x < 0.0f) ? 1u : 0u;
+  else if constexpr (ORDER == 4) return ((y.x < 0.0f) ? 2u : 0u) | ((y.y < 0.0f) ? 1u : 0u);
+  else if constexpr (ORDER == 16) return qam_decide_pb<2>(t, y);
+  else if constexpr (ORDER == 64) return qam_decide_pb<3>(t, y);
+  else return qam_decide_pb<4>(t, y);
 }
 
 __device__ __forceinline__ uint32_t qam_decide(const QamDemapTable& t, float2 y) {

@@ -327,6 +327,7 @@ __global__ void __launch_bounds__(512, 2) k_lmmse_gains(LmmseView e, const float
 // The equalizer works on the unscaled GEMM output A = H / scale with the regularizer
 // s2 / scale^2 and divides the solution by scale: the scale is a power of two, so
 // the result is the one of H itself.
+template <int ORDER>  // modulation order: the demapper's branches and the bit widths are fixed
 __global__ void __launch_bounds__(TC_THREADS, TC_CTAS) k_lmmse_tc(TcView v, int W, const float2* __restrict__ grid,
                                                                   int gcols, int bulk_y, const float* __restrict__ nv,
                                                                   const __grid_constant__ QamDemapTable qt, int mode,
@@ -337,7 +338,8 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS) k_lmmse_tc(TcView v, int 
   __shared__ uint32_t tmem_slot;
   const int mt = blockIdx.x, b = blockIdx.y;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int KP = v.KP, m = v.m;
+  constexpr int m = ORDER == 2 ? 1 : ORDER == 4 ? 2 : ORDER == 16 ? 4 : ORDER == 64 ? 6 : 8;
+  const int KP = v.KP;
   const uint32_t opbytes = (uint32_t)TC_M * KP * 2;  // one 128-row FP16 operand
   unsigned char* a_hi = sm;
   unsigned char* a_lo = sm + opbytes;
@@ -468,7 +470,7 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS) k_lmmse_tc(TcView v, int 
       const int64_t pos = (int64_t)k * m - ((((int64_t)kf * m) >> 7) << 7);
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
-        const uint32_t rx_v = qam_decide(qt, make_float2(x[t].x * inv_scl, x[t].y * inv_scl));
+        const uint32_t rx_v = qam_decide_t<ORDER>(qt, make_float2(x[t].x * inv_scl, x[t].y * inv_scl));
         const uint32_t tx_v = extract_bits_msb(bits + (size_t)(s * 4 + t) * TC_BITBLK * 4, pos, m);
         local += __popc(rx_v ^ tx_v);
       }
@@ -664,7 +666,10 @@ hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int
   const LsView lsv{e->d_tc_ls_cspan, e->d_tc_ls_krange, e->tc_ls_nch_max, e->tc_ls_kcm, e->tc_cnt_max};
   HPX_CUDA(cudaFuncSetAttribute(kls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ls));
   HPX_CUDA(cudaFuncSetAttribute(k_lmmse_gains, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g));
-  HPX_CUDA(cudaFuncSetAttribute(k_lmmse_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
+  const int order = fr->info.modulation_order;
+  auto* ktc = order == 2 ? k_lmmse_tc<2> : order == 4 ? k_lmmse_tc<4> : order == 16 ? k_lmmse_tc<16>
+            : order == 64 ? k_lmmse_tc<64> : k_lmmse_tc<256>;  // qam_demap_table accepted the order
+  HPX_CUDA(cudaFuncSetAttribute(ktc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
   const LmmseView lv = lmmse_view(e);
   TcView tv{e->W, fr->info.num_columns, e->U, e->tc_KP, e->tc_mtiles, e->tc_nwl, fr->info.bits_per_symbol,
             e->d_tc_wlist, e->d_tc_kfirst, e->d_tc_etab, e->d_tc_ftab, e->d_tc_bop, e->d_tc_scale};
@@ -682,7 +687,7 @@ hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int
     k_lmmse_gains<<<nb, 512, smem_g, s>>>(lv, n, e->d_tc_wlist, e->tc_nwl, e->tc_KP, e->d_tc_bop,
                                           e->d_tc_scale, e->d_tc_gls);
     HPX_LAUNCHED("lmmse_gains");
-    k_lmmse_tc<<<dim3(e->tc_mtiles, nb), TC_THREADS, smem_t, s>>>(tv, e->W, g, gcols, bulk_y, n, qt, mode, seed,
+    ktc<<<dim3(e->tc_mtiles, nb), TC_THREADS, smem_t, s>>>(tv, e->W, g, gcols, bulk_y, n, qt, mode, seed,
                                                                   drop0 + d, errors + d, e->d_tc_fail);
     HPX_LAUNCHED("lmmse_tc");
   }
