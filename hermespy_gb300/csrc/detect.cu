@@ -150,11 +150,13 @@ __global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_ideal
       for (int t = 0; t < NTX; ++t) H[r][t] = cmul(Sm[r * NTX + t], g);  // the ideal CSI of hpx_fading_ideal_csi
     }
     fin &= equalize_one<NRX, NTX>(mode, H, y, s2, x);
+    // streams the equalizer does not return are received as zero bits
+    // (BitErrorEvaluator zero-pads the shorter sequence)
+    uint32_t dec[NTX];
+    qam_decide_n<NTX>(qt, x, out_streams, dec);
 #pragma unroll
     for (int t = 0; t < NTX; ++t) {
-      // streams the equalizer does not return are received as zero bits
-      // (BitErrorEvaluator zero-pads the shorter sequence)
-      const uint32_t rx_v = t < out_streams ? qam_decide(qt, x[t]) : 0u;
+      const uint32_t rx_v = dec[t];
       const uint32_t tx_v = extract_bits_msb(bitsm + t * BW - wofs, k * m, m);
       local += __popc(rx_v ^ tx_v);
     }
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(csi_max_threads<NRX, NTX>(), csi_small<NRX, NT
     }
     fin &= equalize_one<NRX, NTX>(mode, H, y, s2, x);
 #pragma unroll
-    for (int t = 0; t < NTX; ++t) {
+    for (int t = 0; t < NTX; ++t) {  // decided stream by stream: qam_decide_n spills in this kernel
       const uint32_t rx_v = t < out_streams ? qam_decide(qt, x[t]) : 0u;
       const uint32_t tx_v = extract_bits_msb(bitsm + t * BW - wofs, k * m, m);
       local += __popc(rx_v ^ tx_v);
@@ -259,9 +261,11 @@ __global__ void __launch_bounds__(LMMSE_THREADS, 2) k_detect_lmmse(LmmseView e, 
       for (int t = 0; t < NTX; ++t) H[r][t] = hp[r * NTX + t];
     }
     fin &= equalize_one<NRX, NTX>(mode, H, y, s2, x);
+    uint32_t dec[NTX];
+    qam_decide_n<NTX>(qt, x, out_streams, dec);
 #pragma unroll
     for (int t = 0; t < NTX; ++t) {
-      const uint32_t rx_v = t < out_streams ? qam_decide(qt, x[t]) : 0u;
+      const uint32_t rx_v = dec[t];
       const uint32_t tx_v = extract_bits_msb(bitsm + t * BW, (int64_t)k * m, m);
       local += __popc(rx_v ^ tx_v);
     }

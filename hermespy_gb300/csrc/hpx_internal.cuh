@@ -406,6 +406,27 @@ __device__ __forceinline__ uint32_t qam_decide_t(const QamDemapTable& t, float2 
   else return qam_decide_pb<4>(t, y);
 }
 
+template <int ORDER, int NTX>
+__device__ __forceinline__ void qam_decide_all(const QamDemapTable& t, const float2 (&x)[NTX], int n,
+                                               uint32_t (&v)[NTX]) {
+#pragma unroll
+  for (int i = 0; i < NTX; ++i) v[i] = i < n ? qam_decide_t<ORDER>(t, x[i]) : 0u;
+}
+
+// Hard decisions of the NTX equalized streams of one element, zero for streams at or
+// past n: one branch on the order for all of them.
+template <int NTX>
+__device__ __forceinline__ void qam_decide_n(const QamDemapTable& t, const float2 (&x)[NTX], int n,
+                                             uint32_t (&v)[NTX]) {
+  switch (t.order) {
+    case 2: qam_decide_all<2>(t, x, n, v); break;
+    case 4: qam_decide_all<4>(t, x, n, v); break;
+    case 16: qam_decide_all<16>(t, x, n, v); break;
+    case 64: qam_decide_all<64>(t, x, n, v); break;
+    default: qam_decide_all<256>(t, x, n, v); break;
+  }
+}
+
 __device__ __forceinline__ uint32_t qam_decide(const QamDemapTable& t, float2 y) {
   switch (t.order) {
     case 2: return (y.x < 0.0f) ? 1u : 0u;

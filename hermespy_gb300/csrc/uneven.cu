@@ -360,9 +360,11 @@ __device__ __forceinline__ unsigned int u_element(int mode, float2 g, const floa
   }
   fin &= equalize_one<NRX, NTX>(mode, H, yv, s2, xv);
   unsigned int e = 0;
+  uint32_t dec[NTX];
+  qam_decide_n<NTX>(qt, xv, out_streams, dec);
 #pragma unroll
   for (int t = 0; t < NTX; ++t) {
-    const uint32_t rx_v = t < out_streams ? qam_decide(qt, xv[t]) : 0u;
+    const uint32_t rx_v = dec[t];
     const uint32_t tx_v = extract_bits_msb(bitsm + t * BW - wofs, k * m, m);
     e += __popc(rx_v ^ tx_v);
   }
