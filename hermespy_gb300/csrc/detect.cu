@@ -719,7 +719,10 @@ hpx_status hpx_detect_lmmse(const hpx_lmmse* lm, int32_t nrx, int32_t mode, cons
   if (!((nrx == 1 && ntx == 1) || (nrx == 2 && ntx == 2) || (nrx == 4 && ntx == 4) || (nrx == 4 && ntx == 2) ||
         (nrx == 2 && ntx == 1) || (nrx == 4 && ntx == 1)))
     return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_lmmse: %dx%d antennas not supported", nrx, ntx);
-  if (nrx == 4 && ntx == 4 && lm->d_tc_ftab) {  // tensor-core response GEMM (lmmse_tc.cu)
+  // tensor-core response GEMM (lmmse_tc.cu). Its batched pilot LS stages at most 8 pilots
+  // of a stream per 32 columns under the comb of 4 that 4 streams need; a layout whose
+  // staging would not fit shared memory takes the FP32 kernel below instead.
+  if (nrx == 4 && ntx == 4 && lm->d_tc_ftab && lm->tc_ls_stages > 0) {
     cudaStream_t s = as_stream(stream);
     HPX_CUDA(cudaMemsetAsync(errors, 0, sizeof(uint32_t) * B, s));
     return lmmse_tc_detect(lm, mode, reinterpret_cast<const float2*>(grid), gcols, nv, seed, drop0, B, errors, s);

@@ -655,7 +655,7 @@ hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int
   const size_t smem_t = lmmse_tc_smem(e);
   if (smem_g > 220 * 1024 || smem_t > 220 * 1024)
     return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_lmmse: frame needs too much shared memory");
-  if (!e->tc_ls_stages)
+  if (!e->tc_ls_stages)  // the caller routes such layouts to the FP32 receiver
     return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_lmmse: pilot layout needs too much shared memory");
   const int ls_st = e->tc_ls_stages, ls_tu = e->tc_ls_tu;
   const size_t smem_ls = lmmse_ls_smem(ls_tu, ls_st, e->tc_ls_kcm, e->tc_cnt_max, e->tc_ls_nch_max);

@@ -179,3 +179,48 @@ def test_fused_lmmse_receiver_matches_staged():
     assert np.all(a > 0)
     assert np.all(np.abs(a.astype(np.int64) - b.astype(np.int64)) <= np.maximum(2, a // 1000)), (a, b)
     _lib.call("hpx_lmmse_destroy", lm)
+
+
+def test_fused_robust_receiver_matches_staged():
+    """hpx_detect_lmmse with design statistics (64 tap delays) counts the errors of
+    hpx_lmmse_estimate + hpx_detect_csi on the same drops: the tensor-core receiver with
+    the batched pilot LS at eight taps per thread (the genie estimator's 23 taps take
+    three)."""
+
+    import types
+
+    from hermespy_gb300.estimation import robust_statistics
+
+    lay = FrameLayout(pilot_frame(64, 4))
+    cfg = mimo_channel()
+    fh = frame_handle(lay)
+    h = fading_handle(cfg, 4, 4, FS)
+    nd = 3
+    st = h.new_state(nd)
+    _lib.call("hpx_fading_realize", h.handle, SEED, 0, nd, _lib.ptr(st), stream())
+    T, D = lay.samples_per_frame, h.max_delay
+    x = torch.empty((nd, 4, T), dtype=torch.complex64, device="cuda")
+    _lib.call("hpx_ofdm_modulate_bits", fh, SEED, 0, nd, 4, _lib.ptr(x), stream())
+    y = torch.empty((nd, 4, T + D), dtype=torch.complex64, device="cuda")
+    p3 = torch.full((nd,), 10 ** (-1.5), dtype=torch.float32, device="cuda")
+    _lib.call("hpx_fading_propagate", h.handle, _lib.ptr(st), nd, _lib.ptr(x), T, _lib.ptr(y), _lib.ptr(p3), SEED, 0,
+              stream())
+    C, W = lay.num_used, lay.num_words
+    grid = torch.empty((nd, 4, W, C), dtype=torch.complex64, device="cuda")
+    _lib.call("hpx_ofdm_demodulate", fh, _lib.ptr(y), T + D, nd * 4, C, _lib.ptr(grid), stream())
+    design, ridge = robust_statistics(types.SimpleNamespace(gain=cfg.gain, power_profile=cfg.power_profile), FS)
+    dh = design.handle(4, 4, FS)
+    lm = ctypes.c_void_p()
+    _lib.check(_lib.load().hpx_lmmse_create_regularized(fh, dh.handle, C, float(ridge), ctypes.byref(lm)))
+    est = torch.empty((nd, 4, 4, W, C), dtype=torch.complex64, device="cuda")
+    _lib.call("hpx_lmmse_estimate", lm, _lib.ptr(grid), C, 4, nd, _lib.ptr(p3), _lib.ptr(est), stream())
+    e1 = torch.empty(nd, dtype=torch.int32, device="cuda")
+    _lib.call("hpx_detect_csi", fh, 4, 4, _lib.EQ_LMMSE, _lib.ptr(grid), C, _lib.ptr(est), C, _lib.ptr(p3), SEED, 0, nd,
+              _lib.ptr(e1), stream())
+    e2 = torch.empty(nd, dtype=torch.int32, device="cuda")
+    _lib.call("hpx_detect_lmmse", lm, 4, _lib.EQ_LMMSE, _lib.ptr(grid), C, _lib.ptr(p3), SEED, 0, nd, _lib.ptr(e2),
+              stream())
+    a, b = host(e1).astype(np.int64), host(e2).astype(np.int64)
+    assert np.all(a > 0)
+    assert np.all(np.abs(a - b) <= np.maximum(2, a // 1000)), (a, b)
+    _lib.call("hpx_lmmse_destroy", lm)
