@@ -372,23 +372,38 @@ __host__ __device__ __forceinline__ float2 qam_symbol(int order, uint32_t v) {
 // Bit i (1 <= i < PB) of a PAM axis is 1 on i open intervals of |x|. Kernels pass
 // the table as a __grid_constant__ parameter, so every bound is a constant-bank
 // operand of its compare.
-template <int PB>
+// The tables' intervals have a fixed shape (checked where qam_demap_table builds them):
+// bit i has i intervals, the first of them open below (lower bound -1, below every |x|)
+// for i >= 2 and the last open above (upper bound +inf). So the lower test of such a
+// first interval only rejects NaN, which its upper test rejects too, and the upper test
+// of a last interval is the sign bit's finiteness test: both are shared, not repeated.
+__host__ __device__ constexpr bool pam_interval_open_below(int i, int k) { return k == 0 && i >= 2; }
+__host__ __device__ constexpr bool pam_interval_open_above(int i, int k) { return k == i - 1; }
+
+// SHARED: use that shape (fewer compares); otherwise every bound is tested, which the
+// register-tight CSI receiver compiles without spills. Both decide the same bits.
+template <int PB, bool SHARED = true>
 __device__ __forceinline__ uint32_t pam_decide(const QamDemapTable& t, float x) {
   const float ax = fabsf(x);
-  uint32_t v = ((x < 0.0f) & (ax < INFINITY)) ? 1u : 0u;  // plain compares, no short circuits
+  const bool fin = ax < INFINITY;
+  uint32_t v = ((x < 0.0f) & fin) ? 1u : 0u;  // plain compares, no short circuits
 #pragma unroll
   for (int i = 1; i < PB; ++i) {
     bool in = false;
 #pragma unroll
-    for (int k = 0; k < i; ++k) in |= (ax > t.lo[i][k]) & (ax < t.hi[i][k]);
+    for (int k = 0; k < i; ++k) {
+      const bool above = (SHARED && pam_interval_open_below(i, k)) ? true : (ax > t.lo[i][k]);
+      const bool below = (SHARED && pam_interval_open_above(i, k)) ? fin : (ax < t.hi[i][k]);
+      in |= above & below;
+    }
     v = (v << 1) | (in ? 1u : 0u);
   }
   return v;
 }
 
-template <int PB>
+template <int PB, bool SHARED = true>
 __device__ __forceinline__ uint32_t qam_decide_pb(const QamDemapTable& t, float2 y) {
-  const uint32_t re = pam_decide<PB>(t, y.x), im = pam_decide<PB>(t, y.y);
+  const uint32_t re = pam_decide<PB, SHARED>(t, y.x), im = pam_decide<PB, SHARED>(t, y.y);
   // interleave: b0 = re0, b1 = im0, b2 = re1, ... (MSB first)
   uint32_t v = 0;
 #pragma unroll
@@ -431,9 +446,9 @@ __device__ __forceinline__ uint32_t qam_decide(const QamDemapTable& t, float2 y)
   switch (t.order) {
     case 2: return (y.x < 0.0f) ? 1u : 0u;
     case 4: return ((y.x < 0.0f) ? 2u : 0u) | ((y.y < 0.0f) ? 1u : 0u);
-    case 16: return qam_decide_pb<2>(t, y);
-    case 64: return qam_decide_pb<3>(t, y);
-    default: return qam_decide_pb<4>(t, y);
+    case 16: return qam_decide_pb<2, false>(t, y);
+    case 64: return qam_decide_pb<3, false>(t, y);
+    default: return qam_decide_pb<4, false>(t, y);
   }
 }
 

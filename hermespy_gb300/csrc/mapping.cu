@@ -99,9 +99,13 @@ hpx_status qam_demap_table(int32_t order, QamDemapTable* out) {
       else if (order == 64) { ivs = PAM8[i]; n = PAM8_N[i]; }
       else { ivs = PAM16[i]; n = PAM16_N[i]; }
       t.count[i] = n;
+      if (n != i) return hpx_fail(HPX_ERR_UNSUPPORTED, "demap table: bit %d has %d intervals", i, n);
       for (int k = 0; k < n; ++k) {
         t.lo[i][k] = ivs[k].a < 0 ? -1.0f : x_upper(ivs[k].a, c);
         t.hi[i][k] = ivs[k].b >= INF ? INFINITY : x_lower(ivs[k].b, c);
+        // the shape pam_decide relies on
+        if ((ivs[k].a < 0) != pam_interval_open_below(i, k) || (ivs[k].b >= INF) != pam_interval_open_above(i, k))
+          return hpx_fail(HPX_ERR_UNSUPPORTED, "demap table: interval %d of bit %d has an unexpected shape", k, i);
       }
     }
     g_tables[slot] = t;
