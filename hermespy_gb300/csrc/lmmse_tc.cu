@@ -666,6 +666,9 @@ hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int
   const LsView lsv{e->d_tc_ls_cspan, e->d_tc_ls_krange, e->tc_ls_nch_max, e->tc_ls_kcm, e->tc_cnt_max};
   HPX_CUDA(cudaFuncSetAttribute(kls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ls));
   HPX_CUDA(cudaFuncSetAttribute(k_lmmse_gains, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g));
+  // gains CTAs of 256 threads where four fit an SM (their phases keep few threads busy,
+  // so more CTAs overlap better), else 512 (e.g. 64 design taps: one CTA per SM)
+  const int gthreads = smem_g <= 56 * 1024 ? 256 : 512;
   const int order = fr->info.modulation_order;
   auto* ktc = order == 2 ? k_lmmse_tc<2> : order == 4 ? k_lmmse_tc<4> : order == 16 ? k_lmmse_tc<16>
             : order == 64 ? k_lmmse_tc<64> : k_lmmse_tc<256>;  // qam_demap_table accepted the order
@@ -684,7 +687,7 @@ hpx_status lmmse_tc_detect(const hpx_lmmse* e, int mode, const float2* grid, int
     kls<<<dim3(e->np, (nb + ls_drops - 1) / ls_drops), ls_threads, smem_ls, s>>>(lv, lsv, e->d_tc_gt, g, gcols, nb,
                                                                                  e->d_tc_gls);
     HPX_LAUNCHED("lmmse_ls");
-    k_lmmse_gains<<<nb, 512, smem_g, s>>>(lv, n, e->d_tc_wlist, e->tc_nwl, e->tc_KP, e->d_tc_bop,
+    k_lmmse_gains<<<nb, gthreads, smem_g, s>>>(lv, n, e->d_tc_wlist, e->tc_nwl, e->tc_KP, e->d_tc_bop,
                                           e->d_tc_scale, e->d_tc_gls);
     HPX_LAUNCHED("lmmse_gains");
     ktc<<<dim3(e->tc_mtiles, nb), TC_THREADS, smem_t, s>>>(tv, e->W, g, gcols, bulk_y, n, qt, mode, seed,
