@@ -124,13 +124,20 @@ __global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_ideal
   float2* hb = reinterpret_cast<float2*>(smem4);
   float2* scratch = hb + fc.L;
   float2* Sm = scratch + fc.L * fc.S1;
-  int* ds = reinterpret_cast<int*>(Sm + NRX * NTX);
+  float2* Mg = Sm + NRX * NTX;  // S^H S
+  int* ds = reinterpret_cast<int*>(Mg + NTX * NTX);
   uint32_t* bitsm = reinterpret_cast<uint32_t*>(ds + fc.L + 4);
   const int64_t k0 = data_offset[w];
   const int nd = num_data_word[w];
   for (int l = threadIdx.x; l < fc.L; l += blockDim.x) ds[l] = fc.delay[l];
   const float2* Sg = v.spatial(b);
   for (int i = threadIdx.x; i < NRX * NTX; i += blockDim.x) Sm[i] = Sg[i];
+  for (int q = threadIdx.x; q < NTX * NTX; q += blockDim.x) {
+    const int i = q / NTX, j = q - i * NTX;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int r = 0; r < NRX; ++r) cfmac(acc, Sg[r * NTX + i], Sg[r * NTX + j]);
+    Mg[q] = acc;
+  }
   stage_bits(bitsm, BW, NTX, seed, drop0 + b, k0, nd, m);
   tap_averages(fc, v.W(b), v.P0(b), window_start[w], N, hb, scratch);  // ends with __syncthreads
   const int64_t wofs = (((k0 * m) >> 5) >> 2) * 4;
@@ -142,14 +149,19 @@ __global__ void __launch_bounds__(detect_max_threads<NRX, NTX>()) k_detect_ideal
     const int64_t k = k0 + j;
     const int c = data_column[k];
     const float2 g = tap_response(fc, hb, ds, tw, bins[c], N);
-    float2 H[NRX][NTX], y[NRX], x[NTX];
+    float2 y[NRX], x[NTX];
 #pragma unroll
-    for (int r = 0; r < NRX; ++r) {
-      y[r] = grid[(((int64_t)b * NRX + r) * W + w) * gcols + c];
+    for (int r = 0; r < NRX; ++r) y[r] = grid[(((int64_t)b * NRX + r) * W + w) * gcols + c];
+    if (gram_equalizer<NRX, NTX>(mode)) {  // H = S g: the Gram from S^H S (uniform branch)
+      fin &= equalize_spatial<NRX, NTX>(mode, Sm, Mg, g, y, s2, x);
+    } else {
+      float2 H[NRX][NTX];
 #pragma unroll
-      for (int t = 0; t < NTX; ++t) H[r][t] = cmul(Sm[r * NTX + t], g);  // the ideal CSI of hpx_fading_ideal_csi
+      for (int r = 0; r < NRX; ++r)
+#pragma unroll
+        for (int t = 0; t < NTX; ++t) H[r][t] = cmul(Sm[r * NTX + t], g);  // the ideal CSI of hpx_fading_ideal_csi
+      fin &= equalize_one<NRX, NTX>(mode, H, y, s2, x);
     }
-    fin &= equalize_one<NRX, NTX>(mode, H, y, s2, x);
     // streams the equalizer does not return are received as zero bits
     // (BitErrorEvaluator zero-pads the shorter sequence)
     uint32_t dec[NTX];
@@ -426,7 +438,7 @@ hpx_status launch_detect_ideal(const hpx_fading* f, const void* state, const hpx
   const FadingConst fc = fading_const(f);
   const int C = fr->info.num_columns, m = fr->info.bits_per_symbol;
   const int BW = staged_bit_words(C, m);
-  const size_t smem = (size_t)fc.L * sizeof(float2) * (1 + fc.S1) + NRX * NTX * sizeof(float2) +
+  const size_t smem = (size_t)fc.L * sizeof(float2) * (1 + fc.S1) + (NRX + NTX) * NTX * sizeof(float2) +
                       (fc.L + 4) * sizeof(int) + (size_t)NTX * BW * 4 + 16;
   auto kern = k_detect_ideal<NRX, NTX>;
   if (smem > 48 * 1024) HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -148,3 +148,42 @@ __device__ __forceinline__ bool equalize_one(int mode, const float2 (&H)[NRX][NT
   return fin;
 }
 
+// Where equalize_spatial replaces equalize_one: LMMSE, whose regularized system keeps
+// the rounding of a Gram formed from S^H S at the level of one formed per element. ZF
+// solves the unregularized system, where near-singular elements turn that rounding
+// into different decisions, so it keeps the per-element arithmetic of the staged
+// receiver it is tested against bit for bit.
+template <int NRX, int NTX>
+__host__ __device__ constexpr bool gram_equalizer(int mode) {
+  return mode == HPX_EQ_LMMSE;
+}
+
+// equalize_one for a channel H = S g: a spatial matrix S (Sm, [NRX][NTX]) fixed over the
+// drop times one scalar response g per element, the ideal CSI of the fading model. Then
+// H^H H = |g|^2 S^H S and H^H y = conj(g) S^H y, with M = S^H S ([NTX][NTX]) formed once
+// per drop: per element the Gram is NTX (NTX + 1) / 2 scalings instead of NRX NTX^2 / 2
+// complex products, and H is never formed. The same system up to rounding (LMMSE: the
+// regularizer is s2).
+template <int NRX, int NTX>
+__device__ __forceinline__ bool equalize_spatial(int mode, const float2* __restrict__ Sm, const float2* __restrict__ M,
+                                                 float2 g, const float2 (&y)[NRX], float s2, float2 (&x)[NTX]) {
+  const float reg = s2;
+  const float gg = fmaf(g.x, g.x, g.y * g.y);
+  float2 A[NTX][NTX], b[NTX];
+#pragma unroll
+  for (int i = 0; i < NTX; ++i) {
+    float2 mf = make_float2(0.f, 0.f);  // (S^H y)_i
+#pragma unroll
+    for (int r = 0; r < NRX; ++r) cfmac(mf, Sm[r * NTX + i], y[r]);
+    b[i] = cmulc(g, mf);
+#pragma unroll
+    for (int j = 0; j < i; ++j) A[i][j] = cscale(M[i * NTX + j], gg);
+    A[i][i] = make_float2(fmaf(M[i * NTX + i].x, gg, reg), 0.0f);
+  }
+  bool fin = true;
+  if (!chol_solve<NTX>(A, b, x, fin)) {
+#pragma unroll
+    for (int t = 0; t < NTX; ++t) x[t] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+  }
+  return fin;
+}

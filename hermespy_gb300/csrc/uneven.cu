@@ -346,19 +346,24 @@ __device__ void u_propagate(const UDrop& d, const FadingConst& fc, int T, const 
 // Ideal CSI + equalization + demap + count of one element (k_detect_ideal); `fin`
 // turns false on a non-finite equalizer pivot.
 template <int NRX, int NTX>
-__device__ __forceinline__ unsigned int u_element(int mode, float2 g, const float2* Sm, const float2* grid, int W,
-                                                  int C, int w, int c, float s2, const QamDemapTable& qt,
-                                                  const uint32_t* bitsm, int BW, int64_t wofs, int64_t k, int m,
-                                                  bool& fin) {
+__device__ __forceinline__ unsigned int u_element(int mode, float2 g, const float2* Sm, const float2* Mg,
+                                                  const float2* grid, int W, int C, int w, int c, float s2,
+                                                  const QamDemapTable& qt, const uint32_t* bitsm, int BW,
+                                                  int64_t wofs, int64_t k, int m, bool& fin) {
   const int out_streams = (mode == HPX_EQ_ZF && NRX == 1) ? 1 : NTX;
-  float2 H[NRX][NTX], yv[NRX], xv[NTX];
+  float2 yv[NRX], xv[NTX];
 #pragma unroll
-  for (int r = 0; r < NRX; ++r) {
-    yv[r] = grid[((int64_t)r * W + w) * C + c];
+  for (int r = 0; r < NRX; ++r) yv[r] = grid[((int64_t)r * W + w) * C + c];
+  if (gram_equalizer<NRX, NTX>(mode)) {  // H = S g: the Gram from S^H S
+    fin &= equalize_spatial<NRX, NTX>(mode, Sm, Mg, g, yv, s2, xv);
+  } else {
+    float2 H[NRX][NTX];
 #pragma unroll
-    for (int t = 0; t < NTX; ++t) H[r][t] = cmul(Sm[r * NTX + t], g);
+    for (int r = 0; r < NRX; ++r)
+#pragma unroll
+      for (int t = 0; t < NTX; ++t) H[r][t] = cmul(Sm[r * NTX + t], g);
+    fin &= equalize_one<NRX, NTX>(mode, H, yv, s2, xv);
   }
-  fin &= equalize_one<NRX, NTX>(mode, H, yv, s2, xv);
   unsigned int e = 0;
   uint32_t dec[NTX];
   qam_decide_n<NTX>(qt, xv, out_streams, dec);
@@ -372,18 +377,18 @@ __device__ __forceinline__ unsigned int u_element(int mode, float2 g, const floa
 }
 
 template <int NRX, int MAXA>
-__device__ __forceinline__ unsigned int u_element_tx(int ntx, int mode, float2 g, const float2* Sm,
+__device__ __forceinline__ unsigned int u_element_tx(int ntx, int mode, float2 g, const float2* Sm, const float2* Mg,
                                                      const float2* grid, int W, int C, int w, int c, float s2,
                                                      const QamDemapTable& qt, const uint32_t* bitsm, int BW,
                                                      int64_t wofs, int64_t k, int m, bool& fin) {
   switch (ntx) {
-    case 1: return u_element<NRX, 1>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
-    case 2: return u_element<NRX, 2>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
+    case 1: return u_element<NRX, 1>(mode, g, Sm, Mg, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
+    case 2: return u_element<NRX, 2>(mode, g, Sm, Mg, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
     case 4:
-      if constexpr (MAXA >= 4) return u_element<NRX, 4>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
+      if constexpr (MAXA >= 4) return u_element<NRX, 4>(mode, g, Sm, Mg, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
       else return 0u;
     default:
-      if constexpr (MAXA >= 8) return u_element<NRX, 8>(mode, g, Sm, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
+      if constexpr (MAXA >= 8) return u_element<NRX, 8>(mode, g, Sm, Mg, grid, W, C, w, c, s2, qt, bitsm, BW, wofs, k, m, fin);
       else return 0u;  // not reached: the batch's kernel covers its largest antenna count
   }
 }
@@ -392,8 +397,16 @@ __device__ __forceinline__ unsigned int u_element_tx(int ntx, int mode, float2 g
 // elements had a non-finite equalizer pivot.
 template <int MAXA>
 __device__ unsigned int u_detect(const UDrop& d, const UFrame& fr, const FadingConst& fc, const int64_t* Wp,
-                                 const int64_t* P0, const float2* Sm, const int* dl, const float2* grid, float s2,
-                                 const QamDemapTable& qt, uint64_t seed, int64_t drop, unsigned char* sm, bool& fin) {
+                                 const int64_t* P0, const float2* Sm, float2* Mg, const int* dl, const float2* grid,
+                                 float s2, const QamDemapTable& qt, uint64_t seed, int64_t drop, unsigned char* sm,
+                                 bool& fin) {
+  // M = S^H S of the drop's spatial response (visible after the first word's tap averages)
+  for (int q = threadIdx.x; q < d.ntx * d.ntx; q += blockDim.x) {
+    const int i = q / d.ntx, j = q - i * d.ntx;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int r = 0; r < d.nrx; ++r) cfmac(acc, Sm[r * d.ntx + i], Sm[r * d.ntx + j]);
+    Mg[q] = acc;
+  }
   float2* hb = reinterpret_cast<float2*>(sm);
   float2* scratch = hb + d.L;
   uint32_t* bitsm = reinterpret_cast<uint32_t*>(scratch + d.L * fc.S1);
@@ -420,13 +433,13 @@ __device__ unsigned int u_detect(const UDrop& d, const UFrame& fr, const FadingC
       const float2 g = tap_response(fc, hb, dl, fr.twiddle, fr.bins[j], fr.N);
       const int64_t k = k0 + j;
       switch (d.nrx) {
-        case 1: local += u_element_tx<1, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
-        case 2: local += u_element_tx<2, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
+        case 1: local += u_element_tx<1, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, Mg, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
+        case 2: local += u_element_tx<2, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, Mg, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin); break;
         case 4:
-          if constexpr (MAXA >= 4) local += u_element_tx<4, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin);
+          if constexpr (MAXA >= 4) local += u_element_tx<4, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, Mg, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin);
           break;
         default:
-          if constexpr (MAXA >= 8) local += u_element_tx<8, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin);
+          if constexpr (MAXA >= 8) local += u_element_tx<8, MAXA>(d.ntx, HPX_EQ_LMMSE, g, Sm, Mg, grid, fr.W, fr.C, w, j, s2, qt, bitsm, BW, wofs, k, fr.m, fin);
           break;
       }
     }
@@ -447,7 +460,8 @@ __global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __
   unsigned char* base = reinterpret_cast<unsigned char*>(smem4);
   int* dl = reinterpret_cast<int*>(base);                      // [64] tap delays
   float2* Sm = reinterpret_cast<float2*>(base + 256);          // [64] spatial
-  unsigned char* work = base + 256 + 64 * sizeof(float2);      // stage union
+  float2* Mg = Sm + 64;                                        // [64] S^H S
+  unsigned char* work = base + 256 + 128 * sizeof(float2);     // stage union
   unsigned char* slot = a.scratch + (size_t)blockIdx.x * a.slot_bytes;
   for (;;) {
     if (threadIdx.x == 0) {
@@ -497,7 +511,7 @@ __global__ void __launch_bounds__(UMAX_THREADS, MINB) k_uneven(UArgs a, const __
       default: u_rx<2048>(fr, d.nrx, fr.T + d.D, y, grid, work); break;
     }
     bool fin = finite_f(np);  // a NaN / inf noise power is an invalid drop too
-    const unsigned int e = u_detect<MAXA>(d, fr, fc, Wp, P0, Sm, dl, grid, np, qts.t[fr.m], a.seed, drop, work, fin);
+    const unsigned int e = u_detect<MAXA>(d, fr, fc, Wp, P0, Sm, Mg, dl, grid, np, qts.t[fr.m], a.seed, drop, work, fin);
     // drop total
     unsigned int v = e;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -743,7 +757,7 @@ hpx_status hpx_uneven_create(const hpx_uneven_drop* drops, int32_t num_drops, do
   u->off_y = u->off_x + round_up(max_x);
   u->off_grid = u->off_y + round_up(max_y);
   u->slot_bytes = u->off_grid + round_up(max_grid);
-  u->smem = 256 + 64 * sizeof(float2) + max_smem + 16;
+  u->smem = 256 + 128 * sizeof(float2) + max_smem + 16;
   u->max_slots = max_slots;
   std::vector<int32_t> order(num_drops);
   std::iota(order.begin(), order.end(), 0);
