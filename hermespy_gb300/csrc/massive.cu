@@ -1,22 +1,25 @@
-// Massive-MIMO receiver: matched filter on the BF16 tensor cores with split (3-term)
-// products, FP32 Cholesky LMMSE / ZF, FP64 only for the elements whose Cholesky
-// condition estimate exceeds 1e4, exact hard demap and bit-error count. No counterpart
-// in the reference (its MIMO equalizer is a per-element numpy pinv,
-// modem/waveform.py:235-250, limited to small arrays).
+// Massive-MIMO receiver: per-element Gram and matched filter on the BF16 tensor
+// cores with split (3-term) products, FP32 Cholesky LMMSE / ZF, FP64 only for the
+// elements whose Cholesky condition estimate exceeds 1e6, exact hard demap and
+// bit-error count. No counterpart in the reference (its MIMO equalizer is a
+// per-element numpy pinv, modem/waveform.py:235-250, limited to small arrays).
 //
-// The ideal channel of an element is H = g S: the drop's spatial matrix S (NRX x 16)
-// times the element's tap response g. So H^H H = |g|^2 M with M = S^H S, formed once per
-// block (FP32), and H^H y = conj(g) S^H y. Per element only S^H y is a product with
-// NRX terms:
-//   P = [Re S; Im S] (2 NRX x 16), Y = [[Re y, Im y]; [Im y, -Re y]],  S^H y = P^T Y
-// (K = 2 NRX). P is split P = P_hi + P_lo into two BF16 numbers once per warp, Y per
-// element, and P^T Y keeps all four products (Y_hi and Y_lo sit side by side in one
-// 8-column B tile, two MMAs per k-step) with FP32 accumulation (mma.sync m16n8k16).
-// Each half-warp then factors |g|^2 M + reg I for one element with its 16 rows in
-// registers (lane i holds row i; packed FP32x2 updates), solves (forward substitution
-// on rows, backward on columns after a transpose through shared memory), demaps its 16
-// streams and counts errors against the Philox bits, regenerated per element. The FP64
-// re-solve of ill-conditioned elements forms their Gram from H itself.
+// Per resource element with H (NRX x 16) and y (NRX):
+//   P = [Re H; Im H] (2 NRX x 16), Q = [Im H; -Re H], Y = [[Re y, Im y]; [Im y, -Re y]]
+//   Re(H^H H) = P^T P,  Im(H^H H) = P^T Q,  H^H y = P^T Y   (K = 2 NRX real GEMMs)
+// Every operand is split X = X_hi + X_lo into two BF16 numbers and each Gram product
+// is X_hi Y_hi + X_hi Y_lo + X_lo Y_hi with FP32 accumulation (mma.sync m16n8k16): the
+// dropped X_lo Y_lo term is below 2^-16 of the product. The matched filter keeps all
+// four terms: Y_hi and Y_lo sit side by side in one 8-column B tile, so two MMAs per
+// k-step give them.
+// The warp computes the Gram of two elements, then each half-warp factors one of
+// them with its 16 rows in registers (lane i holds row i; packed FP32x2 updates),
+// solves (forward substitution on rows, backward on columns after a transpose through
+// shared memory), demaps its 16 streams and counts errors against the Philox bits,
+// regenerated per element.
+// The split operands are built per element from the channel h = g S (tap response g
+// of the element, spatial matrix S of the drop): each lane forms 8 columns of one row,
+// converts them two at a time (BF16x2 and its residual) and writes 16-byte chunks.
 #include <cuda_bf16.h>
 
 #include "fading_dev.cuh"
@@ -25,7 +28,7 @@ namespace {
 
 constexpr int MT = 16;       // transmit streams (users)
 constexpr int MWARPS = 4;
-constexpr float kCondLimit = 1e4f;  // FP32 solves stay within ~1e-3 relative below it
+constexpr float kCondLimit = 1e6f;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -45,6 +48,16 @@ __device__ __forceinline__ void mma16816(float (&c)[4], uint32_t a0, uint32_t a1
       : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
+
+// 3-term split product accumulate: c += Ahi Bhi + Ahi Blo + Alo Bhi
+__device__ __forceinline__ void mma3(float (&c)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4], uint32_t bh0,
+                                     uint32_t bh1, uint32_t bl0, uint32_t bl1) {
+  mma16816(c, ah[0], ah[1], ah[2], ah[3], bh0, bh1);
+  mma16816(c, ah[0], ah[1], ah[2], ah[3], bl0, bl1);
+  mma16816(c, al[0], al[1], al[2], al[3], bh0, bh1);
+}
+
+__device__ __forceinline__ uint32_t neg2(uint32_t v) { return v ^ 0x80008000u; }
 
 // Byte offset of element (row, col) of a [rows][16] bf16 tile whose two 16-byte
 // halves swap on every other group of 4 rows (conflict-free 8-row ldmatrix).
@@ -134,10 +147,10 @@ __device__ __forceinline__ void split2_bf16(float2 v, uint32_t& hi, uint32_t& lo
   memcpy(&lo, &l, sizeof(lo));
 }
 
-// Per-warp shared memory: [P_hi | P_lo] of S (borrowed for the FP64 Gram of an
-// ill-conditioned element, then rebuilt), Y [KR][8] (16-byte rows: columns 0-1 hi, 2-3
-// lo, 4-7 zero), G[2][16][17] (rows padded: a half-warp reading one row per lane hits
-// distinct banks; transposes L), b[2][16], x[2][16] (FP64-path results),
+// Per-warp shared memory: [P_hi | P_lo] (reused for the FP64 Gram of the two elements
+// once the FP32 ones are formed), Y [KR][8] (16-byte rows: columns 0-1 hi, 2-3 lo,
+// 4-7 zero), G[2][16][17] (rows padded: a half-warp reading one row per lane hits
+// distinct banks; reused to transpose L), b[2][16], x[2][16] (FP64-path results),
 // Cholesky column broadcast [2][16] as (re, re, im, im) (reused for the FP64 matched
 // filter), g[2], column[2].
 template <int NRX>
@@ -167,10 +180,9 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
   extern __shared__ float4 smem4[];
   const int w = blockIdx.x, b = blockIdx.y;
   unsigned char* base = reinterpret_cast<unsigned char*>(smem4);
-  // [NRX][SMF] spatial matrix (16-byte aligned rows), M = S^H S [16][17], then taps
+  // [NRX][SMF] spatial matrix (16-byte aligned rows), then taps
   float* Sm = reinterpret_cast<float*>(base + MWARPS * SM::WARP_BYTES);
-  float2* Ms = reinterpret_cast<float2*>(Sm + NRX * SMF);
-  float2* hb = Ms + MT * (MT + 1);
+  float2* hb = reinterpret_cast<float2*>(Sm + NRX * SMF);
   float2* scratch = hb + fc.L;
   int* ds = reinterpret_cast<int*>(scratch + fc.L * fc.S1);
 
@@ -196,42 +208,9 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
     Sm[(i / MT) * SMF + i % MT] = sv.x;
     Sm[(i / MT) * SMF + MT + i % MT] = sv.y;
   }
-  for (int q = threadIdx.x; q < MT * MT; q += blockDim.x) {  // M = S^H S (visible after the tap averages)
-    const int i = q / MT, j = q - i * MT;
-    float2 acc = make_float2(0.f, 0.f);
-    for (int r = 0; r < NRX; ++r) cfmac(acc, Sg[r * MT + i], Sg[r * MT + j]);
-    Ms[i * (MT + 1) + j] = acc;
-  }
   // zero the Y tile once: only columns 0-3 change per element
   for (int i = lane; i < KR * 4; i += 32) reinterpret_cast<uint32_t*>(Yt)[i] = 0u;
   tap_averages(fc, v.W(b), v.P0(b), window_start[w], N, hb, scratch);  // ends with __syncthreads
-  // P tiles of S (the warp's A operand for every element): item = (row r, 8-column
-  // half cb); rows r (Re S) and NRX + r (Im S). Built again after an FP64 re-solve,
-  // which borrows their space.
-  auto build_ps = [&]() {
-#pragma unroll
-    for (int it = lane; it < 2 * NRX; it += 32) {
-      const int r = it >> 1, cb = it & 1;
-      const float4* rp = reinterpret_cast<const float4*>(Sm + r * SMF + cb * 8);
-      const float4* ip = reinterpret_cast<const float4*>(Sm + r * SMF + MT + cb * 8);
-      uint4 rh, rl, ih, il;
-      const float4 sr0 = rp[0], sr1 = rp[1], si0 = ip[0], si1 = ip[1];
-      split2_bf16(make_float2(sr0.x, sr0.y), rh.x, rl.x);
-      split2_bf16(make_float2(sr0.z, sr0.w), rh.y, rl.y);
-      split2_bf16(make_float2(sr1.x, sr1.y), rh.z, rl.z);
-      split2_bf16(make_float2(sr1.z, sr1.w), rh.w, rl.w);
-      split2_bf16(make_float2(si0.x, si0.y), ih.x, il.x);
-      split2_bf16(make_float2(si0.z, si0.w), ih.y, il.y);
-      split2_bf16(make_float2(si1.x, si1.y), ih.z, il.z);
-      split2_bf16(make_float2(si1.z, si1.w), ih.w, il.w);
-      *reinterpret_cast<uint4*>(Phi + toff(r, cb * 8)) = rh;
-      *reinterpret_cast<uint4*>(Plo + toff(r, cb * 8)) = rl;
-      *reinterpret_cast<uint4*>(Phi + toff(NRX + r, cb * 8)) = ih;
-      *reinterpret_cast<uint4*>(Plo + toff(NRX + r, cb * 8)) = il;
-    }
-    __syncwarp();
-  };
-  build_ps();
   const float s2 = nv ? nv[b] : 0.0f;
   const float reg = mode == HPX_EQ_LMMSE ? s2 : 0.0f;
   const uint32_t phi = smem_u32(Phi), plo = smem_u32(Plo), yt = smem_u32(Yt);
@@ -281,13 +260,48 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
       const int j = j0 + s;
+      float2* G = Gs + s * MT * GS;
       float2* bv = bs + s * MT;
-      if (j >= nd) {  // no element: zero right-hand side (an identity system below)
+      if (j >= nd) {  // no element: an identity system keeps the half-warp's arithmetic finite
+        for (int i = lane; i < MT * MT; i += 32) G[(i / MT) * GS + i % MT] = make_float2((i % (MT + 1)) == 0 ? 1.f : 0.f, 0.f);
         if (lane < MT) bv[lane] = make_float2(0.f, 0.f);
         __syncwarp();
         continue;
       }
       const float gx = __shfl_sync(0xffffffffu, gh.x, 16 * s), gy = __shfl_sync(0xffffffffu, gh.y, 16 * s);
+      const float2 gx2 = make_float2(gx, gx), gy2 = make_float2(gy, gy), ngy2 = make_float2(-gy, -gy);
+      // P tiles: item = (row r, 8-column half cb); rows r (Re H) and NRX + r (Im H). Two
+      // columns per packed FMA: Re h = Re s gx - Im s gy, Im h = Re s gy + Im s gx.
+#pragma unroll
+      for (int it = lane; it < 2 * NRX; it += 32) {
+        const int r = it >> 1, cb = it & 1;
+        const float4* rp = reinterpret_cast<const float4*>(Sm + r * SMF + cb * 8);
+        const float4* ip = reinterpret_cast<const float4*>(Sm + r * SMF + MT + cb * 8);
+        float2 hr[4], hi[4];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const float4 sr = rp[q], si = ip[q];
+          const float2 sr0 = make_float2(sr.x, sr.y), sr1 = make_float2(sr.z, sr.w);
+          const float2 si0 = make_float2(si.x, si.y), si1 = make_float2(si.z, si.w);
+          hr[2 * q] = __ffma2_rn(si0, ngy2, __fmul2_rn(sr0, gx2));
+          hr[2 * q + 1] = __ffma2_rn(si1, ngy2, __fmul2_rn(sr1, gx2));
+          hi[2 * q] = __ffma2_rn(si0, gx2, __fmul2_rn(sr0, gy2));
+          hi[2 * q + 1] = __ffma2_rn(si1, gx2, __fmul2_rn(sr1, gy2));
+        }
+        uint4 rh, rl, ih, il;
+        split2_bf16(hr[0], rh.x, rl.x);
+        split2_bf16(hr[1], rh.y, rl.y);
+        split2_bf16(hr[2], rh.z, rl.z);
+        split2_bf16(hr[3], rh.w, rl.w);
+        split2_bf16(hi[0], ih.x, il.x);
+        split2_bf16(hi[1], ih.y, il.y);
+        split2_bf16(hi[2], ih.z, il.z);
+        split2_bf16(hi[3], ih.w, il.w);
+        *reinterpret_cast<uint4*>(Phi + toff(r, cb * 8)) = rh;
+        *reinterpret_cast<uint4*>(Plo + toff(r, cb * 8)) = rl;
+        *reinterpret_cast<uint4*>(Phi + toff(NRX + r, cb * 8)) = ih;
+        *reinterpret_cast<uint4*>(Plo + toff(NRX + r, cb * 8)) = il;
+      }
       // Y tile: row r = [Re y, Im y], row NRX + r = [Im y, -Re y]; hi in columns 0-1, lo in 2-3
 #pragma unroll
       for (int q = 0; q < YR; ++q) {
@@ -301,35 +315,68 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
         *reinterpret_cast<uint2*>(Yt + (NRX + r) * 16) = make_uint2(h1, l1);
       }
       __syncwarp();
-      float by[4] = {};
+      float gr[2][4] = {}, gi[2][4] = {}, by[4] = {};
 #pragma unroll
       for (int ks = 0; ks < KS / 2; ++ks) {
         const int ks2 = ks + KS / 2;
+        // A = P^T fragments of k-steps ks (rows of Re H) and ks2 (rows of Im H)
+        // and the same matrices in B order (a0, a2, a1, a3): the B pair of n-tile nt is
+        // registers 2 nt, 2 nt + 1 of it, consecutive as the MMA wants them
+        uint32_t bh[2][4], bl[2][4];
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+          const int kk = p == 0 ? ks : ks2;
+          const int rb = kk * 16 + (j8 & 1) * 8 + r8, cb2 = (j8 >> 1) * 8;
+          ldsm_x4_t(phi + toff(rb, cb2), bh[p][0], bh[p][1], bh[p][2], bh[p][3]);
+          ldsm_x4_t(plo + toff(rb, cb2), bl[p][0], bl[p][1], bl[p][2], bl[p][3]);
+        }
         // Y fragments of both k-steps: matrices (ks, k 0-7), (ks, k 8-15), (ks2, k 0-7), (ks2, k 8-15)
         uint32_t yf[4];
         ldsm_x4_t(yt + ((j8 >> 1 ? ks2 : ks) * 16 + (j8 & 1) * 8 + r8) * 16, yf[0], yf[1], yf[2], yf[3]);
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
-          uint32_t ah[4], al[4];  // A = P^T fragments of k-step ks (rows of Re S) or ks2 (rows of Im S)
+          uint32_t ah[4], al[4];  // A order, loaded per k-step to keep registers down
           {
             const int rr = (p == 0 ? ks : ks2) * 16 + (j8 >> 1) * 8 + r8, cc = (j8 & 1) * 8;
             ldsm_x4_t(phi + toff(rr, cc), ah[0], ah[1], ah[2], ah[3]);
             ldsm_x4_t(plo + toff(rr, cc), al[0], al[1], al[2], al[3]);
           }
-          // (P_hi + P_lo)^T [Y_hi | Y_lo], the lo half summed in below
+          // B = P fragments of the same k-step (B order), Q those of the partner k-step
+          const int q = 1 - p;  // Q = [Im H; -Re H]: the partner k-step, negated in the lower half
+#pragma unroll
+          for (int nt = 0; nt < 2; ++nt) {
+            mma3(gr[nt], ah, al, bh[p][2 * nt], bh[p][2 * nt + 1], bl[p][2 * nt], bl[p][2 * nt + 1]);
+            uint32_t qh0 = bh[q][2 * nt], qh1 = bh[q][2 * nt + 1], ql0 = bl[q][2 * nt], ql1 = bl[q][2 * nt + 1];
+            if (p == 1) {
+              qh0 = neg2(qh0);
+              qh1 = neg2(qh1);
+              ql0 = neg2(ql0);
+              ql1 = neg2(ql1);
+            }
+            mma3(gi[nt], ah, al, qh0, qh1, ql0, ql1);
+          }
+          // matched filter: (P_hi + P_lo)^T [Y_hi | Y_lo], the lo half summed in below
           mma16816(by, ah[0], ah[1], ah[2], ah[3], yf[2 * p], yf[2 * p + 1]);
           mma16816(by, al[0], al[1], al[2], al[3], yf[2 * p], yf[2 * p + 1]);
         }
       }
-      const int gm = lane >> 2;
-      // S^H y: columns 0-1 (Y_hi) of lanes 4i plus columns 2-3 (Y_lo) of lanes 4i + 1;
-      // H^H y = conj(g) S^H y
+      // C fragments: rows lane/4 (+8), columns 2 (lane % 4) (+1) of each 8-column tile
+      const int gm = lane >> 2, gn = (lane & 3) * 2;
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+        for (int hr = 0; hr < 2; ++hr)
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const int i = gm + hr * 8, jj = nt * 8 + gn + e;
+            G[i * GS + jj] = make_float2(gr[nt][hr * 2 + e], gi[nt][hr * 2 + e]);
+          }
+      // H^H y: columns 0-1 (Y_hi) of lanes 4i plus columns 2-3 (Y_lo) of lanes 4i + 1
 #pragma unroll
       for (int e = 0; e < 4; ++e) by[e] += __shfl_down_sync(0xffffffffu, by[e], 1);
       if ((lane & 3) == 0) {
-        const float2 g = make_float2(gx, gy);
-        bv[gm] = cmulc(g, make_float2(by[0], by[1]));
-        bv[gm + 8] = cmulc(g, make_float2(by[2], by[3]));
+        bv[gm] = make_float2(by[0], by[1]);
+        bv[gm + 8] = make_float2(by[2], by[3]);
       }
       __syncwarp();
     }
@@ -340,12 +387,10 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
     float2* G = Gs + half * MT * GS;
     float4* col = colb + half * MT;
     float2 a[MT];
-    const float2 gme = gsave[half];
-    const float g2 = valid ? fmaf(gme.x, gme.x, gme.y * gme.y) : 0.0f;  // |g|^2 (no element: identity)
 #pragma unroll
     for (int jj = 0; jj < MT; ++jj) {
-      a[jj] = cscale(Ms[row * GS + jj], g2);
-      if (jj == row) a[jj] = make_float2(valid ? a[jj].x + reg : 1.0f, 0.f);  // compile-time index: a[] stays in registers
+      a[jj] = G[row * GS + jj];
+      if (jj == row) a[jj] = make_float2(a[jj].x + reg, 0.f);  // compile-time index: a[] stays in registers
     }
     float2 bi = bs[half * MT + row];
     float pmin = INFINITY, pmax = 0.f, inv_i = 0.f;
@@ -406,7 +451,7 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
       acc = cadd(acc, cmulc(a[p], xp));  // L[p][i] = 0 for i > p; lane p's sum is not read after step p
     }
     __syncwarp();  // G reads done before the next element pair's Gram
-    const bool cond_bad = !ok || pmax * pmax > kCondLimit * pmin * pmin;  // (pmax / pmin)^2 > 1e4
+    const bool cond_bad = !ok || pmax * pmax > kCondLimit * pmin * pmin;  // (pmax / pmin)^2 > 1e6
     const unsigned need = __ballot_sync(0xffffffffu, valid && cond_bad && row == 0);
     if (need) {
       // FP64 Gram and matched filter of the flagged elements from their channel
@@ -446,7 +491,6 @@ __global__ void __launch_bounds__(MWARPS * 32, 3) k_detect_massive(
       __syncwarp();
       if (mine) xi = xs[half * MT + row];
       n64 += (row == 0 && mine) ? 1u : 0u;
-      build_ps();  // the FP64 Gram borrowed the P tiles' space
     }
     if (valid) {
       bad = bad || !(fabsf(xi.x) < INFINITY && fabsf(xi.y) < INFINITY);
@@ -480,8 +524,7 @@ hpx_status launch_massive(const hpx_fading* f, const void* state, const hpx_fram
   const FadingConst fc = fading_const(f);
   const int C = fr->info.num_columns, m = fr->info.bits_per_symbol;
   const size_t smem = (size_t)MWARPS * MassiveSmem<NRX>::WARP_BYTES + (size_t)NRX * SMF * sizeof(float) +
-                      (size_t)MT * (MT + 1) * sizeof(float2) + (size_t)fc.L * sizeof(float2) * (1 + fc.S1) +
-                      (size_t)fc.L * sizeof(int);
+                      (size_t)fc.L * sizeof(float2) * (1 + fc.S1) + (size_t)fc.L * sizeof(int);
   if (smem > 220 * 1024) return hpx_fail(HPX_ERR_UNSUPPORTED, "detect_massive: frame needs %zu bytes of shared memory", smem);
   auto kern = k_detect_massive<NRX>;
   HPX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
